@@ -1,0 +1,261 @@
+"""ctypes binding of the C ABI (include/bem2d_gpu.h) for tests and the bench.
+
+Loads bem2d_gb300/libbem2d_gpu.so and fails loudly if it is missing or if no
+GPU is present: there is no CPU fallback.  Arrays may be numpy (host) or
+torch CUDA tensors (device); the library takes either.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import geometry as G
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libbem2d_gpu.so")
+
+OK = 0
+ERR = {-1: "ARG", -2: "CUDA", -3: "NOMEM", -4: "NONFINITE", -5: "NOCONV",
+       -6: "TIMEOUT", -7: "UNSUPPORTED"}
+KERNEL = {"single": 0, "double": 1, "conjdouble": 2, "combined": 3}
+FUN = {"planewave": 0, "normalplanewave": 1, "combinedplanewave": 2}
+PREC = {"fp64": 0, "mixed": 1}
+
+# symbols declared in include/bem2d_gpu.h
+EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
+           "bem2d_ctx_stream", "bem2d_ctx_set_stream", "bem2d_ctx_launch_count",
+           "bem2d_gauss", "bem2d_discrete_kernel", "bem2d_eval_ident",
+           "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
+           "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer"]
+
+
+class Bem2dError(RuntimeError):
+    def __init__(self, code, msg):
+        self.code = code
+        super().__init__("bem2d_gpu error %d (%s): %s" % (code, ERR.get(code, "INFO"), msg))
+
+
+class LapackError(Bem2dError):
+    """A zero pivot (the reference throws LapackError)."""
+
+
+class Geometry_c(ctypes.Structure):
+    _fields_ = [("n_elem", ctypes.c_int32),
+                ("kind", ctypes.c_void_p), ("param", ctypes.c_void_p),
+                ("index", ctypes.c_void_p), ("next", ctypes.c_void_p),
+                ("prev", ctypes.c_void_p),
+                ("n_unk", ctypes.c_int32),
+                ("unk_elem", ctypes.c_void_p), ("unk_kind", ctypes.c_void_p),
+                ("unk_param", ctypes.c_void_p)]
+
+
+class Quad_c(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32), ("N", ctypes.c_int32), ("sigma", ctypes.c_double)]
+
+
+class SolveInfo_c(ctypes.Structure):
+    _fields_ = [("info", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("residual", ctypes.c_double)]
+
+
+_LIB = None
+
+
+def load():
+    """Load the CUDA library (raises if it is not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libbem2d_gpu.so is not built; run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = ctypes.CDLL(LIB_PATH)
+        vp, i32, i64, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+        lib.bem2d_ctx_create.argtypes = [i32, ctypes.POINTER(vp)]
+        lib.bem2d_ctx_destroy.argtypes = [vp]
+        lib.bem2d_ctx_destroy.restype = None
+        lib.bem2d_ctx_last_error.argtypes = [vp]
+        lib.bem2d_ctx_last_error.restype = ctypes.c_char_p
+        lib.bem2d_ctx_stream.argtypes = [vp]
+        lib.bem2d_ctx_stream.restype = vp
+        lib.bem2d_ctx_set_stream.argtypes = [vp, vp]
+        lib.bem2d_ctx_launch_count.argtypes = [vp]
+        lib.bem2d_ctx_launch_count.restype = i64
+        lib.bem2d_gauss.argtypes = [i32, vp, vp]
+        lib.bem2d_discrete_kernel.argtypes = [vp, vp, vp, i32, d, d, d, d, d, vp, i64]
+        lib.bem2d_eval_ident.argtypes = [vp, vp, vp, vp, i64]
+        lib.bem2d_dot_prod_basfuns.argtypes = [vp, vp, vp, i32, d, d, d, d, d, d, vp]
+        lib.bem2d_solve_system.argtypes = [vp, i32, vp, i64, vp, vp, i32, d, vp]
+        lib.bem2d_scattering_solve.argtypes = [vp, vp, vp, d, d, d, d, d, i32, d, vp, vp]
+        lib.bem2d_fma_peak.argtypes = [i32, ctypes.POINTER(d)]
+        lib.bem2d_ctx_enable_timers.argtypes = [vp, i32]
+        lib.bem2d_ctx_timer.argtypes = [vp, i32, ctypes.POINTER(d), ctypes.POINTER(i64)]
+        _LIB = lib
+    return _LIB
+
+
+def _ptr(a):
+    """Raw address of a numpy array or a torch tensor."""
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class _GeomHold:
+    """A C geometry struct that keeps its arrays alive."""
+
+    def __init__(self, g):
+        a = g.arrays() if isinstance(g, G.Geometry) else g
+        self.arrays = a
+        self.c = Geometry_c(len(a["kind"]), a["kind"].ctypes.data, a["param"].ctypes.data,
+                            a["index"].ctypes.data, a["next"].ctypes.data,
+                            a["prev"].ctypes.data, len(a["unk_elem"]),
+                            a["unk_elem"].ctypes.data, a["unk_kind"].ctypes.data,
+                            a["unk_param"].ctypes.data)
+        self.n = len(a["unk_elem"])
+
+
+def quad(q=(3, 5, 0.15)):
+    return Quad_c(int(q[0]), int(q[1]), float(q[2]))
+
+
+class Context:
+    """One bem2d_ctx (device workspace + stream)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.bem2d_ctx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise Bem2dError(rc, "bem2d_ctx_create failed (no GPU?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bem2d_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc == 0:
+            return
+        msg = self.lib.bem2d_ctx_last_error(self.h).decode()
+        if rc > 0:
+            raise LapackError(rc, msg)
+        raise Bem2dError(rc, msg)
+
+    @property
+    def launches(self):
+        return int(self.lib.bem2d_ctx_launch_count(self.h))
+
+    @property
+    def stream(self):
+        return self.lib.bem2d_ctx_stream(self.h)
+
+    PHASES = ("far", "near", "lu", "solve")
+
+    def enable_timers(self, on=True):
+        self._check(self.lib.bem2d_ctx_enable_timers(self.h, 1 if on else 0))
+
+    def timers(self):
+        """{phase: (total ms, count)} since enable_timers()."""
+        out = {}
+        for i, name in enumerate(self.PHASES):
+            ms, n = ctypes.c_double(), ctypes.c_int64()
+            self._check(self.lib.bem2d_ctx_timer(self.h, i, ctypes.byref(ms), ctypes.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    # -- assembly ----------------------------------------------------------
+    def discrete_kernel(self, g, kernel="combined", k=10.0, eta=None, q=(3, 5, 0.15),
+                        alpha=1.0, beta=0.0, out=None):
+        gh = _GeomHold(g)
+        n = gh.n
+        if out is None:
+            out = np.zeros((n, n), dtype=np.complex128, order="F")
+        ld = n
+        if hasattr(out, "stride"):  # torch: column-major view, or row-major storage of A^T
+            ld = out.stride(1) if out.stride(0) == 1 else out.stride(0)
+        eta = float(k) if eta is None else float(eta)
+        qq = quad(q)
+        self._check(self.lib.bem2d_discrete_kernel(
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
+            eta, float(alpha), float(beta), _ptr(out), ld))
+        return out
+
+    def eval_ident(self, g, q=(3, 5, 0.15), out=None):
+        gh = _GeomHold(g)
+        n = gh.n
+        if out is None:
+            out = np.zeros((n, n), dtype=np.complex128, order="F")
+        qq = quad(q)
+        self._check(self.lib.bem2d_eval_ident(self.h, ctypes.byref(gh.c), ctypes.byref(qq),
+                                              _ptr(out), n))
+        return out
+
+    def rhs(self, g, k, direction, eta=None, q=(3, 5, 0.15), fun="combinedplanewave",
+            scale=2.0, out=None):
+        gh = _GeomHold(g)
+        if out is None:
+            out = np.zeros(gh.n, dtype=np.complex128)
+        eta = float(k) if eta is None else float(eta)
+        qq = quad(q)
+        self._check(self.lib.bem2d_dot_prod_basfuns(
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), FUN[fun], float(k), 0.0,
+            float(direction[0]), float(direction[1]), eta, float(scale), _ptr(out)))
+        return out
+
+    # -- solve -------------------------------------------------------------
+    def solve(self, A, b, precision="fp64", tol=0.0, out=None):
+        n = A.shape[0]
+        if out is None:
+            out = np.zeros(n, dtype=np.complex128)
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
+            b = np.ascontiguousarray(b, dtype=np.complex128)
+            lda = n
+        else:
+            lda = A.stride(1)
+        info = SolveInfo_c()
+        self._check(self.lib.bem2d_solve_system(self.h, n, _ptr(A), lda, _ptr(b), _ptr(out),
+                                                PREC[precision], float(tol), ctypes.byref(info)))
+        self.last_info = (info.info, info.iterations, info.residual)
+        return out
+
+    def scattering_solve(self, g, k, direction, eta=None, q=(3, 5, 0.15), precision="fp64",
+                         tol=0.0, out=None):
+        gh = _GeomHold(g)
+        if out is None:
+            out = np.zeros(gh.n, dtype=np.complex128)
+        eta = float(k) if eta is None else float(eta)
+        qq = quad(q)
+        info = SolveInfo_c()
+        self._check(self.lib.bem2d_scattering_solve(
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), float(k), 0.0, eta,
+            float(direction[0]), float(direction[1]), PREC[precision], float(tol), _ptr(out),
+            ctypes.byref(info)))
+        self.last_info = (info.info, info.iterations, info.residual)
+        return out
+
+
+def gauss(n):
+    lib = load()
+    x = np.zeros(n)
+    w = np.zeros(n)
+    rc = lib.bem2d_gauss(n, x.ctypes.data, w.ctypes.data)
+    if rc:
+        raise Bem2dError(rc, "bem2d_gauss")
+    return x, w
+
+
+def fma_peak(precision="fp64"):
+    """Measured FMA throughput (TFLOP/s) of the FP64 or FP32 pipe."""
+    lib = load()
+    v = ctypes.c_double()
+    rc = lib.bem2d_fma_peak(PREC[precision], ctypes.byref(v))
+    if rc:
+        raise Bem2dError(rc, "bem2d_fma_peak")
+    return v.value

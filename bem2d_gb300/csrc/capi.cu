@@ -1,0 +1,778 @@
+// C ABI of the bem2d GB300 path (include/bem2d_gpu.h): context, device
+// workspace, host-side geometry checks, quadrature rules, near-pair lists and
+// the orchestration of the assembly and solve kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+
+namespace bem2d_gpu {
+
+// ---------------------------------------------------------------------------
+// Context: one stream, a pool of named device buffers that only grow, and
+// cached quadrature rules.
+struct Buffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct RuleKey {
+  int L, N;
+  double sigma;
+  bool operator<(const RuleKey& o) const {
+    if (L != o.L) return L < o.L;
+    if (N != o.N) return N < o.N;
+    return sigma < o.sigma;
+  }
+};
+
+struct HostRules {
+  std::vector<double> gx, gw, r1, r2, r3;  // r*: (x, y, w) triplets
+};
+
+}  // namespace bem2d_gpu
+
+struct bem2d_ctx {
+  // per-phase event timers (measurement helpers)
+  bool timers = false;
+  double phase_ms[4] = {0, 0, 0, 0};
+  long long phase_n[4] = {0, 0, 0, 0};
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  long long launches = 0;
+  std::unordered_map<std::string, bem2d_gpu::Buffer> bufs;
+  std::map<bem2d_gpu::RuleKey, std::pair<void*, bem2d_gpu::DevRules>> rules;
+};
+
+namespace bem2d_gpu {
+
+static int fail(bem2d_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CUDA_TRY(ctx, expr)                                                        \
+  do {                                                                             \
+    cudaError_t e_ = (expr);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? BEM2D_ERR_NOMEM : BEM2D_ERR_CUDA, \
+                  "%s: %s", #expr, cudaGetErrorString(e_));                        \
+  } while (0)
+
+#define CHECK_LAUNCH(ctx)                                                          \
+  do {                                                                             \
+    cudaError_t e_ = cudaGetLastError();                                           \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(ctx, BEM2D_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+  } while (0)
+
+static void* ws(bem2d_ctx* c, const char* name, size_t bytes, int* rc) {
+  Buffer& b = c->bufs[name];
+  if (b.bytes >= bytes && b.ptr) return b.ptr;
+  if (b.ptr) cudaFree(b.ptr);
+  b.ptr = nullptr;
+  b.bytes = 0;
+  const size_t sz = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(&b.ptr, sz);
+  if (e != cudaSuccess) {
+    b.ptr = nullptr;
+    *rc = fail(c, BEM2D_ERR_NOMEM, "cudaMalloc(%zu) for %s: %s", sz, name, cudaGetErrorString(e));
+    return nullptr;
+  }
+  b.bytes = sz;
+  return b.ptr;
+}
+
+// Event pair around one phase when timers are on; resolved after a sync.
+static int tic(bem2d_ctx* c, int phase) {
+  if (!c->timers) return -1;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, c->stream);
+  c->pending.push_back(std::make_pair(phase, std::make_pair(a, b)));
+  return (int)c->pending.size() - 1;
+}
+static void toc(bem2d_ctx* c, int id) {
+  if (id >= 0) cudaEventRecord(c->pending[id].second.second, c->stream);
+}
+static void resolve_timers(bem2d_ctx* c) {
+  for (auto& p : c->pending) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+      c->phase_ms[p.first] += ms;
+      c->phase_n[p.first] += 1;
+    }
+    cudaEventDestroy(p.second.first);
+    cudaEventDestroy(p.second.second);
+  }
+  c->pending.clear();
+  cudaGetLastError();
+}
+
+static bool is_device_ptr(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Legendre rule on [0,1] by Newton iteration on P_n (nodes ascending,
+// weights summing to 1): the rule Gauss() builds by Golub-Welsch
+// (lib/bem2d_quadrature.cpp:10-56).
+static void gauss01(int n, double* x, double* w) {
+  if (n == 1) {
+    x[0] = 0.5;
+    w[0] = 1.0;
+    return;
+  }
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = std::cos(kPi * (i + 0.75) / (n + 0.5));
+    double dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      const double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-17) break;
+    }
+    // recompute the derivative at the converged node
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= n; ++k) {
+      const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    const double wt = 1.0 / ((1.0 - z * z) * dp * dp);  // = (2/((1-z^2)P'^2)) / 2
+    // z descends with i: node i from the right end, mirrored on the left
+    x[n - 1 - i] = 0.5 * (1.0 + z);
+    x[i] = 0.5 * (1.0 - z);
+    w[n - 1 - i] = wt;
+    w[i] = wt;
+  }
+}
+
+// Gauss2D::Rescale (lib/bem2d_quadpoints.cpp:52-73) appended to `out`.
+static void append_box(std::vector<double>& out, const std::vector<double>& gx,
+                       const std::vector<double>& gw, double a, double b, double c,
+                       double d) {
+  const int N = (int)gx.size();
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) {
+      out.push_back(a + (b - a) * gx[i]);
+      out.push_back(c + (d - c) * gx[j]);
+      out.push_back((b - a) * (d - c) * (gw[i] * gw[j]));
+    }
+}
+
+// AdaptedGauss1/2/3 (lib/bem2d_quadpoints.cpp:75-183).
+static HostRules make_rules(int L, int N, double sigma) {
+  HostRules r;
+  r.gx.resize(N);
+  r.gw.resize(N);
+  gauss01(N, r.gx.data(), r.gw.data());
+  std::vector<double> xl;
+  for (int i = 0; i < L; ++i) xl.push_back(std::pow(sigma, L - i));
+  xl.push_back(1.0);
+  for (int i = 0; i < L; ++i)
+    for (int j = 0; j < L; ++j) append_box(r.r1, r.gx, r.gw, xl[i], xl[i + 1], xl[j], xl[j + 1]);
+  {
+    double a = sigma, b = 1;
+    for (int l = L; l > 0; --l) {
+      append_box(r.r2, r.gx, r.gw, 0, a, 1 - b, 1 - a);
+      append_box(r.r2, r.gx, r.gw, a, b, 1 - b, 1 - a);
+      append_box(r.r2, r.gx, r.gw, a, b, 1 - a, 1);
+      a *= sigma;
+      b *= sigma;
+    }
+  }
+  {
+    double a = 1, b = sigma;
+    for (int l = L; l > 0; --l) {
+      append_box(r.r3, r.gx, r.gw, 1 - a, 1 - b, 0, b);
+      append_box(r.r3, r.gx, r.gw, 1 - a, 1 - b, b, a);
+      append_box(r.r3, r.gx, r.gw, 1 - b, 1, b, a);
+      a *= sigma;
+      b *= sigma;
+    }
+  }
+  return r;
+}
+
+static int get_rules(bem2d_ctx* c, const bem2d_quad* q, DevRules* out) {
+  const RuleKey key{q->L, q->N, q->sigma};
+  auto it = c->rules.find(key);
+  if (it != c->rules.end()) {
+    *out = it->second.second;
+    return BEM2D_OK;
+  }
+  const HostRules h = make_rules(q->L, q->N, q->sigma);
+  std::vector<double> all;
+  all.insert(all.end(), h.gx.begin(), h.gx.end());
+  all.insert(all.end(), h.gw.begin(), h.gw.end());
+  all.insert(all.end(), h.r1.begin(), h.r1.end());
+  all.insert(all.end(), h.r2.begin(), h.r2.end());
+  all.insert(all.end(), h.r3.begin(), h.r3.end());
+  void* d = nullptr;
+  CUDA_TRY(c, cudaMalloc(&d, sizeof(double) * std::max<size_t>(all.size(), 1)));
+  CUDA_TRY(c, cudaMemcpy(d, all.data(), sizeof(double) * all.size(), cudaMemcpyHostToDevice));
+  const double* p = static_cast<const double*>(d);
+  DevRules r;
+  r.ng = q->N;
+  r.gx = p;
+  r.gw = p + q->N;
+  r.r1 = p + 2 * q->N;
+  r.n1 = (int)h.r1.size() / 3;
+  r.r2 = r.r1 + h.r1.size();
+  r.n2 = (int)h.r2.size() / 3;
+  r.r3 = r.r2 + h.r2.size();
+  r.n3 = (int)h.r3.size() / 3;
+  c->rules[key] = std::make_pair(d, r);
+  *out = r;
+  return BEM2D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side validation, upload, near-pair list and node table of a geometry.
+struct Staged {
+  DevGeom g;
+  DevRules r;
+  NodeTable t;
+  NearPair* pairs;
+  int npairs;
+};
+
+static int check_quad(bem2d_ctx* c, const bem2d_quad* q) {
+  if (!q) return fail(c, BEM2D_ERR_ARG, "quad is NULL");
+  if (q->N < 1 || q->N > 64) return fail(c, BEM2D_ERR_ARG, "QuadOption.N=%d out of [1,64]", q->N);
+  if (q->L < 0 || q->L > 64) return fail(c, BEM2D_ERR_ARG, "QuadOption.L=%d out of [0,64]", q->L);
+  if (q->L > 0 && !(q->sigma > 0.0 && q->sigma < 1.0))
+    return fail(c, BEM2D_ERR_ARG, "QuadOption.sigma=%g not in (0,1)", q->sigma);
+  return BEM2D_OK;
+}
+
+static int check_geom(bem2d_ctx* c, const bem2d_geometry* g) {
+  if (!g) return fail(c, BEM2D_ERR_ARG, "geometry is NULL");
+  if (g->n_elem < 1 || g->n_unk < 1)
+    return fail(c, BEM2D_ERR_ARG, "empty geometry (n_elem=%d, n_unk=%d)", g->n_elem, g->n_unk);
+  if (!g->kind || !g->param || !g->index || !g->next || !g->prev || !g->unk_elem ||
+      !g->unk_kind || !g->unk_param)
+    return fail(c, BEM2D_ERR_ARG, "geometry has a NULL table");
+  for (int e = 0; e < g->n_elem; ++e)
+    if (g->kind[e] < BEM2D_ELEM_SEGMENT || g->kind[e] > BEM2D_ELEM_INVELLIPSE)
+      return fail(c, BEM2D_ERR_UNSUPPORTED, "element %d has unknown kind %d", e, g->kind[e]);
+  for (int u = 0; u < g->n_unk; ++u) {
+    if (g->unk_elem[u] < 0 || g->unk_elem[u] >= g->n_elem)
+      return fail(c, BEM2D_ERR_ARG, "unknown %d refers to element %d", u, g->unk_elem[u]);
+    if (g->unk_kind[u] == BEM2D_BASIS_POLY) {
+      const double d = g->unk_param[u];
+      if (!(d >= 0 && d <= 64 && d == std::floor(d)))
+        return fail(c, BEM2D_ERR_ARG, "unknown %d: polynomial degree %g", u, d);
+    } else if (g->unk_kind[u] != BEM2D_BASIS_LIN) {
+      return fail(c, BEM2D_ERR_UNSUPPORTED, "unknown %d has basis kind %d", u, g->unk_kind[u]);
+    }
+  }
+  return BEM2D_OK;
+}
+
+// Pairs that DiscreteKernel integrates with the graded rules
+// (lib/bem2d_quadrature.h:271-282): same element index -> IntegrateIdent,
+// else test next() == trial index -> AdaptedGauss3, else prev() -> AdaptedGauss2.
+static std::vector<NearPair> near_pairs(const bem2d_geometry* g) {
+  std::unordered_map<long long, std::vector<int>> by_index;
+  for (int u = 0; u < g->n_unk; ++u) by_index[g->index[g->unk_elem[u]]].push_back(u);
+  std::vector<NearPair> out;
+  out.reserve((size_t)g->n_unk * 3);
+  for (int i = 0; i < g->n_unk; ++i) {
+    const int e = g->unk_elem[i];
+    const long long keys[3] = {g->index[e], g->next[e], g->prev[e]};
+    const int rules[3] = {RULE_SELF, RULE_G3, RULE_G2};
+    for (int k = 0; k < 3; ++k) {
+      if (k > 0 && keys[k] == keys[0]) continue;
+      if (k == 2 && keys[2] == keys[1]) continue;
+      auto it = by_index.find(keys[k]);
+      if (it == by_index.end()) continue;
+      for (int j : it->second) out.push_back(NearPair{i, j, rules[k], k == 0 ? 1 : 0});
+    }
+  }
+  return out;
+}
+
+static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, bool nodes,
+                 bool pairs, Staged* st) {
+  int rc = check_geom(c, g);
+  if (rc) return rc;
+  if ((rc = check_quad(c, q))) return rc;
+  if ((rc = get_rules(c, q, &st->r))) return rc;
+  const int ne = g->n_elem, nu = g->n_unk;
+  // pack the tables: doubles first (alignment), then 64-bit, then 32-bit
+  const size_t b_param = sizeof(double) * 8 * ne, b_up = sizeof(double) * nu;
+  const size_t b_links = sizeof(long long) * 3 * ne;
+  const size_t b_ints = sizeof(int) * (ne + 2 * nu);
+  const size_t total = b_param + b_up + b_links + b_ints;
+  std::vector<char> h(total);
+  char* p = h.data();
+  memcpy(p, g->param, b_param);
+  memcpy(p + b_param, g->unk_param, b_up);
+  long long* lk = reinterpret_cast<long long*>(p + b_param + b_up);
+  for (int e = 0; e < ne; ++e) {
+    lk[e] = g->index[e];
+    lk[ne + e] = g->next[e];
+    lk[2 * ne + e] = g->prev[e];
+  }
+  int* ints = reinterpret_cast<int*>(p + b_param + b_up + b_links);
+  memcpy(ints, g->kind, sizeof(int) * ne);
+  memcpy(ints + ne, g->unk_elem, sizeof(int) * nu);
+  memcpy(ints + ne + nu, g->unk_kind, sizeof(int) * nu);
+  char* d = static_cast<char*>(ws(c, "geom", total, &rc));
+  if (!d) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(d, h.data(), total, cudaMemcpyHostToDevice, c->stream));
+  DevGeom& dg = st->g;
+  dg.n_elem = ne;
+  dg.n_unk = nu;
+  dg.param = reinterpret_cast<const double*>(d);
+  dg.unk_param = reinterpret_cast<const double*>(d + b_param);
+  dg.index = reinterpret_cast<const long long*>(d + b_param + b_up);
+  dg.next = dg.index + ne;
+  dg.prev = dg.index + 2 * ne;
+  const int* di = reinterpret_cast<const int*>(d + b_param + b_up + b_links);
+  dg.kind = di;
+  dg.unk_elem = di + ne;
+  dg.unk_kind = di + ne + nu;
+  st->pairs = nullptr;
+  st->npairs = 0;
+  if (pairs) {
+    const std::vector<NearPair> np = near_pairs(g);
+    st->npairs = (int)np.size();
+    st->pairs = static_cast<NearPair*>(ws(c, "pairs", sizeof(NearPair) * np.size(), &rc));
+    if (!st->pairs) return rc;
+    if (!np.empty())
+      CUDA_TRY(c, cudaMemcpyAsync(st->pairs, np.data(), sizeof(NearPair) * np.size(),
+                                  cudaMemcpyHostToDevice, c->stream));
+  }
+  if (nodes) {
+    const size_t nn = (size_t)nu * q->N;
+    double* t = static_cast<double*>(ws(c, "nodes", sizeof(double) * 5 * nn, &rc));
+    if (!t) return rc;
+    st->t = NodeTable{t, t + nn, t + 2 * nn, t + 3 * nn, t + 4 * nn};
+    launch_node_table(dg, st->r, st->t, c->stream);
+    ++c->launches;
+    CHECK_LAUNCH(c);
+  }
+  // the host table `h` must outlive the async copy
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEM2D_OK;
+}
+
+static int check_k(bem2d_ctx* c, double k_re, double k_im) {
+  if (k_im != 0.0)
+    return fail(c, BEM2D_ERR_UNSUPPORTED, "complex wavenumbers (k.im=%g) are not supported", k_im);
+  if (!std::isfinite(k_re)) return fail(c, BEM2D_ERR_ARG, "wavenumber is not finite");
+  return BEM2D_OK;
+}
+
+// Assemble beta*M + alpha*K into a device matrix (ld).
+static int assemble_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, double eta,
+                        double alpha, double beta, double2* A, long long ld) {
+  int t = tic(c, BEM2D_PHASE_FAR);
+  launch_far_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, A, ld, c->stream);
+  toc(c, t);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  t = tic(c, BEM2D_PHASE_NEAR);
+  launch_near_fp64(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
+                   c->stream);
+  toc(c, t);
+  if (st.npairs) ++c->launches;
+  CHECK_LAUNCH(c);
+  return BEM2D_OK;
+}
+
+// Output helpers: run `fill` into a device matrix (the caller's, or a
+// workspace one that is then copied to the caller's host memory).
+template <typename F>
+static int with_matrix_out(bem2d_ctx* c, void* out, long long ld, int n, F fill) {
+  if (!out) return fail(c, BEM2D_ERR_ARG, "output pointer is NULL");
+  if (ld < n) return fail(c, BEM2D_ERR_ARG, "leading dimension %lld < %d", ld, n);
+  int rc = 0;
+  if (is_device_ptr(out)) {
+    if ((rc = fill(static_cast<double2*>(out), ld))) return rc;
+  } else {
+    double2* d = static_cast<double2*>(ws(c, "out", sizeof(double2) * (size_t)n * n, &rc));
+    if (!d) return rc;
+    if ((rc = fill(d, (long long)n))) return rc;
+    CUDA_TRY(c, cudaMemcpy2DAsync(out, sizeof(double2) * ld, d, sizeof(double2) * n,
+                                  sizeof(double2) * n, n, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  resolve_timers(c);
+  return BEM2D_OK;
+}
+
+}  // namespace bem2d_gpu
+
+using namespace bem2d_gpu;
+
+extern "C" {
+
+int bem2d_ctx_create(int device, bem2d_ctx** out) {
+  if (!out) return BEM2D_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return BEM2D_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return BEM2D_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return BEM2D_ERR_CUDA;
+  bem2d_ctx* c = new bem2d_ctx;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BEM2D_ERR_CUDA;
+  }
+  c->own_stream = true;
+  *out = c;
+  return BEM2D_OK;
+}
+
+void bem2d_ctx_destroy(bem2d_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->bufs)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  for (auto& kv : c->rules) cudaFree(kv.second.first);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* bem2d_ctx_last_error(const bem2d_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+void* bem2d_ctx_stream(bem2d_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int bem2d_ctx_set_stream(bem2d_ctx* c, void* stream) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (c->own_stream && c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  c->stream = static_cast<cudaStream_t>(stream);
+  c->own_stream = false;
+  return BEM2D_OK;
+}
+
+int64_t bem2d_ctx_launch_count(const bem2d_ctx* c) { return c ? c->launches : 0; }
+
+int bem2d_ctx_enable_timers(bem2d_ctx* c, int enable) {
+  if (!c) return BEM2D_ERR_ARG;
+  c->timers = enable != 0;
+  for (int i = 0; i < 4; ++i) {
+    c->phase_ms[i] = 0;
+    c->phase_n[i] = 0;
+  }
+  return BEM2D_OK;
+}
+
+int bem2d_ctx_timer(const bem2d_ctx* c, int phase, double* ms, int64_t* count) {
+  if (!c || phase < 0 || phase > 3) return BEM2D_ERR_ARG;
+  if (ms) *ms = c->phase_ms[phase];
+  if (count) *count = c->phase_n[phase];
+  return BEM2D_OK;
+}
+
+int bem2d_gauss(int n, double* x, double* w) {
+  if (n < 1 || !x || !w) return BEM2D_ERR_ARG;
+  gauss01(n, x, w);
+  return BEM2D_OK;
+}
+
+int bem2d_discrete_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
+                          int kernel, double k_re, double k_im, double eta, double alpha,
+                          double beta, void* out, int64_t ld) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (kernel < BEM2D_KERNEL_SINGLE || kernel > BEM2D_KERNEL_COMBINED)
+    return fail(c, BEM2D_ERR_ARG, "unknown kernel %d", kernel);
+  int rc = check_k(c, k_re, k_im);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  Staged st;
+  if ((rc = stage(c, geom, quad, true, true, &st))) return rc;
+  return with_matrix_out(c, out, ld, geom->n_unk, [&](double2* A, long long lda) {
+    return assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, lda);
+  });
+}
+
+int bem2d_eval_ident(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
+                     void* out, int64_t ld) {
+  if (!c) return BEM2D_ERR_ARG;
+  cudaSetDevice(c->device);
+  Staged st;
+  int rc = stage(c, geom, quad, false, true, &st);
+  if (rc) return rc;
+  const int n = geom->n_unk;
+  return with_matrix_out(c, out, ld, n, [&](double2* A, long long lda) {
+    CUDA_TRY(c, cudaMemset2DAsync(A, sizeof(double2) * lda, 0, sizeof(double2) * n, n, c->stream));
+    launch_ident(st.g, st.r, st.pairs, st.npairs, A, lda, c->stream);
+    if (st.npairs) ++c->launches;
+    CHECK_LAUNCH(c);
+    return BEM2D_OK;
+  });
+}
+
+int bem2d_dot_prod_basfuns(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
+                           int fun, double k_re, double k_im, double dir_x, double dir_y,
+                           double eta, double scale, void* out) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (fun < BEM2D_FUN_PLANEWAVE || fun > BEM2D_FUN_COMBINEDPLANEWAVE)
+    return fail(c, BEM2D_ERR_ARG, "unknown functional %d", fun);
+  if (!out) return fail(c, BEM2D_ERR_ARG, "output pointer is NULL");
+  int rc = check_k(c, k_re, k_im);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  Staged st;
+  if ((rc = stage(c, geom, quad, true, false, &st))) return rc;
+  const int n = geom->n_unk;
+  const bool dev = is_device_ptr(out);
+  double2* b = dev ? static_cast<double2*>(out)
+                   : static_cast<double2*>(ws(c, "rhs_out", sizeof(double2) * n, &rc));
+  if (!b) return rc;
+  launch_rhs(st.g, st.t, st.r.ng, fun, k_re, dir_x, dir_y, eta, scale, b, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  if (!dev)
+    CUDA_TRY(c, cudaMemcpyAsync(out, b, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEM2D_OK;
+}
+
+}  // extern "C"
+
+namespace bem2d_gpu {
+
+// Solve with device-resident A (lda) and b; x written to device memory.
+static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const double2* b,
+                     double2* x, int precision, double tol, bem2d_solve_info* info) {
+  int rc = 0;
+  bem2d_solve_info rep{0, 0, 0.0};
+  LuWork w;
+  int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
+  if (!ints) return rc;
+  w.ipiv = ints + 8;
+  w.info = ints;
+  w.status = ints + 1;
+  w.barrier = reinterpret_cast<unsigned*>(ints + 2);
+  w.scratch_bytes = lu_scratch_bytes(n);
+  w.scratch = ws(c, "lu_scratch", w.scratch_bytes, &rc);
+  if (!w.scratch) return rc;
+  int hinfo[2] = {0, 0};
+  if (precision == BEM2D_PREC_FP64) {
+    double2* LU = static_cast<double2*>(ws(c, "lu64", sizeof(double2) * (size_t)n * n, &rc));
+    if (!LU) return rc;
+    CUDA_TRY(c, cudaMemcpy2DAsync(LU, sizeof(double2) * n, A, sizeof(double2) * lda,
+                                  sizeof(double2) * n, n, cudaMemcpyDeviceToDevice, c->stream));
+    int t = tic(c, BEM2D_PHASE_LU);
+    if ((rc = lu_factor<double2>(LU, n, n, w, c->stream, &c->launches)))
+      return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    toc(c, t);
+    CHECK_LAUNCH(c);
+    CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "LU panel barrier timed out");
+    rep.info = hinfo[0];
+    if (info) *info = rep;
+    if (hinfo[0]) return fail(c, hinfo[0], "zero pivot at column %d", hinfo[0]);
+    if (x != b) CUDA_TRY(c, cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, c->stream));
+    t = tic(c, BEM2D_PHASE_SOLVE);
+    lu_solve<double2>(LU, n, n, w.ipiv, x, c->stream, &c->launches);
+    toc(c, t);
+    CHECK_LAUNCH(c);
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    resolve_timers(c);
+    return BEM2D_OK;
+  }
+  if (precision != BEM2D_PREC_MIXED) return fail(c, BEM2D_ERR_ARG, "unknown precision %d", precision);
+  if (!(tol > 0)) tol = 1e-12;
+  float2* LU = static_cast<float2*>(ws(c, "lu32", sizeof(float2) * (size_t)n * n, &rc));
+  if (!LU) return rc;
+  double2* r = static_cast<double2*>(ws(c, "ir_r", sizeof(double2) * n, &rc));
+  float2* d = static_cast<float2*>(ws(c, "ir_d", sizeof(float2) * n, &rc));
+  double2* part = static_cast<double2*>(ws(c, "ir_part", residual_part_bytes(n), &rc));
+  double* red = static_cast<double*>(ws(c, "ir_red", sumsq_part_bytes() + 64, &rc));
+  if (!r || !d || !part || !red) return rc;
+  double* scal = red + sumsq_part_bytes() / sizeof(double);  // [0] |A|^2 [1] |b|^2 [2] |r|^2 [3] |x|^2
+  launch_to_c64(A, lda, LU, n, n, n, c->stream);
+  ++c->launches;
+  launch_sumsq(A, lda, n, n, red, scal, c->stream);
+  launch_sumsq(b, n, n, 1, red, scal + 1, c->stream);
+  c->launches += 4;
+  int tl = tic(c, BEM2D_PHASE_LU);
+  if ((rc = lu_factor<float2>(LU, n, n, w, c->stream, &c->launches)))
+    return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+  toc(c, tl);
+  CHECK_LAUNCH(c);
+  double hs[4];
+  CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(hs, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "LU panel barrier timed out");
+  rep.info = hinfo[0];
+  if (hinfo[0]) {
+    if (info) *info = rep;
+    return fail(c, hinfo[0], "zero pivot at column %d (complex64 factor)", hinfo[0]);
+  }
+  const double normA = std::sqrt(hs[0]), normb = std::sqrt(hs[1]);
+  // x0 = 0, r0 = b
+  CUDA_TRY(c, cudaMemsetAsync(x, 0, sizeof(double2) * n, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(r, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, c->stream));
+  double rnorm = normb, xnorm = 0.0, best = INFINITY;
+  int stall = 0;
+  const int max_it = 30;
+  for (int it = 0;; ++it) {
+    const double berr = rnorm / (normA * xnorm + normb);
+    rep.residual = berr;
+    rep.iterations = it;
+    if (!std::isfinite(berr)) {
+      if (info) *info = rep;
+      return fail(c, BEM2D_ERR_NONFINITE, "non-finite residual in refinement");
+    }
+    if (berr <= tol || rnorm == 0.0) break;
+    if (berr < 0.5 * best) {
+      best = berr;
+      stall = 0;
+    } else if (++stall >= 3) {
+      if (info) *info = rep;
+      return fail(c, BEM2D_ERR_NOCONV, "refinement stalled at backward error %.3e", berr);
+    }
+    if (it >= max_it) {
+      if (info) *info = rep;
+      return fail(c, BEM2D_ERR_NOCONV, "refinement did not reach %.1e in %d steps", tol, max_it);
+    }
+    // d = LU32^{-1} (r / |r|);  x += |r| d;  r = b - A x
+    const int ts = tic(c, BEM2D_PHASE_SOLVE);
+    launch_scale_to_c64(n, r, 1.0 / rnorm, d, c->stream);
+    lu_solve<float2>(LU, n, n, w.ipiv, d, c->stream, &c->launches);
+    launch_axpy_c64(n, rnorm, d, x, c->stream);
+    launch_residual(A, lda, n, x, b, r, part, c->stream);
+    launch_sumsq(r, n, n, 1, red, scal + 2, c->stream);
+    launch_sumsq(x, n, n, 1, red, scal + 3, c->stream);
+    toc(c, ts);
+    c->launches += 8;
+    CHECK_LAUNCH(c);
+    CUDA_TRY(c, cudaMemcpyAsync(hs, scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    rnorm = std::sqrt(hs[2]);
+    xnorm = std::sqrt(hs[3]);
+  }
+  resolve_timers(c);
+  if (info) *info = rep;
+  return BEM2D_OK;
+}
+
+// Copy host data to a workspace buffer unless it is already on the device.
+static const double2* dev_in(bem2d_ctx* c, const void* p, size_t rows, size_t cols, long long ld,
+                             const char* name, long long* ld_out, int* rc) {
+  if (is_device_ptr(p)) {
+    *ld_out = ld;
+    return static_cast<const double2*>(p);
+  }
+  double2* d = static_cast<double2*>(ws(c, name, sizeof(double2) * rows * cols, rc));
+  if (!d) return nullptr;
+  cudaError_t e = cudaMemcpy2DAsync(d, sizeof(double2) * rows, p, sizeof(double2) * ld,
+                                    sizeof(double2) * rows, cols, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    *rc = fail(c, BEM2D_ERR_CUDA, "host-to-device copy: %s", cudaGetErrorString(e));
+    return nullptr;
+  }
+  *ld_out = (long long)rows;
+  return d;
+}
+
+}  // namespace bem2d_gpu
+
+extern "C" {
+
+int bem2d_solve_system(bem2d_ctx* c, int n, const void* A, int64_t lda, const void* b, void* x,
+                       int precision, double tol, bem2d_solve_info* info) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !b || !x) return fail(c, BEM2D_ERR_ARG, "bad arguments (n=%d)", n);
+  if (lda < n) return fail(c, BEM2D_ERR_ARG, "lda %lld < n %d", (long long)lda, n);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long ldA = 0, ldb = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "in_A", &ldA, &rc);
+  if (!dA) return rc;
+  const double2* db = dev_in(c, b, n, 1, n, "in_b", &ldb, &rc);
+  if (!db) return rc;
+  const bool xdev = is_device_ptr(x);
+  double2* dx = xdev ? static_cast<double2*>(x)
+                     : static_cast<double2*>(ws(c, "out_x", sizeof(double2) * n, &rc));
+  if (!dx) return rc;
+  rc = solve_dev(c, n, dA, ldA, db, dx, precision, tol, info);
+  if (rc) return rc;
+  if (!xdev) {
+    CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  return BEM2D_OK;
+}
+
+int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
+                           double k_re, double k_im, double eta, double dir_x, double dir_y,
+                           int precision, double tol, void* x, bem2d_solve_info* info) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (!x) return fail(c, BEM2D_ERR_ARG, "output pointer is NULL");
+  int rc = check_k(c, k_re, k_im);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  Staged st;
+  if ((rc = stage(c, geom, quad, true, true, &st))) return rc;
+  const int n = geom->n_unk;
+  double2* A = static_cast<double2*>(ws(c, "sys_A", sizeof(double2) * (size_t)n * n, &rc));
+  if (!A) return rc;
+  double2* b = static_cast<double2*>(ws(c, "sys_b", sizeof(double2) * n, &rc));
+  if (!b) return rc;
+  if ((rc = assemble_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n))) return rc;
+  launch_rhs(st.g, st.t, st.r.ng, BEM2D_FUN_COMBINEDPLANEWAVE, k_re, dir_x, dir_y, eta, 2.0, b,
+             c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  const bool xdev = is_device_ptr(x);
+  double2* dx = xdev ? static_cast<double2*>(x)
+                     : static_cast<double2*>(ws(c, "out_x", sizeof(double2) * n, &rc));
+  if (!dx) return rc;
+  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info))) return rc;
+  if (!xdev) {
+    CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  }
+  return BEM2D_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,266 @@
+// Shared device-side definitions of the bem2d GB300 path: element geometry,
+// bases, kernel functions and the internal launch interfaces between the
+// translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/bem2d_gpu.h"
+#include "hankel.cuh"
+
+namespace bem2d_gpu {
+
+constexpr double kPi = 3.14159265358979323846;
+
+// ---- device view of a geometry ------------------------------------------
+// Element table and flat unknown list (see bem2d_geometry in bem2d_gpu.h).
+struct DevGeom {
+  int n_elem;
+  int n_unk;
+  const int* kind;
+  const double* param;  // 8 per element
+  const long long* index;
+  const long long* next;
+  const long long* prev;
+  const int* unk_elem;
+  const int* unk_kind;
+  const double* unk_param;
+};
+
+// Element Map(t) and Deriv(t) (lib/bem2d_element.h:72-116): an affine
+// ConstElement or an AnalyticCurveElement on one of the library curves
+// (lib/bem2d_curvetypes.h:13-99), evaluated in FP64.
+struct ElemPt {
+  double mx, my, dx, dy;
+};
+
+__device__ __forceinline__ void curve_eval(int kind, const double* c, double t,
+                                           ElemPt* r) {
+  const double tp = 2 * kPi * t;
+  double s, co;
+  switch (kind) {
+    case BEM2D_ELEM_CIRCLE:
+      sincos(tp, &s, &co);
+      r->mx = co;
+      r->my = s;
+      r->dx = 2 * kPi * (-1.0 * s);
+      r->dy = 2 * kPi * co;
+      break;
+    case BEM2D_ELEM_TREFOIL: {
+      sincos(tp, &s, &co);
+      double s3, c3;
+      sincos(3 * 2 * kPi * t, &s3, &c3);
+      const double rr = 1 + 0.3 * c3;
+      const double rp = -0.3 * 3 * 2 * kPi * s3;
+      r->mx = rr * co;
+      r->my = rr * s;
+      r->dx = rp * co - rr * 2 * kPi * s;
+      r->dy = rp * s + rr * 2 * kPi * co;
+      break;
+    }
+    case BEM2D_ELEM_KITE: {
+      sincos(tp, &s, &co);
+      double s2, c2;
+      sincos(4 * kPi * t, &s2, &c2);
+      r->mx = co + 0.65 * c2 - 0.65;
+      r->my = 1.5 * s;
+      r->dx = -2 * kPi * s - 0.65 * 4 * kPi * s2;
+      r->dy = 1.5 * 2 * kPi * co;
+      break;
+    }
+    case BEM2D_ELEM_ELLIPSE: {
+      const double rho = c[0];
+      sincos(tp, &s, &co);
+      r->mx = rho * co;
+      r->my = 1 / rho * s;
+      r->dx = -rho * 2 * kPi * s;
+      r->dy = 2 * kPi / rho * co;
+      break;
+    }
+    case BEM2D_ELEM_ELLIPSEARC: {
+      const double a = c[0], b = c[1], t1 = c[2], t2 = c[3];
+      sincos(t1 + t * (t2 - t1), &s, &co);
+      r->mx = a * co;
+      r->my = b * s;
+      r->dx = -a * (t2 - t1) * s;
+      r->dy = b * (t2 - t1) * co;
+      break;
+    }
+    case BEM2D_ELEM_INVELLIPSE: {
+      // z(t) = e^s / (1 + alpha e^{2s}), s = 2 pi i t
+      const double al = c[0];
+      double s2, c2;
+      sincos(tp, &s, &co);
+      sincos(2 * tp, &s2, &c2);
+      const double qr = 1.0 + al * c2, qi = al * s2;
+      const double qn = qr * qr + qi * qi;
+      r->mx = (co * qr + s * qi) / qn;
+      r->my = (s * qr - co * qi) / qn;
+      // z'(t) = 2 pi i e^s (1 - alpha e^{2s}) / q^2
+      const double q2r = qr * qr - qi * qi, q2i = 2 * qr * qi;
+      const double q2n = q2r * q2r + q2i * q2i;
+      const double ur = 1.0 - al * c2, ui = -al * s2;
+      const double nr = co * ur - s * ui, ni = co * ui + s * ur;
+      const double ir = -2 * kPi * ni, ii = 2 * kPi * nr;
+      r->dx = (ir * q2r + ii * q2i) / q2n;
+      r->dy = (ii * q2r - ir * q2i) / q2n;
+      break;
+    }
+    default:
+      r->mx = r->my = r->dx = r->dy = __longlong_as_double(0x7ff8000000000000LL);
+  }
+}
+
+__device__ __forceinline__ ElemPt elem_eval(int kind, const double* p, double t) {
+  ElemPt r;
+  if (kind == BEM2D_ELEM_SEGMENT) {
+    const double ddx = p[2] - p[0], ddy = p[3] - p[1];
+    r.mx = p[0] + ddx * t;
+    r.my = p[1] + ddy * t;
+    r.dx = ddx;
+    r.dy = ddy;
+  } else {
+    const double t1 = p[0], t2 = p[1];
+    curve_eval(kind, p + 2, t1 + t * (t2 - t1), &r);
+    r.dx *= (t2 - t1);
+    r.dy *= (t2 - t1);
+  }
+  return r;
+}
+
+// Normal(t) = normalize(Deriv.y, -Deriv.x) (lib/bem2d_element.h:29-34).
+__device__ __forceinline__ void elem_normal(const ElemPt& p, double* nx, double* ny) {
+  const double l = sqrt(p.dy * p.dy + p.dx * p.dx);
+  *nx = p.dy / l;
+  *ny = -p.dx / l;
+}
+
+__device__ __forceinline__ double elem_jac(const ElemPt& p) {
+  return sqrt(p.dx * p.dx + p.dy * p.dy);
+}
+
+// PolBasis t^d / LinBasis (lib/bem2d_basistypes.h:28-62); all library bases
+// used here are real, so conj(phi) = phi.
+__device__ __forceinline__ double basis_eval(int kind, double param, double t) {
+  if (kind == BEM2D_BASIS_LIN) return param == -1.0 ? 1 - t : t;
+  const int deg = (int)param;
+  double r = 1;
+  for (int i = 0; i < deg; ++i) r *= t;
+  return r;
+}
+
+// ---- kernels (lib/bem2d_kernel.cpp:15-112), real wavenumber ---------------
+// Returns K(x, y) for test point x with normal n1 and trial point y with
+// normal n2.  kq = k/4, eq = eta/4.
+template <int KERNEL>
+__device__ __forceinline__ void kernel_d(double kk, double kq, double eq,
+                                         double xx, double xy, double yx,
+                                         double yy, double n1x, double n1y,
+                                         double n2x, double n2y, double* re,
+                                         double* im) {
+  const double wx = xx - yx, wy = xy - yy;
+  const double d = sqrt(wx * wx + wy * wy);
+  double j0, y0, j1, y1;
+  hankel01_d(kk * d, &j0, &y0, &j1, &y1);
+  if (KERNEL == BEM2D_KERNEL_SINGLE) {
+    *re = -0.25 * y0;
+    *im = 0.25 * j0;
+  } else {
+    // DoubleLayer uses w = y - x and the trial normal; the others w = x - y
+    // and the test normal.
+    const double dot = (KERNEL == BEM2D_KERNEL_DOUBLE) ? -(n2x * wx + n2y * wy)
+                                                       : (n1x * wx + n1y * wy);
+    const double c = dot / d;
+    *re = kq * c * y1;
+    *im = -kq * c * j1;
+    if (KERNEL == BEM2D_KERNEL_COMBINED) {
+      *re = fma(eq, j0, *re);
+      *im = fma(eq, y0, *im);
+    }
+  }
+}
+
+// ---- near-pair rules -------------------------------------------------------
+enum NearRule : int { RULE_SELF = 0, RULE_G2 = 1, RULE_G3 = 2 };
+
+struct NearPair {
+  int i;     // test unknown (row)
+  int j;     // trial unknown (column)
+  int rule;  // NearRule
+  int same;  // element indices equal (mass-matrix term applies)
+};
+
+// Quadrature rules on the device: Gauss nodes on [0,1] and the three
+// adapted rules (lib/bem2d_quadpoints.cpp:75-183), points as (x, y, w).
+struct DevRules {
+  int ng;                // Gauss points
+  const double* gx;      // [ng]
+  const double* gw;      // [ng]
+  int n1, n2, n3;        // sizes of AdaptedGauss1/2/3
+  const double* r1;      // [3*n1] x, y, w
+  const double* r2;
+  const double* r3;
+};
+
+// ---- launch interfaces (assembly.cu) ------------------------------------
+struct NodeTable {
+  // Far-field node data per unknown u and Gauss node q (index u*ng + q).
+  double* x;
+  double* y;
+  double* nx;
+  double* ny;
+  double* w;  // |J(x_q)| * w_q * phi_u(x_q)
+};
+
+void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
+                       cudaStream_t s);
+void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
+                     double k, double eta, double alpha, double2* out,
+                     long long ld, cudaStream_t s);
+void launch_near_fp64(const DevGeom& g, const DevRules& r, const NearPair* pairs,
+                      int npairs, int kernel, double k, double eta, double alpha,
+                      double beta, double2* out, long long ld, cudaStream_t s);
+void launch_ident(const DevGeom& g, const DevRules& r, const NearPair* pairs,
+                  int npairs, double2* out, long long ld, cudaStream_t s);
+void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
+                double dx, double dy, double eta, double scale, double2* out,
+                cudaStream_t s);
+
+// ---- launch interfaces (lu.cu) --------------------------------------------
+struct LuWork {
+  int* ipiv;             // [n] pivot rows (0-based): row i was swapped with ipiv[i]
+  int* info;             // [1] first zero pivot (1-based) or 0
+  int* status;           // [1] nonzero: a bounded device wait gave up
+  unsigned* barrier;     // [2] grid barrier counter / generation
+  void* scratch;         // panel exchange buffers
+  size_t scratch_bytes;
+};
+
+// Bytes of LuWork::scratch the panel kernels need for n unknowns.
+size_t lu_scratch_bytes(int n);
+
+// LU with partial pivoting in place; T = double2 (complex128) or float2.
+template <typename T>
+int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
+              long long* launches);
+template <typename T>
+void lu_solve(const T* LU, long long lda, int n, const int* ipiv, T* b,
+              cudaStream_t s, long long* launches);
+
+void launch_residual(const double2* A, long long lda, int n, const double2* x,
+                     const double2* b, double2* r, double2* part, cudaStream_t s);
+size_t residual_part_bytes(int n);
+void launch_to_c64(const double2* src, long long lds, float2* dst, long long ldd,
+                   int rows, int cols, cudaStream_t s);
+void launch_scale_to_c64(int n, const double2* src, double scale, float2* dst,
+                         cudaStream_t s);
+void launch_axpy_c64(int n, double scale, const float2* d, double2* x, cudaStream_t s);
+// *out = sum |a_ij|^2 (part: sumsq_part_bytes() of scratch)
+void launch_sumsq(const double2* A, long long ld, int rows, int cols, double* part,
+                  double* out, cudaStream_t s);
+size_t sumsq_part_bytes();
+
+}  // namespace bem2d_gpu

@@ -1,0 +1,190 @@
+/*
+ * bem2d_gpu.h -- C ABI of the GB300 (sm_103a) Galerkin assembly and dense
+ * solve path of bem2d.
+ *
+ * Every entry point replaces one routine of the reference library; the
+ * comment above each names it (file:line in the reference project).  The C++
+ * API in bem2d_gb300/lib (same class and function names as the reference's
+ * lib/) is written on top of these calls, and so is the Python test/bench
+ * binding (bem2d_gb300/capi.py).
+ *
+ * Conventions
+ *  - Matrices are complex128 (interleaved re, im), column-major, entry (i,j)
+ *    at index i + j*ld: the reference's Matrix layout
+ *    (lib/bem2d_mathroutines.cpp:78-140).
+ *  - Matrix/vector pointers may be host or device memory; the library looks
+ *    the pointer up and copies host data through its own device workspace.
+ *    Calls are stream-ordered on the context's stream and return after the
+ *    results are in place (host results copied back).
+ *  - Return values: 0 = success; > 0 = LAPACK-style info (a zero pivot at
+ *    column `info`, 1-based: the reference throws LapackError); < 0 = one of
+ *    the BEM2D_ERR_* codes.  bem2d_ctx_last_error() gives a message.
+ *  - A context is not thread-safe; use one per host thread.
+ */
+#ifndef BEM2D_GPU_H
+#define BEM2D_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define BEM2D_OK 0
+#define BEM2D_ERR_ARG (-1)         /* bad argument: reference ParameterException / SizeError / ArrayMismatch */
+#define BEM2D_ERR_CUDA (-2)        /* CUDA runtime error */
+#define BEM2D_ERR_NOMEM (-3)       /* device allocation failed */
+#define BEM2D_ERR_NONFINITE (-4)   /* NaN/Inf in an assembled entry or a residual */
+#define BEM2D_ERR_NOCONV (-5)      /* iterative refinement / iteration did not converge */
+#define BEM2D_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up */
+#define BEM2D_ERR_UNSUPPORTED (-7) /* complex wavenumber, unknown element or basis kind */
+
+/* ---- element kinds (lib/bem2d_element.h:72-116, lib/bem2d_curvetypes.h) -
+ * param row (8 doubles) per element:
+ *   SEGMENT     p1x p1y p2x p2y                 ConstElement(p1, p2)
+ *   curves      t1 t2 c0 c1 c2 c3               AnalyticCurveElement(t1, t2, curve)
+ *     CIRCLE, TREFOIL, KITE: no curve parameters
+ *     ELLIPSE: c0 = rho;  ELLIPSEARC: c0..c3 = a, b, theta1, theta2
+ *     INVELLIPSE: c0 = alpha                                                  */
+#define BEM2D_ELEM_SEGMENT 0
+#define BEM2D_ELEM_CIRCLE 1
+#define BEM2D_ELEM_TREFOIL 2
+#define BEM2D_ELEM_KITE 3
+#define BEM2D_ELEM_ELLIPSE 4
+#define BEM2D_ELEM_ELLIPSEARC 5
+#define BEM2D_ELEM_INVELLIPSE 6
+
+/* ---- basis kinds (lib/bem2d_basistypes.h:28-62) ------------------------ */
+#define BEM2D_BASIS_POLY 0 /* PolBasis(degree): t^degree; param = degree */
+#define BEM2D_BASIS_LIN 1  /* LinBasis(sign): t or 1-t; param = sign     */
+
+/* ---- kernels (lib/bem2d_kernel.h:12-88) -------------------------------- */
+#define BEM2D_KERNEL_SINGLE 0     /* SingleLayer               */
+#define BEM2D_KERNEL_DOUBLE 1     /* DoubleLayer               */
+#define BEM2D_KERNEL_CONJDOUBLE 2 /* ConjDoubleLayer           */
+#define BEM2D_KERNEL_COMBINED 3   /* CombinedSingleConjDouble  */
+
+/* ---- incident-field functionals (lib/bem2d_fun.h:14-93) ---------------- */
+#define BEM2D_FUN_PLANEWAVE 0
+#define BEM2D_FUN_NORMALPLANEWAVE 1
+#define BEM2D_FUN_COMBINEDPLANEWAVE 2
+
+/* ---- solver precision -------------------------------------------------- */
+#define BEM2D_PREC_FP64 0  /* complex128 LU, FP64 throughout                 */
+#define BEM2D_PREC_MIXED 1 /* complex64 LU + FP64 iterative refinement      */
+
+/* QuadOption (lib/bem2d_quadrature.h:26-30). */
+typedef struct {
+  int32_t L;
+  int32_t N;
+  double sigma;
+} bem2d_quad;
+
+/* Geometry in flat form: the element list of Geometry (lib/bem2d_geometry.h)
+ * with each element's index()/next()/prev() (lib/bem2d_element.h:36-58;
+ * -1 = unset), and the (element, basis) list of Geometry::FlatMap()
+ * (lib/bem2d_geometry.h:48-57) whose order numbers the unknowns. */
+typedef struct {
+  int32_t n_elem;
+  const int32_t* kind;    /* [n_elem]     BEM2D_ELEM_*                      */
+  const double* param;    /* [n_elem * 8] see above                         */
+  const int64_t* index;   /* [n_elem]                                       */
+  const int64_t* next;    /* [n_elem]                                       */
+  const int64_t* prev;    /* [n_elem]                                       */
+  int32_t n_unk;
+  const int32_t* unk_elem;  /* [n_unk] element position (0..n_elem-1)     */
+  const int32_t* unk_kind;  /* [n_unk] BEM2D_BASIS_*                       */
+  const double* unk_param;  /* [n_unk] degree or sign                      */
+} bem2d_geometry;
+
+/* Solver report. */
+typedef struct {
+  int32_t info;         /* LAPACK-style info of the factorisation (0 = ok)   */
+  int32_t iterations;   /* refinement steps taken (mixed precision)          */
+  double residual;      /* final ||b - A x||_2 / (||A||_F ||x||_2 + ||b||_2) */
+} bem2d_solve_info;
+
+typedef struct bem2d_ctx bem2d_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+int bem2d_ctx_create(int device, bem2d_ctx** ctx);
+void bem2d_ctx_destroy(bem2d_ctx* ctx);
+const char* bem2d_ctx_last_error(const bem2d_ctx* ctx);
+/* cudaStream_t the context issues its work on (default: its own stream). */
+void* bem2d_ctx_stream(bem2d_ctx* ctx);
+int bem2d_ctx_set_stream(bem2d_ctx* ctx, void* stream);
+/* Number of kernels this context has launched so far. */
+int64_t bem2d_ctx_launch_count(const bem2d_ctx* ctx);
+
+/* ---- quadrature rules -------------------------------------------------- */
+/* Gauss(x, w, N) on [0,1]: replaces lib/bem2d_quadrature.cpp:10-56 (host). */
+int bem2d_gauss(int n, double* x, double* w);
+
+/* ---- assembly ---------------------------------------------------------- */
+/* out = beta * EvalIdent(geom) + alpha * DiscreteKernel(geom, quad, kernel):
+ * replaces DiscreteKernel<kernel> (lib/bem2d_quadrature.h:231-294) and, with
+ * alpha = 2, beta = 1, kernel = COMBINED, the matrix of
+ * SoundSoftScattering::DiscretizeMatrix (lib/bem2d_soundsoftscattering.h:95-103).
+ * eta is the coupling of COMBINED (CombinedSingleConjDouble(k) uses eta = k).
+ * precision: BEM2D_PREC_FP64 only (the mixed solver consumes FP64 matrices).
+ * out: complex128 n_unk x n_unk, leading dimension ld >= n_unk. */
+int bem2d_discrete_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom,
+                          const bem2d_quad* quad, int kernel, double k_re,
+                          double k_im, double eta, double alpha, double beta,
+                          void* out, int64_t ld);
+
+/* out = mass matrix: replaces EvalIdent (lib/bem2d_quadrature.cpp:79-127). */
+int bem2d_eval_ident(bem2d_ctx* ctx, const bem2d_geometry* geom,
+                     const bem2d_quad* quad, void* out, int64_t ld);
+
+/* out[i] = scale * sum_q fun(x_q) |J| phi_i(x_q) w_q: replaces DotProdBasFuns
+ * (lib/bem2d_quadrature.h:130-156) with PlaneWave / NormalPlaneWave /
+ * CombinedPlaneWave (lib/bem2d_fun.h:14-93); SoundSoftScattering::
+ * DiscretizeRhs uses COMBINEDPLANEWAVE with scale = 2. */
+int bem2d_dot_prod_basfuns(bem2d_ctx* ctx, const bem2d_geometry* geom,
+                           const bem2d_quad* quad, int fun, double k_re,
+                           double k_im, double dir_x, double dir_y, double eta,
+                           double scale, void* out);
+
+/* ---- dense solve ------------------------------------------------------- */
+/* x = A^{-1} b: replaces SolveSystem (lib/bem2d_mathroutines.cpp:323-351,
+ * LAPACK zgetrf + zgetrs).  A (n x n, lda) and b are not modified.
+ * BEM2D_PREC_FP64: blocked complex128 LU with partial pivoting.
+ * BEM2D_PREC_MIXED: complex64 LU with partial pivoting, then FP64 iterative
+ *   refinement with the complex128 A until residual <= tol (tol <= 0 selects
+ *   1e-12), at most 30 steps. */
+int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
+                       const void* b, void* x, int precision, double tol,
+                       bem2d_solve_info* info);
+
+/* SoundSoftScattering::Discretize() + Solve() in one call
+ * (lib/bem2d_soundsoftscattering.h:95-126): A = Id + 2 K_combined(k, eta),
+ * b = 2 <CombinedPlaneWave(dir, k, eta), phi_i>, x = A^{-1} b.  A and b stay
+ * in the context's device workspace; only x (n_unk complex128) is written. */
+int bem2d_scattering_solve(bem2d_ctx* ctx, const bem2d_geometry* geom,
+                           const bem2d_quad* quad, double k_re, double k_im,
+                           double eta, double dir_x, double dir_y,
+                           int precision, double tol, void* x,
+                           bem2d_solve_info* info);
+
+/* ---- measurement helpers (no counterpart in the reference) ------------ */
+/* Sustained FMA throughput of the FP64 (BEM2D_PREC_FP64) or FP32
+ * (BEM2D_PREC_MIXED) pipe of the current device in TFLOP/s (2 flops per
+ * FMA): the roofline denominator of the assembly kernels. */
+int bem2d_fma_peak(int precision, double* tflops);
+
+/* Per-phase device timers (CUDA events on the context's stream).  Phases:
+ * 0 far-field assembly kernel, 1 near-field kernel, 2 LU factorisation,
+ * 3 triangular solves and refinement.  Enabling resets the totals. */
+#define BEM2D_PHASE_FAR 0
+#define BEM2D_PHASE_NEAR 1
+#define BEM2D_PHASE_LU 2
+#define BEM2D_PHASE_SOLVE 3
+int bem2d_ctx_enable_timers(bem2d_ctx* ctx, int enable);
+int bem2d_ctx_timer(const bem2d_ctx* ctx, int phase, double* ms, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BEM2D_GPU_H */

@@ -1,0 +1,105 @@
+"""Generate the committed golden fixtures from the reference library itself.
+
+Builds oracle/_ref/ref_dump (the reference's lib/ compiled in place with the
+shims in oracle/shim, see oracle/Makefile), runs it on every case in
+cases.py, and stores the outputs as tests/golden/<case>.npz.
+
+Small cases keep full matrices.  Larger ones keep size-independent probes:
+A @ v and A^H @ w for seeded vectors, the diagonal, 4096 seeded entries, the
+right-hand side, the solution and the norm / condition number.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from golden.cases import CASES, QUAD  # noqa: E402
+
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+
+
+def probes(A, seed):
+    rng = np.random.default_rng(seed)
+    n = A.shape[0]
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    w = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ii = rng.integers(0, n, 4096)
+    jj = rng.integers(0, n, 4096)
+    return dict(probe_v=v, probe_w=w, Av=A @ v, AHw=A.conj().T @ w,
+                diag=np.diag(A).copy(), sample_i=ii, sample_j=jj,
+                sample=A[ii, jj], fro=np.linalg.norm(A))
+
+
+def read_c(path, shape):
+    return np.fromfile(path, dtype=np.complex128).reshape(shape, order="F")
+
+
+def run_case(name, spec):
+    g = spec["geom"]()
+    n = g.n_unknowns
+    k, eta, d = spec["k"], spec["eta"], spec["direction"]
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        lines = g.to_refspec(QUAD)
+        if spec.get("scattering", True):
+            lines.append("op scattering %.17g 0 %.17g %.17g %.17g %s/sys"
+                         % (k, d[0], d[1], eta, tmp))
+        lines.append("op ident %s/ident.bin" % tmp)
+        for kn in spec.get("kernels", ()):
+            lines.append("op kernel %s %.17g 0 %.17g %s/k_%s.bin" % (kn, k, eta, tmp, kn))
+        if spec.get("numrange"):
+            lines.append("op numrange %.17g 0 %.17g %d %s/numrange.txt"
+                         % (k, eta, spec["numrange"], tmp))
+        if spec.get("singvals"):
+            lines.append("op singvals %.17g 0 %.17g %s/singvals.bin" % (k, eta, tmp))
+        with open(os.path.join(tmp, "case.txt"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        subprocess.run([REF_DUMP, os.path.join(tmp, "case.txt")], check=True,
+                       stdout=subprocess.DEVNULL)
+        out["ident_diag"] = np.diag(read_c(tmp + "/ident.bin", (n, n))).copy()
+        if spec.get("scattering", True):
+            A = read_c(tmp + "/sys_A.bin", (n, n))
+            out["rhs"] = np.fromfile(tmp + "/sys_rhs.bin", dtype=np.complex128)
+            out["x"] = np.fromfile(tmp + "/sys_x.bin", dtype=np.complex128)
+            out["normcond"] = np.fromfile(tmp + "/sys_normcond.bin", dtype=np.float64)
+            if spec["full"]:
+                out["A"] = A
+            else:
+                out.update(probes(A, 1234))
+        for kn in spec.get("kernels", ()):
+            out["K_" + kn] = read_c("%s/k_%s.bin" % (tmp, kn), (n, n))
+        if spec.get("numrange"):
+            pts = np.loadtxt(tmp + "/numrange.txt")
+            out["numrange"] = pts[:, 0] + 1j * pts[:, 1]
+        if spec.get("singvals"):
+            out["singvals"] = np.fromfile(tmp + "/singvals.bin", dtype=np.float64)
+    meta = dict(name=name, n=n, k=k, eta=eta, direction=list(d), quad=list(QUAD))
+    out["meta"] = np.array(json.dumps(meta))
+    return out
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"],
+                   check=True, stdout=subprocess.DEVNULL)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        res = run_case(name, CASES[name])
+        path = os.path.join(ROOT, "tests", "golden", name + ".npz")
+        np.savez_compressed(path, **res)
+        print("%-16s n=%-5d %7.1f KB" % (name, json.loads(str(res["meta"]))["n"],
+                                          os.path.getsize(path) / 1024))
+
+
+if __name__ == "__main__":
+    main()

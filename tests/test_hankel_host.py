@@ -1,0 +1,63 @@
+"""Accuracy of the device Hankel evaluator (bem2d_gb300/csrc/hankel.cuh).
+
+The evaluator is header-only and compiles for the host too; this builds it
+with g++ and checks H0, H1 against mpmath (50 digits) and against the POSIX
+libm Bessel functions that stand in for GSL in the oracle.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def hk(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("hk") / "libhk.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared",
+                    "-I" + os.path.join(ROOT, "bem2d_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "hankel_host.cpp"), "-o", out],
+                   check=True)
+    lib = ctypes.CDLL(out)
+
+    def f(x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        o = np.zeros((len(x), 4))
+        lib.hankel01_d_host(ctypes.c_int(len(x)), x.ctypes.data_as(ctypes.c_void_p),
+                            o.ctypes.data_as(ctypes.c_void_p))
+        return o[:, 0] + 1j * o[:, 1], o[:, 2] + 1j * o[:, 3]
+    return f
+
+
+def test_against_mpmath(hk):
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 30
+    rng = np.random.default_rng(7)
+    x = np.concatenate([10 ** rng.uniform(-9, 4.3, 1500), np.linspace(3.95, 4.05, 21),
+                        np.linspace(7.95, 8.05, 21), [4.0, 8.0]])
+    h0, h1 = hk(x)
+    e0 = max(abs(complex(h0[i]) - complex(mp.hankel1(0, xi))) / abs(mp.hankel1(0, xi))
+             for i, xi in enumerate(x))
+    e1 = max(abs(complex(h1[i]) - complex(mp.hankel1(1, xi))) / abs(mp.hankel1(1, xi))
+             for i, xi in enumerate(x))
+    # stated accuracy of the FP64 evaluator: 1e-15 relative to |H|
+    assert e0 < 1e-15 and e1 < 1e-15, (e0, e1)
+
+
+def test_against_libm(hk):
+    """POSIX libm j0/j1/y0/y1 (the oracle's stand-in for GSL)."""
+    libm = ctypes.CDLL("libm.so.6")
+    f = {}
+    for name in ("j0", "j1", "y0", "y1"):
+        fn = getattr(libm, name)
+        fn.restype = ctypes.c_double
+        fn.argtypes = [ctypes.c_double]
+        f[name] = np.vectorize(fn)
+    x = np.linspace(1e-3, 2e4, 40001)
+    h0, h1 = hk(x)
+    r0 = np.abs(h0 - (f["j0"](x) + 1j * f["y0"](x))) / np.abs(h0)
+    r1 = np.abs(h1 - (f["j1"](x) + 1j * f["y1"](x))) / np.abs(h1)
+    assert r0.max() < 4e-15 and r1.max() < 4e-15, (r0.max(), r1.max())

@@ -1,0 +1,132 @@
+"""The CPU oracle (oracle/bem2d_oracle.c) pinned against the reference.
+
+The golden fixtures in tests/golden were produced by the reference library
+itself (compiled in place, oracle/Makefile `ref`; generator
+tests/golden/make_golden.py).  These tests keep the C restatement, which the
+GPU tests use as their checker, tied to them.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from golden.cases import CASES, QUAD
+from oracle import oracle as O
+
+# FP64 agreement of the restatement with the reference (rounding order only)
+TOL_MAT = 1e-12
+
+
+def load(name):
+    z = np.load(_path(name))
+    return z, json.loads(str(z["meta"]))
+
+
+def _path(name):
+    import os
+    return os.path.join(os.path.dirname(__file__), "golden", name + ".npz")
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from bem2d_gb300 import _build
+    _build.build_oracle(with_reference=False)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_port_matches_reference(name):
+    z, meta = load(name)
+    spec = CASES[name]
+    g = spec["geom"]()
+    assert g.n_unknowns == meta["n"]
+    k, eta, d = spec["k"], spec["eta"], spec["direction"]
+    M = O.eval_ident(g, QUAD[1])
+    assert np.abs(np.diag(M) - z["ident_diag"]).max() <= 1e-15 * np.abs(z["ident_diag"]).max()
+    if "rhs" in z:
+        A, b = O.system(g, k, d, eta, QUAD)
+        assert rel(b, z["rhs"]) < TOL_MAT
+        if "A" in z:
+            assert rel(A, z["A"]) < TOL_MAT
+        else:
+            assert rel(A @ z["probe_v"], z["Av"]) < TOL_MAT
+            assert rel(A.conj().T @ z["probe_w"], z["AHw"]) < TOL_MAT
+            assert rel(A[z["sample_i"], z["sample_j"]], z["sample"]) < TOL_MAT
+            assert rel(np.diag(A), z["diag"]) < TOL_MAT
+        x = O.solve(A, b)
+        # the graded L-shape is ill-conditioned (element sizes down to 0.15^8)
+        assert rel(x, z["x"]) < (1e-8 if name == "lshape_graded" else 1e-11)
+        nrm, cond = O.norm_cond(O.change_basis(A, M))
+        assert abs(nrm - z["normcond"][0]) < 1e-12 * nrm
+        assert abs(cond - z["normcond"][1]) < (1e-8 if name == "lshape_graded" else 1e-11) * cond
+    for kn in spec.get("kernels", ()):
+        K = O.discrete_kernel(g, kn, k, eta, QUAD)
+        R = z["K_" + kn]
+        if np.linalg.norm(R) == 0:
+            assert np.abs(K).max() < 1e-15
+        else:
+            assert rel(K, R) < TOL_MAT
+
+
+def test_numrange_restatement():
+    """NumRange(ChangeBasis(A, Id), n): support-line intersection of the
+    extreme eigenvalues of the Hermitian parts (lib/bem2d_mathroutines.cpp:590-653)."""
+    z, meta = load("square_numrange")
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A, _ = O.system(g, spec["k"], spec["direction"], spec["eta"], QUAD)
+    B = O.change_basis(A, O.eval_ident(g, QUAD[1]))
+    n = spec["numrange"]
+    steps = np.arange(n) * (np.pi / n)
+    lmax = O.numrange_lmax(B, steps)
+    lmin = -O.numrange_lmax(B, steps + np.pi)
+    eigs = np.concatenate([lmin, lmax, lmin[:1]])
+    st = np.concatenate([steps, steps, [0.0]])
+    pts = []
+    for i in range(2 * n):
+        c1, c2, s1, s2 = np.cos(st[i]), np.cos(st[i + 1]), np.sin(st[i]), np.sin(st[i + 1])
+        t1 = (eigs[i + 1] - eigs[i] * (c1 * c2 + s1 * s2)) / (s1 * c2 - s2 * c1)
+        pts.append(np.exp(-1j * st[i]) * (eigs[i] + 1j * t1))
+    pts.append(pts[0])
+    # the reference writes the points with 6 significant digits
+    assert np.abs(np.array(pts) - z["numrange"]).max() < 1e-5 * np.abs(z["numrange"]).max()
+
+
+def test_singular_values():
+    z, meta = load("square_numrange")
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A, _ = O.system(g, spec["k"], spec["direction"], spec["eta"], QUAD)
+    B = O.change_basis(A, O.eval_ident(g, QUAD[1]))
+    from scipy.linalg import svd
+    s = svd(B, compute_uv=False, lapack_driver="gesvd")
+    assert np.abs(s - z["singvals"]).max() < 1e-12 * s[0]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 10, 20, 30])
+def test_gauss_rule(n):
+    x, w = O.gauss(n)
+    assert np.all(np.diff(x) > 0) and abs(w.sum() - 1) < 1e-15
+    # exact for polynomials of degree 2n-1 on [0,1]
+    for p in range(2 * n):
+        assert abs(np.sum(w * x ** p) - 1.0 / (p + 1)) < 1e-14
+
+
+def test_adapted_rule_weight_sums():
+    """Graded rules leave out the innermost sigma^L corner box: weight sums
+    (1 - sigma^L)^2 (self) and 1 - sigma^(2L) (neighbours)."""
+    L, N, s = 3, 5, 0.15
+    x, w = O.gauss(N)
+    W = np.outer(w, w).sum()
+    xl = [s ** (L - i) for i in range(L)] + [1.0]
+    s1 = sum((xl[i + 1] - xl[i]) * (xl[j + 1] - xl[j]) * W for i in range(L) for j in range(L))
+    assert abs(s1 - (1 - s ** L) ** 2) < 1e-15
+    a, b, tot = s, 1.0, 0.0
+    for _ in range(L):
+        tot += (a * (b - a) + (b - a) * (b - a) + (b - a) * a) * W
+        a, b = a * s, b * s
+    assert abs(tot - (1 - s ** (2 * L))) < 1e-15
