@@ -353,7 +353,9 @@ static int panel_blocks(int H) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   }
-  return std::max(1, std::min(nsm, (H + 15) / 16));
+  // at least 64 rows per block: fewer blocks make the per-column barrier
+  // and the pivot agreement cheaper; one block per SM at most
+  return std::max(1, std::min(nsm, (H + 63) / 64));
 }
 
 template <typename T>
@@ -404,11 +406,18 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
 
 // ---- triangular solves ----------------------------------------------------
 // Forward step of panel k0: swaps of the panel applied to b, then
-// y = L11^{-1} b[k0:k0+nb].
+// y = L11^{-1} b[k0:k0+nb].  The nb x nb diagonal block is staged in shared
+// memory first (coalesced), so the sequential sweep reads only smem.
 template <typename T>
 __global__ void fwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0, int nb,
                                 const int* __restrict__ ipiv, T* b) {
-  __shared__ T y[kNB];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB]
+  T* y = D + kNB * kNB;                   // [kNB]
+  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
+    const int s = v / nb, r = v - s * nb;
+    D[s * kNB + r] = LU[(size_t)(k0 + s) * lda + k0 + r];
+  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < nb; ++s) {
       const int p = ipiv[k0 + s];
@@ -425,7 +434,7 @@ __global__ void fwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0,
     __syncthreads();
     const T ys = y[s];
     const int r = threadIdx.x;
-    if (r > s && r < nb) y[r] = cfms(y[r], LU[(size_t)(k0 + s) * lda + k0 + r], ys);
+    if (r > s && r < nb) y[r] = cfms(y[r], D[s * kNB + r], ys);
   }
   __syncthreads();
   if (threadIdx.x < nb) b[k0 + threadIdx.x] = y[threadIdx.x];
@@ -447,15 +456,26 @@ __global__ void gemv_sub_kernel(const T* __restrict__ LU, long long lda, int c0,
 
 template <typename T>
 __global__ void bwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0, int nb, T* b) {
-  __shared__ T y[kNB];
-  if (threadIdx.x < nb) y[threadIdx.x] = b[k0 + threadIdx.x];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB]
+  T* rd = D + kNB * kNB;                  // [kNB]
+  T* y = rd + kNB;                        // [kNB]
+  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
+    const int s = v / nb, r = v - s * nb;
+    D[s * kNB + r] = LU[(size_t)(k0 + s) * lda + k0 + r];
+  }
+  __syncthreads();
+  if (threadIdx.x < nb) {
+    rd[threadIdx.x] = crcp(D[threadIdx.x * kNB + threadIdx.x]);
+    y[threadIdx.x] = b[k0 + threadIdx.x];
+  }
   for (int s = nb - 1; s >= 0; --s) {
     __syncthreads();
-    if (threadIdx.x == 0) y[s] = cmul(y[s], crcp(LU[(size_t)(k0 + s) * lda + k0 + s]));
-    __syncthreads();
-    const T xs = y[s];
+    const T xs = cmul(y[s], rd[s]);
     const int r = threadIdx.x;
-    if (r < s) y[r] = cfms(y[r], LU[(size_t)(k0 + s) * lda + k0 + r], xs);
+    if (r < s) y[r] = cfms(y[r], D[s * kNB + r], xs);
+    __syncthreads();
+    if (r == s) y[s] = xs;
   }
   __syncthreads();
   if (threadIdx.x < nb) b[k0 + threadIdx.x] = y[threadIdx.x];
@@ -464,9 +484,16 @@ __global__ void bwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0,
 template <typename T>
 void lu_solve(const T* LU, long long lda, int n, const int* ipiv, T* b, cudaStream_t s,
               long long* launches) {
+  const size_t dsm = sizeof(T) * (kNB * kNB + 2 * kNB);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(fwd_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+    cudaFuncSetAttribute(bwd_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+    attr = true;
+  }
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = std::min(kNB, n - k0);
-    fwd_diag_kernel<T><<<1, kNB, 0, s>>>(LU, lda, k0, nb, ipiv, b);
+    fwd_diag_kernel<T><<<1, kNB, dsm, s>>>(LU, lda, k0, nb, ipiv, b);
     ++*launches;
     const int r0 = k0 + nb;
     if (r0 < n) {
@@ -477,7 +504,7 @@ void lu_solve(const T* LU, long long lda, int n, const int* ipiv, T* b, cudaStre
   const int last = ((n - 1) / kNB) * kNB;
   for (int k0 = last; k0 >= 0; k0 -= kNB) {
     const int nb = std::min(kNB, n - k0);
-    bwd_diag_kernel<T><<<1, kNB, 0, s>>>(LU, lda, k0, nb, b);
+    bwd_diag_kernel<T><<<1, kNB, dsm, s>>>(LU, lda, k0, nb, b);
     ++*launches;
     if (k0 > 0) {
       gemv_sub_kernel<T><<<(k0 + 127) / 128, 128, 0, s>>>(LU, lda, k0, nb, 0, k0, b);

@@ -45,6 +45,11 @@ def workload(name):
         return dict(g=g, k=100.0, eta=100.0, d=(math.cos(th), math.sin(th)),
                     desc="kite N=2048 equispaced, k=100, eta=k, plane wave angle "
                          "%.15g (rng seed 0), QuadOption{3,5,0.15}" % th)
+    if name == "kite4096":
+        th = float(np.random.default_rng(0).uniform(0, 2 * math.pi))
+        g = G.kite(4096).add_poly_basis(0)
+        return dict(g=g, k=100.0, eta=100.0, d=(math.cos(th), math.sin(th)),
+                    desc="kite N=4096 equispaced, k=100, eta=k (profiling case)")
     if name == "disk160":
         g = G.curve_equispaced(G.CIRCLE, 160).add_poly_basis(0)
         return dict(g=g, k=10.0, eta=10.0, d=(1.0, 0.0),
@@ -153,6 +158,28 @@ def run_reference(args):
                                    "of the reference + scipy LAPACK zgetrf/zgetrs)"},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}))
+
+
+def run_only(args):
+    """Profiling driver: one phase only (assembly or solve), no JSON line."""
+    import torch
+    from bem2d_gb300 import capi
+    w = workload(args.workload)
+    n = w["g"].n_unknowns
+    arrays = w["g"].arrays()
+    ctx = capi.Context(0)
+    ctx.enable_timers(True)
+    A = torch.empty((n, n), dtype=torch.complex128, device="cuda")
+    x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    for _ in range(args.warmup + args.steps):
+        if args.only == "assembly":
+            ctx.discrete_kernel(arrays, "combined", w["k"], w["eta"], QUAD, 2.0, 1.0, out=A)
+        else:
+            ctx.scattering_solve(arrays, w["k"], w["d"], w["eta"], QUAD,
+                                 precision=args.only, out=x)
+    torch.cuda.synchronize()
+    print(json.dumps({"only": args.only, "workload": args.workload,
+                      "timers_ms": {k: v[0] / max(v[1], 1) for k, v in ctx.timers().items()}}))
 
 
 def run_ours(args):
@@ -297,8 +324,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="kite2048")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--only", choices=["assembly", "mixed", "fp64"],
+                    help="profiling driver: run one phase, print its timers")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

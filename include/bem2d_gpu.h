@@ -152,8 +152,10 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* ctx, const bem2d_geometry* geom,
  * LAPACK zgetrf + zgetrs).  A (n x n, lda) and b are not modified.
  * BEM2D_PREC_FP64: blocked complex128 LU with partial pivoting.
  * BEM2D_PREC_MIXED: complex64 LU with partial pivoting, then FP64 iterative
- *   refinement with the complex128 A until residual <= tol (tol <= 0 selects
- *   1e-12), at most 30 steps. */
+ *   refinement with the complex128 A until the backward error
+ *   ||b - A x|| / (||A||_F ||x|| + ||b||) <= tol (tol <= 0 selects 1e-14);
+ *   if progress stalls first, a backward error <= max(tol, 1e-12) is
+ *   accepted, otherwise BEM2D_ERR_NOCONV.  At most 30 steps. */
 int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
                        const void* b, void* x, int precision, double tol,
                        bem2d_solve_info* info);
