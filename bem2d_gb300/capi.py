@@ -26,7 +26,8 @@ PREC = {"fp64": 0, "mixed": 1}
 # symbols declared in include/bem2d_gpu.h
 EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_ctx_stream", "bem2d_ctx_set_stream", "bem2d_ctx_launch_count",
-           "bem2d_gauss", "bem2d_discrete_kernel", "bem2d_eval_ident",
+           "bem2d_gauss", "bem2d_discrete_kernel", "bem2d_discrete_kernel_mixed",
+           "bem2d_eval_ident",
            "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
            "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer"]
 
@@ -84,6 +85,8 @@ def load():
         lib.bem2d_ctx_launch_count.restype = i64
         lib.bem2d_gauss.argtypes = [i32, vp, vp]
         lib.bem2d_discrete_kernel.argtypes = [vp, vp, vp, i32, d, d, d, d, d, vp, i64]
+        lib.bem2d_discrete_kernel_mixed.argtypes = [vp, vp, vp, i32, d, d, d, d, d, vp, i64,
+                                                    vp, i64]
         lib.bem2d_eval_ident.argtypes = [vp, vp, vp, vp, i64]
         lib.bem2d_dot_prod_basfuns.argtypes = [vp, vp, vp, i32, d, d, d, d, d, d, vp]
         lib.bem2d_solve_system.argtypes = [vp, i32, vp, i64, vp, vp, i32, d, vp]
@@ -185,6 +188,20 @@ class Context:
             self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
             eta, float(alpha), float(beta), _ptr(out), ld))
         return out
+
+    def discrete_kernel_mixed(self, g, kernel="combined", k=10.0, eta=None, q=(3, 5, 0.15),
+                              alpha=1.0, beta=0.0):
+        """Mixed-precision assembly: (complex128, complex64) host matrices."""
+        gh = _GeomHold(g)
+        n = gh.n
+        out = np.zeros((n, n), dtype=np.complex128, order="F")
+        out32 = np.zeros((n, n), dtype=np.complex64, order="F")
+        eta = float(k) if eta is None else float(eta)
+        qq = quad(q)
+        self._check(self.lib.bem2d_discrete_kernel_mixed(
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
+            eta, float(alpha), float(beta), _ptr(out), n, _ptr(out32), n))
+        return out, out32
 
     def eval_ident(self, g, q=(3, 5, 0.15), out=None):
         gh = _GeomHold(g)

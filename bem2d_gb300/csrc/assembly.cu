@@ -13,30 +13,56 @@
 //  ident_kernel       EvalIdent (lib/bem2d_quadrature.cpp:79-127)
 //  rhs_kernel         DotProdBasFuns (lib/bem2d_quadrature.h:111-156)
 #include "common.cuh"
+#include "ff.cuh"
 
 namespace bem2d_gpu {
 
 // ---------------------------------------------------------------------------
-__global__ void node_table_kernel(DevGeom g, DevRules r, NodeTable t) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= g.n_unk * r.ng) return;
-  const int u = idx / r.ng, q = idx - u * r.ng;
+// One thread per unknown: Map, Normal and |J| w phi at each Gauss node (FP64
+// table); optionally the float-float table relative to the element centre
+// Map(1/2).
+__global__ void node_table_kernel(DevGeom g, DevRules r, NodeTable t, NodeTableFF tf,
+                                  int want_ff) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= g.n_unk) return;
   const int e = g.unk_elem[u];
-  const double tq = r.gx[q];
-  const ElemPt p = elem_eval(g.kind[e], g.param + 8 * (size_t)e, tq);
-  double nx, ny;
-  elem_normal(p, &nx, &ny);
-  t.x[idx] = p.mx;
-  t.y[idx] = p.my;
-  t.nx[idx] = nx;
-  t.ny[idx] = ny;
-  t.w[idx] = elem_jac(p) * r.gw[q] * basis_eval(g.unk_kind[u], g.unk_param[u], tq);
+  const double* prm = g.param + 8 * (size_t)e;
+  const ElemPt mid = elem_eval(g.kind[e], prm, 0.5);
+  float rad = 0.0f;
+  for (int q = 0; q < r.ng; ++q) {
+    const size_t idx = (size_t)u * r.ng + q;
+    const double tq = r.gx[q];
+    const ElemPt p = elem_eval(g.kind[e], prm, tq);
+    double nx, ny;
+    elem_normal(p, &nx, &ny);
+    const double w = elem_jac(p) * r.gw[q] * basis_eval(g.unk_kind[u], g.unk_param[u], tq);
+    t.x[idx] = p.mx;
+    t.y[idx] = p.my;
+    t.nx[idx] = nx;
+    t.ny[idx] = ny;
+    t.w[idx] = w;
+    if (want_ff) {
+      const double ox = p.mx - mid.mx, oy = p.my - mid.my;
+      const ff fox = ff_from_double(ox), foy = ff_from_double(oy);
+      const ff fnx = ff_from_double(nx), fny = ff_from_double(ny), fw = ff_from_double(w);
+      tf.ox[idx] = make_float2(fox.hi, fox.lo);
+      tf.oy[idx] = make_float2(foy.hi, foy.lo);
+      tf.nx[idx] = make_float2(fnx.hi, fnx.lo);
+      tf.ny[idx] = make_float2(fny.hi, fny.lo);
+      tf.w[idx] = make_float2(fw.hi, fw.lo);
+      rad = fmaxf(rad, (float)sqrt(ox * ox + oy * oy));
+    }
+  }
+  if (want_ff) {
+    tf.c[u] = make_double2(mid.mx, mid.my);
+    tf.rad[u] = rad * (1.0f + 1e-6f);
+  }
 }
 
 void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
-                       cudaStream_t s) {
-  const int n = g.n_unk * r.ng;
-  node_table_kernel<<<(n + 255) / 256, 256, 0, s>>>(g, r, t);
+                       const NodeTableFF* tf, cudaStream_t s) {
+  NodeTableFF z{};
+  node_table_kernel<<<(g.n_unk + 127) / 128, 128, 0, s>>>(g, r, t, tf ? *tf : z, tf ? 1 : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -205,7 +231,8 @@ template <int KERNEL>
 __global__ void __launch_bounds__(256)
 near_fp64_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs,
                  int npairs, double k, double eta, double alpha, double beta,
-                 double2* __restrict__ out, long long ld) {
+                 double2* __restrict__ out, long long ld, float2* __restrict__ out32,
+                 long long ld32) {
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (wid >= npairs) return;
@@ -243,26 +270,28 @@ near_fp64_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs,
     double re = alpha * acc_re, im = alpha * acc_im;
     if (pr.same && beta != 0.0) re = fma(beta, mass_entry(g, r, pr.i, pr.j), re);
     out[(size_t)pr.j * ld + pr.i] = make_double2(re, im);
+    if (out32) out32[(size_t)pr.j * ld32 + pr.i] = make_float2((float)re, (float)im);
   }
 }
 
 void launch_near_fp64(const DevGeom& g, const DevRules& r, const NearPair* pairs,
                       int npairs, int kernel, double k, double eta, double alpha,
-                      double beta, double2* out, long long ld, cudaStream_t s) {
+                      double beta, double2* out, long long ld, cudaStream_t s,
+                      float2* out32, long long ld32) {
   if (npairs == 0) return;
   const int blocks = (npairs * 32 + 255) / 256;
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      near_fp64_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld);
+      near_fp64_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
       break;
     case BEM2D_KERNEL_DOUBLE:
-      near_fp64_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld);
+      near_fp64_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
       break;
     case BEM2D_KERNEL_CONJDOUBLE:
-      near_fp64_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld);
+      near_fp64_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
       break;
     default:
-      near_fp64_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld);
+      near_fp64_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
   }
 }
 

@@ -1,0 +1,295 @@
+// Mixed-precision far-field assembly (sm_103a): the bulk of the Galerkin
+// matrix evaluated in float-float arithmetic on the FP32 pipe.
+//
+// Same tiling as the FP64 far kernel (32 x 32 tiles, one lane per test
+// unknown, node data staged in shared memory).  Pair geometry: the centre
+// difference of the two elements in FP64, node offsets from the centres in
+// float-float, so |x - y| keeps ~48 bits relative to itself even for
+// neighbouring elements.  Entries whose element pair admits k|x - y| <= 8
+// anywhere (bounded with the element radii) are deferred to an FP64 pass,
+// where the small-argument Hankel pieces live; adjacent and identical pairs
+// belong to the FP64 near-field kernel as in the FP64 path.  Each entry is
+// stored twice: complex128 (refinement residual) and complex64 (the LU).
+#include "common.cuh"
+#include "ff.cuh"
+#include "hankel_ff.cuh"
+
+namespace bem2d_gpu {
+
+struct KConstFF {
+  ff k, invk, kq, eq, amp0;
+};
+
+template <int KERNEL>
+__device__ __forceinline__ ffc kernel_ff(ff dx, ff dy, ff n1x, ff n1y, ff n2x, ff n2y,
+                                         const KConstFF& kc, const float* tab) {
+  const ff d2 = ff_add_fast(ff_sqr(dx), ff_sqr(dy));
+  const ff y = ff_rsqrt(d2);  // 1/d
+  const ff d = ff_mul(d2, y);
+  const ff x = ff_mul(d, kc.k);
+  const ff ix = ff_mul(y, kc.invk);
+  ff p0, q0, p1, q1;
+  pq_ff(x.hi, ix, &p0, &q0, &p1, &q1);
+  const ff amp = ff_mul(kc.amp0, ff_sqrt(ix));
+  const ffc e = expi_ff(x, tab);
+  ffc F;
+  if (KERNEL == BEM2D_KERNEL_SINGLE) {
+    // (i/4) H0:  F = (i/4)(P0 + i Q0)
+    F.re = ff_scale2(ff_neg(q0), 0.25f);
+    F.im = ff_scale2(p0, 0.25f);
+  } else {
+    ff dot;
+    if (KERNEL == BEM2D_KERNEL_DOUBLE)
+      dot = ff_neg(ff_add_fast(ff_mul(n2x, dx), ff_mul(n2y, dy)));
+    else
+      dot = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));
+    const ff cc = ff_mul(ff_mul(dot, y), kc.kq);  // (k/4) n.w/d
+    // -i (k/4) c H1 with H1 = -i amp (P1 + i Q1) E  ->  -(k/4) c (P1 + i Q1)
+    F.re = ff_neg(ff_mul(cc, p1));
+    F.im = ff_neg(ff_mul(cc, q1));
+    if (KERNEL == BEM2D_KERNEL_COMBINED) {
+      F.re = ff_add_fast(F.re, ff_mul(kc.eq, p0));
+      F.im = ff_add_fast(F.im, ff_mul(kc.eq, q0));
+    }
+  }
+  // K = amp E F
+  ffc K;
+  K.re = ff_mul(amp, ff_add_fast(ff_mul(e.re, F.re), ff_neg(ff_mul(e.im, F.im))));
+  K.im = ff_mul(amp, ff_add_fast(ff_mul(e.re, F.im), ff_mul(e.im, F.re)));
+  return K;
+}
+
+// One entry in FP64 from the FP64 node table (deferred entries).
+template <int KERNEL>
+__device__ __forceinline__ void entry_fp64(const NodeTable& t, int ng, int row, int col,
+                                           double k, double kq, double eq, double* re,
+                                           double* im) {
+  double ar = 0.0, ai = 0.0;
+  for (int q1 = 0; q1 < ng; ++q1) {
+    const size_t a = (size_t)row * ng + q1;
+    const double x1 = t.x[a], y1 = t.y[a], n1x = t.nx[a], n1y = t.ny[a], w1 = t.w[a];
+    for (int q2 = 0; q2 < ng; ++q2) {
+      const size_t b = (size_t)col * ng + q2;
+      double vr, vi;
+      kernel_d<KERNEL>(k, kq, eq, x1, y1, t.x[b], t.y[b], n1x, n1y, t.nx[b], t.ny[b], &vr, &vi);
+      const double ww = w1 * t.w[b];
+      ar = fma(vr, ww, ar);
+      ai = fma(vi, ww, ai);
+    }
+  }
+  *re = ar;
+  *im = ai;
+}
+
+constexpr int kTileF = 32;
+constexpr int kFarFFThreads = 256;
+constexpr float kDeferX = 8.001f;
+
+template <int KERNEL, int NG>
+__global__ void __launch_bounds__(kFarFFThreads)
+far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, double k,
+              double eta, double alpha, double2* __restrict__ out, long long ld,
+              float2* __restrict__ out32, long long ld32, DeferList dl, const float* gtab) {
+  const int ng = NG > 0 ? NG : ng_rt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* tab = reinterpret_cast<float*>(smem_raw);             // 256
+  double2* cen = reinterpret_cast<double2*>(tab + 256);        // rows 32, cols 32
+  float2* rs = reinterpret_cast<float2*>(cen + 2 * kTileF);    // [5][ng][32]
+  float2* cs = rs + 5 * ng * kTileF;                           // [5][ng][32]
+  float* rad = reinterpret_cast<float*>(cs + 5 * ng * kTileF); // rows 32, cols 32
+  long long* links = reinterpret_cast<long long*>(rad + 2 * kTileF);  // 4 x 32
+
+  const int row0 = blockIdx.x * kTileF, col0 = blockIdx.y * kTileF;
+  const int n = g.n_unk;
+  for (int v = threadIdx.x; v < 256; v += blockDim.x) tab[v] = gtab[v];
+  const int SZ = ng * kTileF;
+  for (int v = threadIdx.x; v < SZ; v += blockDim.x) {
+    const int q = v / kTileF, l = v - q * kTileF;
+    const int ur = min(row0 + l, n - 1), uc = min(col0 + l, n - 1);
+    const size_t ir = (size_t)ur * ng + q, ic = (size_t)uc * ng + q;
+    const int o = q * kTileF + l;
+    rs[o] = tf.ox[ir];
+    rs[SZ + o] = tf.oy[ir];
+    rs[2 * SZ + o] = tf.nx[ir];
+    rs[3 * SZ + o] = tf.ny[ir];
+    rs[4 * SZ + o] = tf.w[ir];
+    cs[o] = tf.ox[ic];
+    cs[SZ + o] = tf.oy[ic];
+    cs[2 * SZ + o] = tf.nx[ic];
+    cs[3 * SZ + o] = tf.ny[ic];
+    cs[4 * SZ + o] = tf.w[ic];
+  }
+  if (threadIdx.x < kTileF) {
+    const int l = threadIdx.x;
+    const int ur = min(row0 + l, n - 1), uc = min(col0 + l, n - 1);
+    cen[l] = tf.c[ur];
+    cen[kTileF + l] = tf.c[uc];
+    rad[l] = tf.rad[ur];
+    rad[kTileF + l] = tf.rad[uc];
+    const int er = g.unk_elem[ur], ec = g.unk_elem[uc];
+    links[l] = g.index[er];
+    links[kTileF + l] = g.next[er];
+    links[2 * kTileF + l] = g.prev[er];
+    links[3 * kTileF + l] = g.index[ec];
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int row = row0 + lane;
+  const long long ri = links[lane], rn = links[kTileF + lane], rp = links[2 * kTileF + lane];
+  const double2 crow = cen[lane];
+  const float rrow = rad[lane];
+  const float kf = (float)k;
+
+#pragma unroll 1
+  for (int cc = warp; cc < kTileF; cc += kFarFFThreads / 32) {
+    const int col = col0 + cc;
+    const long long ci = links[3 * kTileF + cc];
+    const bool near = (ri == ci) || (rn == ci) || (rp == ci);
+    if (row >= n || col >= n || near) continue;
+    const double dxc = crow.x - cen[kTileF + cc].x, dyc = crow.y - cen[kTileF + cc].y;
+    const float dist = sqrtf((float)(dxc * dxc + dyc * dyc));
+    if (kf * (dist * (1.0f - 1e-6f) - rrow - rad[kTileF + cc]) <= kDeferX) {
+      // small arguments somewhere on this pair: FP64 pass (or here, if the
+      // list is full)
+      const unsigned slot = atomicAdd(dl.count, 1u);
+      if (slot < dl.capacity) {
+        dl.ij[slot] = make_int2(row, col);
+      } else {
+        double re, im;
+        entry_fp64<KERNEL>(t, ng, row, col, k, 0.25 * k, 0.25 * eta, &re, &im);
+        out[(size_t)col * ld + row] = make_double2(alpha * re, alpha * im);
+        out32[(size_t)col * ld32 + row] = make_float2((float)(alpha * re), (float)(alpha * im));
+      }
+      continue;
+    }
+    const ff Dx = ff_from_double(dxc), Dy = ff_from_double(dyc);
+    ffc acc;
+    acc.re = ff_make(0.0f, 0.0f);
+    acc.im = ff_make(0.0f, 0.0f);
+#pragma unroll 1
+    for (int q1 = 0; q1 < ng; ++q1) {
+      const int o1 = q1 * kTileF + lane;
+      const float2 a0 = rs[o1], a1 = rs[SZ + o1], a2 = rs[2 * SZ + o1], a3 = rs[3 * SZ + o1],
+                   a4 = rs[4 * SZ + o1];
+      const ff ox1 = ff_make(a0.x, a0.y), oy1 = ff_make(a1.x, a1.y);
+      const ff n1x = ff_make(a2.x, a2.y), n1y = ff_make(a3.x, a3.y), w1 = ff_make(a4.x, a4.y);
+#pragma unroll 1
+      for (int q2 = 0; q2 < ng; ++q2) {
+        const int o2 = q2 * kTileF + cc;
+        const float2 b0 = cs[o2], b1 = cs[SZ + o2], b2 = cs[2 * SZ + o2], b3 = cs[3 * SZ + o2],
+                     b4 = cs[4 * SZ + o2];
+        const ff dx = ff_add_fast(Dx, ff_add_fast(ox1, ff_make(-b0.x, -b0.y)));
+        const ff dy = ff_add_fast(Dy, ff_add_fast(oy1, ff_make(-b1.x, -b1.y)));
+        const ffc K = kernel_ff<KERNEL>(dx, dy, n1x, n1y, ff_make(b2.x, b2.y),
+                                        ff_make(b3.x, b3.y), kc, tab);
+        const ff ww = ff_mul(w1, ff_make(b4.x, b4.y));
+        acc.re = ff_add_fast(acc.re, ff_mul(K.re, ww));
+        acc.im = ff_add_fast(acc.im, ff_mul(K.im, ww));
+      }
+    }
+    const double re = alpha * ff_to_double(acc.re), im = alpha * ff_to_double(acc.im);
+    out[(size_t)col * ld + row] = make_double2(re, im);
+    out32[(size_t)col * ld32 + row] = make_float2((float)re, (float)im);
+  }
+}
+
+template <int KERNEL>
+__global__ void deferred_fp64_kernel(NodeTable t, int ng, double k, double eta, double alpha,
+                                     const int2* __restrict__ ij, const unsigned* count,
+                                     unsigned cap, double2* __restrict__ out, long long ld,
+                                     float2* __restrict__ out32, long long ld32) {
+  const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= min(*count, cap)) return;
+  const int2 e = ij[p];
+  double re, im;
+  entry_fp64<KERNEL>(t, ng, e.x, e.y, k, 0.25 * k, 0.25 * eta, &re, &im);
+  re *= alpha;
+  im *= alpha;
+  out[(size_t)e.y * ld + e.x] = make_double2(re, im);
+  out32[(size_t)e.y * ld32 + e.x] = make_float2((float)re, (float)im);
+}
+
+static const float* expi_table_dev() {
+  static float* d = nullptr;  // per process; one device
+  if (!d) {
+    float h[256];
+    expi_table(h);
+    cudaMalloc(&d, sizeof h);
+    cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
+  }
+  return d;
+}
+
+template <int KERNEL>
+static void launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+                            double k, double eta, double alpha, double2* out, long long ld,
+                            float2* out32, long long ld32, DeferList dl, cudaStream_t s) {
+  KConstFF kc;
+  kc.k = ff_from_double(k);
+  kc.invk = ff_from_double(1.0 / k);
+  kc.kq = ff_from_double(0.25 * k);
+  kc.eq = ff_from_double(0.25 * eta);
+  kc.amp0 = ff_from_double(0.79788456080286535588);  // sqrt(2/pi)
+  const size_t smem = sizeof(float) * 256 + sizeof(double2) * 2 * kTileF +
+                      sizeof(float2) * 10 * ng * kTileF + sizeof(float) * 2 * kTileF +
+                      sizeof(long long) * 4 * kTileF;
+  dim3 grid((g.n_unk + kTileF - 1) / kTileF, (g.n_unk + kTileF - 1) / kTileF);
+  const float* tab = expi_table_dev();
+  if (ng == 5) {
+    far_ff_kernel<KERNEL, 5><<<grid, kFarFFThreads, smem, s>>>(g, t, tf, ng, kc, k, eta, alpha, out,
+                                                               ld, out32, ld32, dl, tab);
+  } else {
+    auto fn = far_ff_kernel<KERNEL, 0>;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<grid, kFarFFThreads, smem, s>>>(g, t, tf, ng, kc, k, eta, alpha, out, ld, out32, ld32, dl,
+                                         tab);
+  }
+}
+
+void launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+                   int kernel, double k, double eta, double alpha, double2* out,
+                   long long ld, float2* out32, long long ld32, DeferList dl,
+                   cudaStream_t s) {
+  switch (kernel) {
+    case BEM2D_KERNEL_SINGLE:
+      launch_far_ff_k<BEM2D_KERNEL_SINGLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
+      break;
+    case BEM2D_KERNEL_DOUBLE:
+      launch_far_ff_k<BEM2D_KERNEL_DOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
+      break;
+    case BEM2D_KERNEL_CONJDOUBLE:
+      launch_far_ff_k<BEM2D_KERNEL_CONJDOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl,
+                                               s);
+      break;
+    default:
+      launch_far_ff_k<BEM2D_KERNEL_COMBINED>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
+  }
+}
+
+// Grid sized by the list capacity; threads beyond the device-side count exit.
+void launch_deferred_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                          double eta, double alpha, const DeferList& dl, unsigned n,
+                          double2* out, long long ld, float2* out32, long long ld32,
+                          cudaStream_t s) {
+  (void)g;
+  (void)n;
+  if (dl.capacity == 0) return;
+  const unsigned blocks = (dl.capacity + 127) / 128;
+  switch (kernel) {
+    case BEM2D_KERNEL_SINGLE:
+      deferred_fp64_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      break;
+    case BEM2D_KERNEL_DOUBLE:
+      deferred_fp64_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      break;
+    case BEM2D_KERNEL_CONJDOUBLE:
+      deferred_fp64_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      break;
+    default:
+      deferred_fp64_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+  }
+}
+
+}  // namespace bem2d_gpu

@@ -264,6 +264,8 @@ struct Staged {
   DevGeom g;
   DevRules r;
   NodeTable t;
+  NodeTableFF tf;
+  bool has_ff = false;
   NearPair* pairs;
   int npairs;
 };
@@ -325,7 +327,7 @@ static std::vector<NearPair> near_pairs(const bem2d_geometry* g) {
 }
 
 static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, bool nodes,
-                 bool pairs, Staged* st) {
+                 bool pairs, Staged* st, bool ff_nodes = false) {
   int rc = check_geom(c, g);
   if (rc) return rc;
   if ((rc = check_quad(c, q))) return rc;
@@ -381,7 +383,17 @@ static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, boo
     double* t = static_cast<double*>(ws(c, "nodes", sizeof(double) * 5 * nn, &rc));
     if (!t) return rc;
     st->t = NodeTable{t, t + nn, t + 2 * nn, t + 3 * nn, t + 4 * nn};
-    launch_node_table(dg, st->r, st->t, c->stream);
+    st->has_ff = ff_nodes;
+    if (ff_nodes) {
+      const size_t bytes = sizeof(float2) * 5 * nn + sizeof(double2) * nu + sizeof(float) * nu;
+      char* f = static_cast<char*>(ws(c, "nodes_ff", bytes, &rc));
+      if (!f) return rc;
+      float2* f2 = reinterpret_cast<float2*>(f);
+      double2* cen = reinterpret_cast<double2*>(f2 + 5 * nn);
+      st->tf = NodeTableFF{f2, f2 + nn, f2 + 2 * nn, f2 + 3 * nn, f2 + 4 * nn, cen,
+                           reinterpret_cast<float*>(cen + nu)};
+    }
+    launch_node_table(dg, st->r, st->t, ff_nodes ? &st->tf : nullptr, c->stream);
     ++c->launches;
     CHECK_LAUNCH(c);
   }
@@ -408,6 +420,39 @@ static int assemble_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, do
   t = tic(c, BEM2D_PHASE_NEAR);
   launch_near_fp64(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
                    c->stream);
+  toc(c, t);
+  if (st.npairs) ++c->launches;
+  CHECK_LAUNCH(c);
+  return BEM2D_OK;
+}
+
+// Mixed assembly: float-float far field + FP64 deferred and near-field
+// entries, into a complex128 (A, ld) and a complex64 (A32, ld32) matrix.
+static int assemble_mixed_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, double eta,
+                              double alpha, double beta, double2* A, long long ld, float2* A32,
+                              long long ld32) {
+  const long long n = st.g.n_unk;
+  const unsigned cap = (unsigned)std::min<long long>(
+      n * n, std::max<long long>(1 << 20, n * n / 8));
+  int rc = 0;
+  char* d = static_cast<char*>(ws(c, "defer", sizeof(int2) * (size_t)cap + 256, &rc));
+  if (!d) return rc;
+  DeferList dl;
+  dl.count = reinterpret_cast<unsigned*>(d);
+  dl.ij = reinterpret_cast<int2*>(d + 256);
+  dl.capacity = cap;
+  CUDA_TRY(c, cudaMemsetAsync(dl.count, 0, sizeof(unsigned), c->stream));
+  int t = tic(c, BEM2D_PHASE_FAR);
+  launch_far_ff(st.g, st.t, st.tf, st.r.ng, kernel, k, eta, alpha, A, ld, A32, ld32, dl,
+                c->stream);
+  launch_deferred_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, dl, 0, A, ld, A32, ld32,
+                       c->stream);
+  toc(c, t);
+  c->launches += 2;
+  CHECK_LAUNCH(c);
+  t = tic(c, BEM2D_PHASE_NEAR);
+  launch_near_fp64(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
+                   c->stream, A32, ld32);
   toc(c, t);
   if (st.npairs) ++c->launches;
   CHECK_LAUNCH(c);
@@ -529,6 +574,42 @@ int bem2d_discrete_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_
   });
 }
 
+int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
+                                const bem2d_quad* quad, int kernel, double k_re, double k_im,
+                                double eta, double alpha, double beta, void* out, int64_t ld,
+                                void* out32, int64_t ld32) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (kernel < BEM2D_KERNEL_SINGLE || kernel > BEM2D_KERNEL_COMBINED)
+    return fail(c, BEM2D_ERR_ARG, "unknown kernel %d", kernel);
+  int rc = check_k(c, k_re, k_im);
+  if (rc) return rc;
+  if (!(k_re > 0)) return fail(c, BEM2D_ERR_ARG, "mixed assembly needs k > 0");
+  if (!out || !out32) return fail(c, BEM2D_ERR_ARG, "output pointer is NULL");
+  cudaSetDevice(c->device);
+  Staged st;
+  if ((rc = stage(c, geom, quad, true, true, &st, true))) return rc;
+  const int n = geom->n_unk;
+  if (ld < n || ld32 < n) return fail(c, BEM2D_ERR_ARG, "leading dimension < %d", n);
+  const bool d64 = is_device_ptr(out), d32 = is_device_ptr(out32);
+  double2* A = d64 ? static_cast<double2*>(out)
+                   : static_cast<double2*>(ws(c, "out", sizeof(double2) * (size_t)n * n, &rc));
+  if (!A) return rc;
+  float2* B = d32 ? static_cast<float2*>(out32)
+                  : static_cast<float2*>(ws(c, "out32", sizeof(float2) * (size_t)n * n, &rc));
+  if (!B) return rc;
+  const long long la = d64 ? ld : n, lb = d32 ? ld32 : n;
+  if ((rc = assemble_mixed_dev(c, st, kernel, k_re, eta, alpha, beta, A, la, B, lb))) return rc;
+  if (!d64)
+    CUDA_TRY(c, cudaMemcpy2DAsync(out, sizeof(double2) * ld, A, sizeof(double2) * n,
+                                  sizeof(double2) * n, n, cudaMemcpyDeviceToHost, c->stream));
+  if (!d32)
+    CUDA_TRY(c, cudaMemcpy2DAsync(out32, sizeof(float2) * ld32, B, sizeof(float2) * n,
+                                  sizeof(float2) * n, n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  resolve_timers(c);
+  return BEM2D_OK;
+}
+
 int bem2d_eval_ident(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
                      void* out, int64_t ld) {
   if (!c) return BEM2D_ERR_ARG;
@@ -577,20 +658,32 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
 namespace bem2d_gpu {
 
 // Solve with device-resident A (lda) and b; x written to device memory.
+// A32pre: a complex64 copy of A already in the "lu32" workspace (mixed
+// assembly writes it); otherwise A is converted here.
 static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const double2* b,
-                     double2* x, int precision, double tol, bem2d_solve_info* info) {
+                     double2* x, int precision, double tol, bem2d_solve_info* info,
+                     bool a32_ready = false) {
   int rc = 0;
   bem2d_solve_info rep{0, 0, 0.0};
   LuWork w;
+  // ints: [0] info [1] status [8, 8+n) ipiv
   int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
   if (!ints) return rc;
   w.ipiv = ints + 8;
   w.info = ints;
   w.status = ints + 1;
-  w.barrier = reinterpret_cast<unsigned*>(ints + 2);
   w.scratch_bytes = lu_scratch_bytes(n);
   w.scratch = ws(c, "lu_scratch", w.scratch_bytes, &rc);
   if (!w.scratch) return rc;
+  char* aux = static_cast<char*>(
+      ws(c, "lu_aux", lu_aux_bytes(n, precision == BEM2D_PREC_FP64 ? sizeof(double2)
+                                                                  : sizeof(float2)), &rc));
+  if (!aux) return rc;
+  w.dinv = aux;
+  w.perm = reinterpret_cast<int*>(aux + (lu_aux_bytes(n, precision == BEM2D_PREC_FP64
+                                                             ? sizeof(double2)
+                                                             : sizeof(float2)) -
+                                         256 - sizeof(int) * (size_t)n));
   int hinfo[2] = {0, 0};
   if (precision == BEM2D_PREC_FP64) {
     double2* LU = static_cast<double2*>(ws(c, "lu64", sizeof(double2) * (size_t)n * n, &rc));
@@ -608,12 +701,14 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
     rep.info = hinfo[0];
     if (info) *info = rep;
     if (hinfo[0]) return fail(c, hinfo[0], "zero pivot at column %d", hinfo[0]);
-    if (x != b) CUDA_TRY(c, cudaMemcpyAsync(x, b, sizeof(double2) * n, cudaMemcpyDeviceToDevice, c->stream));
     t = tic(c, BEM2D_PHASE_SOLVE);
-    lu_solve<double2>(LU, n, n, w.ipiv, x, c->stream, &c->launches);
+    if ((rc = lu_solve<double2>(LU, n, n, w, b, x, c->stream, &c->launches)))
+      return fail(c, rc, "triangular solve launch: %s", cudaGetErrorString(cudaGetLastError()));
     toc(c, t);
     CHECK_LAUNCH(c);
+    CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "triangular solve wait timed out");
     resolve_timers(c);
     return BEM2D_OK;
   }
@@ -630,8 +725,10 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
   double* red = static_cast<double*>(ws(c, "ir_red", sumsq_part_bytes() + 64, &rc));
   if (!r || !d || !part || !red) return rc;
   double* scal = red + sumsq_part_bytes() / sizeof(double);  // [0] |A|^2 [1] |b|^2 [2] |r|^2 [3] |x|^2
-  launch_to_c64(A, lda, LU, n, n, n, c->stream);
-  ++c->launches;
+  if (!a32_ready) {
+    launch_to_c64(A, lda, LU, n, n, n, c->stream);
+    ++c->launches;
+  }
   launch_sumsq(A, lda, n, n, red, scal, c->stream);
   launch_sumsq(b, n, n, 1, red, scal + 1, c->stream);
   c->launches += 4;
@@ -682,7 +779,8 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
     // d = LU32^{-1} (r / |r|);  x += |r| d;  r = b - A x
     const int ts = tic(c, BEM2D_PHASE_SOLVE);
     launch_scale_to_c64(n, r, 1.0 / rnorm, d, c->stream);
-    lu_solve<float2>(LU, n, n, w.ipiv, d, c->stream, &c->launches);
+    if ((rc = lu_solve<float2>(LU, n, n, w, d, d, c->stream, &c->launches)))
+      return fail(c, rc, "triangular solve launch: %s", cudaGetErrorString(cudaGetLastError()));
     launch_axpy_c64(n, rnorm, d, x, c->stream);
     launch_residual(A, lda, n, x, b, r, part, c->stream);
     launch_sumsq(r, n, n, 1, red, scal + 2, c->stream);
@@ -691,7 +789,9 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
     c->launches += 8;
     CHECK_LAUNCH(c);
     CUDA_TRY(c, cudaMemcpyAsync(hs, scal, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "triangular solve wait timed out");
     rnorm = std::sqrt(hs[2]);
     xnorm = std::sqrt(hs[3]);
   }
@@ -757,13 +857,21 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   if (rc) return rc;
   cudaSetDevice(c->device);
   Staged st;
-  if ((rc = stage(c, geom, quad, true, true, &st))) return rc;
+  if ((rc = stage(c, geom, quad, true, true, &st, precision == BEM2D_PREC_MIXED))) return rc;
   const int n = geom->n_unk;
   double2* A = static_cast<double2*>(ws(c, "sys_A", sizeof(double2) * (size_t)n * n, &rc));
   if (!A) return rc;
   double2* b = static_cast<double2*>(ws(c, "sys_b", sizeof(double2) * n, &rc));
   if (!b) return rc;
-  if ((rc = assemble_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n))) return rc;
+  const bool mixed = precision == BEM2D_PREC_MIXED;
+  if (mixed) {
+    float2* A32 = static_cast<float2*>(ws(c, "lu32", sizeof(float2) * (size_t)n * n, &rc));
+    if (!A32) return rc;
+    if ((rc = assemble_mixed_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n, A32, n)))
+      return rc;
+  } else if ((rc = assemble_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n))) {
+    return rc;
+  }
   launch_rhs(st.g, st.t, st.r.ng, BEM2D_FUN_COMBINEDPLANEWAVE, k_re, dir_x, dir_y, eta, 2.0, b,
              c->stream);
   ++c->launches;
@@ -772,7 +880,7 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   double2* dx = xdev ? static_cast<double2*>(x)
                      : static_cast<double2*>(ws(c, "out_x", sizeof(double2) * n, &rc));
   if (!dx) return rc;
-  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info))) return rc;
+  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info, mixed))) return rc;
   if (!xdev) {
     CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));

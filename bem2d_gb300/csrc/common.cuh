@@ -215,14 +215,49 @@ struct NodeTable {
   double* w;  // |J(x_q)| * w_q * phi_u(x_q)
 };
 
+// Far-field node data for the float-float kernel: node offsets from the
+// unknown's element centre, normals and weights as (hi, lo) float pairs,
+// the centre in FP64 and the largest offset (radius) per unknown.
+struct NodeTableFF {
+  float2* ox;
+  float2* oy;
+  float2* nx;
+  float2* ny;
+  float2* w;
+  double2* c;
+  float* rad;
+};
+
+// Fills the FP64 table and, when tf != nullptr, the float-float one.
 void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
-                       cudaStream_t s);
+                       const NodeTableFF* tf, cudaStream_t s);
+
+// Entries the float-float far kernel leaves to FP64 (an argument k|x-y| <= 8
+// somewhere on the element pair): (row, column) list with a counter.
+struct DeferList {
+  int2* ij;
+  unsigned* count;
+  unsigned capacity;
+};
+
+// Mixed far field: float-float evaluation, writes complex128 (out) and
+// complex64 (out32) copies; deferred entries go to `dl`.
+void launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+                   int kernel, double k, double eta, double alpha, double2* out,
+                   long long ld, float2* out32, long long ld32, DeferList dl,
+                   cudaStream_t s);
+// FP64 evaluation of the deferred entries (both outputs).
+void launch_deferred_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
+                          double k, double eta, double alpha, const DeferList& dl,
+                          unsigned n, double2* out, long long ld, float2* out32,
+                          long long ld32, cudaStream_t s);
 void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
                      double k, double eta, double alpha, double2* out,
                      long long ld, cudaStream_t s);
 void launch_near_fp64(const DevGeom& g, const DevRules& r, const NearPair* pairs,
                       int npairs, int kernel, double k, double eta, double alpha,
-                      double beta, double2* out, long long ld, cudaStream_t s);
+                      double beta, double2* out, long long ld, cudaStream_t s,
+                      float2* out32 = nullptr, long long ld32 = 0);
 void launch_ident(const DevGeom& g, const DevRules& r, const NearPair* pairs,
                   int npairs, double2* out, long long ld, cudaStream_t s);
 void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
@@ -234,21 +269,26 @@ struct LuWork {
   int* ipiv;             // [n] pivot rows (0-based): row i was swapped with ipiv[i]
   int* info;             // [1] first zero pivot (1-based) or 0
   int* status;           // [1] nonzero: a bounded device wait gave up
-  unsigned* barrier;     // [2] grid barrier counter / generation
-  void* scratch;         // panel exchange buffers
+  void* scratch;         // panel exchange slots (lu_scratch_bytes)
   size_t scratch_bytes;
+  int* perm;             // [n] row permutation of the pivots (filled by lu_factor)
+  void* dinv;            // inverses of the 64 x 64 diagonal blocks of L and U
 };
 
 // Bytes of LuWork::scratch the panel kernels need for n unknowns.
 size_t lu_scratch_bytes(int n);
+// Bytes of perm + dinv for n unknowns of `elem` bytes each.
+size_t lu_aux_bytes(int n, size_t elem);
 
 // LU with partial pivoting in place; T = double2 (complex128) or float2.
+// Also fills w.perm and w.dinv for lu_solve.
 template <typename T>
 int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
               long long* launches);
+// x = A^{-1} b with the factor of lu_factor (b and x may alias).
 template <typename T>
-void lu_solve(const T* LU, long long lda, int n, const int* ipiv, T* b,
-              cudaStream_t s, long long* launches);
+int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+             cudaStream_t s, long long* launches);
 
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);

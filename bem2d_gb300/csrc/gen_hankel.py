@@ -122,6 +122,52 @@ def emit_polys(prefix, polys, ctype):
     return "\n".join(lines) + "\n"
 
 
+def split_ff(v):
+    """Nearest float pair (hi, lo) with hi + lo ~ v to 2^-48."""
+    import numpy as np
+    hi = np.float32(float(v))
+    lo = np.float32(float(v - mp.mpf(float(hi))))
+    return float(hi), float(lo)
+
+
+def f32(v):
+    import numpy as np
+    return float(np.float32(float(v)))
+
+
+FF_INTERVALS = ((8, 16), (16, 64), (64, None))
+FF_TAIL_BOUND = 1.5e-8
+
+
+def emit_ff_polys(idx, polys):
+    """Compensated evaluation of monomial polynomials in t (|t| <= 1): the
+    tail sum_{k>=m} c_k t^(k-m), bounded by FF_TAIL_BOUND, in FP32 Horner on
+    t.hi; the head c_0 .. c_{m-1} in float-float Horner."""
+    out = []
+    for i, p in enumerate(polys):
+        tails = [sum(abs(v) for v in p[k:]) for k in range(len(p))] + [0]
+        m = next(k for k in range(len(p) + 1) if tails[k] < FF_TAIL_BOUND)
+        m = max(m, 1)
+        lines = ["__host__ __device__ __forceinline__ ff hkff_%d_%d(ff t) {" % (idx, i)]
+        if m < len(p):
+            expr = "%.9ef" % f32(p[-1])
+            for c in reversed(p[m:-1]):
+                expr = "fmaf(%s, t.hi, %.9ef)" % (expr, f32(c))
+            lines.append("  const float tail = %s;" % expr)
+            hi, lo = split_ff(p[m - 1])
+            lines.append("  ff y = ff_add_f(ff_make(%.9ef, %.9ef), t.hi * tail);" % (hi, lo))
+        else:
+            hi, lo = split_ff(p[m - 1])
+            lines.append("  ff y = ff_make(%.9ef, %.9ef);" % (hi, lo))
+        for c in reversed(p[:m - 1]):
+            hi, lo = split_ff(c)
+            lines.append("  y = ff_add_fast(ff_make(%.9ef, %.9ef), ff_mul(t, y));" % (hi, lo))
+        lines.append("  return y;")
+        lines.append("}")
+        out.append("\n".join(lines))
+    return "\n".join(out) + "\n"
+
+
 def main():
     out = ["// Generated by gen_hankel.py: polynomial pieces of the device Hankel",
            "// evaluator (see hankel.cuh).  Do not edit by hand.",
@@ -142,6 +188,20 @@ def main():
         out.append("constexpr int hk_terms_%s[3] = {%d, %d, %d};\n"
                    % (suffix, max(map(len, small)), max(map(len, mid)), max(map(len, far))))
     with open(os.path.join(HERE, "hankel_coeffs.h"), "w") as f:
+        f.write("\n".join(out) + "\n")
+    # float-float tables for x > 8 (three intervals)
+    out = ["// Generated by gen_hankel.py: float-float pieces of the Hankel evaluator",
+           "// for x > 8 (see hankel_ff.cuh).  Do not edit by hand.",
+           "#pragma once", '#include "ff.cuh"', "", "namespace bem2d_gpu {", ""]
+    for idx, (X, xhi) in enumerate(FF_INTERVALS):
+        funcs, slo = pq_funcs(X, mp.mpf(xhi) if xhi else None)
+        polys = [fit(f, 2e-18) for f in funcs]
+        out.append("// x in [%d, %s): P0, (x/%d) Q0, P1, (x/%d) Q1 in t = 2 (s - %s)/(1 - %s) - 1,"
+                   % (X, xhi if xhi else "inf", X, X, mp.nstr(slo, 6), mp.nstr(slo, 6)))
+        out.append("// s = (%d/x)^2" % X)
+        out.append(emit_ff_polys(idx, polys))
+    out.append("}  // namespace bem2d_gpu")
+    with open(os.path.join(HERE, "hankel_ff_coeffs.h"), "w") as f:
         f.write("\n".join(out) + "\n")
 
 

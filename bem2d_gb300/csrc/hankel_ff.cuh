@@ -1,0 +1,103 @@
+// Far-field kernel evaluation in float-float arithmetic (FP32 pipe) for
+// arguments x = k d > 8: H0 and H1 in modulus-phase form
+//   H_nu(x) = sqrt(2/(pi x)) (P_nu + i Q_nu) e^{i(x - (2 nu + 1) pi/4)}
+// with P, Q from hankel_ff_coeffs.h (three intervals of x), and e^{i(x-pi/4)}
+// from a Cody-Waite reduction modulo 2 pi/64 plus short Taylor polynomials
+// around a 64-entry table of e^{i(2 pi j/64 - pi/4)}.  Accuracy ~1e-14
+// relative to |H|; the same source builds on the host for accuracy tests.
+#pragma once
+
+#include "ff.cuh"
+#include "hankel_ff_coeffs.h"
+
+namespace bem2d_gpu {
+
+struct ffc {
+  ff re, im;
+};
+
+// 2 pi / 64 = C1 + C2 + C3 (C1, C2 single-precision, C3 the rest)
+constexpr float kRedC1 = 0.09817477315664291f;
+constexpr float kRedC2 = -2.7319617679211206e-09f;
+constexpr float kRedC3 = -1.0719528187536762e-16f;
+constexpr float kRedInv = 10.18591594696045f;  // 64 / (2 pi)
+
+// e^{i(x - pi/4)} for x > 0 (ff), table tab[j] = (cos, sin)(2 pi j/64 - pi/4)
+// as ff pairs: tab[4 j] = cos.hi, tab[4 j + 1] = cos.lo, [+2], [+3] = sin.
+__host__ __device__ __forceinline__ ffc expi_ff(ff x, const float* tab) {
+  const float j = rintf(x.hi * kRedInv);
+  const float r1 = fmaf(-j, kRedC1, x.hi);  // exact
+  ff r = two_sum(r1, x.lo);
+  r = ff_sub(r, two_prod(j, kRedC2));
+  r = ff_add_f(r, -j * kRedC3);
+  const int idx = ((int)j) & 63;
+  const ff r2 = ff_sqr(r);
+  // sin r = r - r^3 (1/6 - r^2/120 + r^4/5040)
+  const float st = r2.hi * fmaf(r2.hi, 1.0f / 5040.0f, -1.0f / 120.0f);
+  const ff S = ff_add_f(ff_make(0.1666666716337204f, -4.967053879312289e-09f), st);
+  const ff sinr = ff_add_fast(r, ff_neg(ff_mul(ff_mul(r, r2), S)));
+  // cos r = 1 - r^2 (1/2 - r^2/24 + r^4/720 - r^6/40320)
+  const float ct = r2.hi * r2.hi * fmaf(r2.hi, -1.0f / 40320.0f, 1.0f / 720.0f);
+  const ff C = ff_add_f(ff_add_fast(ff_make(0.5f, 0.0f),
+                                    ff_neg(ff_mul(r2, ff_make(0.0416666679084301f,
+                                                              -1.2417634698280722e-09f)))),
+                        ct);
+  const ff cosr = ff_add_fast(ff_make(1.0f, 0.0f), ff_neg(ff_mul(r2, C)));
+  const ff ca = ff_make(tab[4 * idx], tab[4 * idx + 1]);
+  const ff sa = ff_make(tab[4 * idx + 2], tab[4 * idx + 3]);
+  ffc e;
+  e.re = ff_add_fast(ff_mul(ca, cosr), ff_neg(ff_mul(sa, sinr)));
+  e.im = ff_add_fast(ff_mul(sa, cosr), ff_mul(ca, sinr));
+  return e;
+}
+
+// P0, Q0, P1, Q1 at x > 8 given ix = 1/x.
+__host__ __device__ __forceinline__ void pq_ff(float xhi, ff ix, ff* p0, ff* q0, ff* p1,
+                                               ff* q1) {
+  const ff ix2 = ff_sqr(ix);
+  if (xhi < 16.0f) {
+    const ff s = ff_scale2(ix2, 64.0f);  // (8/x)^2 in [1/4, 1]
+    // t = 2 (s - 1/4) / (3/4) - 1 = (8/3) s - 5/3
+    const ff tt = ff_add_fast(ff_mul(s, ff_make(2.6666667461395264f, -7.947286206899662e-08f)),
+                              ff_make(-1.6666666269302368f, -3.973643103449831e-08f));
+    const ff q = ff_scale2(ix, 8.0f);
+    *p0 = hkff_0_0(tt);
+    *q0 = ff_mul(hkff_0_1(tt), q);
+    *p1 = hkff_0_2(tt);
+    *q1 = ff_mul(hkff_0_3(tt), q);
+  } else if (xhi < 64.0f) {
+    const ff s = ff_scale2(ix2, 256.0f);  // (16/x)^2 in [1/16, 1]
+    // t = (32 s - 17) / 15
+    const ff t = ff_mul(ff_add_f(ff_scale2(s, 32.0f), -17.0f),
+                        ff_make(0.06666667014360428f, -3.47693762670076e-09f));
+    const ff q = ff_scale2(ix, 16.0f);
+    *p0 = hkff_1_0(t);
+    *q0 = ff_mul(hkff_1_1(t), q);
+    *p1 = hkff_1_2(t);
+    *q1 = ff_mul(hkff_1_3(t), q);
+  } else {
+    const ff s = ff_scale2(ix2, 4096.0f);  // (64/x)^2 in (0, 1]
+    const ff t = ff_add_f(ff_scale2(s, 2.0f), -1.0f);
+    const ff q = ff_scale2(ix, 64.0f);
+    *p0 = hkff_2_0(t);
+    *q0 = ff_mul(hkff_2_1(t), q);
+    *p1 = hkff_2_2(t);
+    *q1 = ff_mul(hkff_2_3(t), q);
+  }
+}
+
+// Host-side table of e^{i(2 pi j/64 - pi/4)} as ff pairs (4 floats per j).
+inline void expi_table(float* tab) {
+  for (int j = 0; j < 64; ++j) {
+    const long double a = 2.0L * 3.14159265358979323846264338327950288L * j / 64.0L -
+                          3.14159265358979323846264338327950288L / 4.0L;
+    const long double c = cosl(a), s = sinl(a);
+    const float ch = (float)c, sh = (float)s;
+    tab[4 * j] = ch;
+    tab[4 * j + 1] = (float)(c - (long double)ch);
+    tab[4 * j + 2] = sh;
+    tab[4 * j + 3] = (float)(s - (long double)sh);
+  }
+}
+
+}  // namespace bem2d_gpu

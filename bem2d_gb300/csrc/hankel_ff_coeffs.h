@@ -1,0 +1,101 @@
+// Generated by gen_hankel.py: float-float pieces of the Hankel evaluator
+// for x > 8 (see hankel_ff.cuh).  Do not edit by hand.
+#pragma once
+#include "ff.cuh"
+
+namespace bem2d_gpu {
+
+// x in [8, 16): P0, (x/8) Q0, P1, (x/8) Q1 in t = 2 (s - 0.25)/(1 - 0.25) - 1,
+// s = (8/x)^2
+__host__ __device__ __forceinline__ ff hkff_0_0(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(8.157953886e-15f, t.hi, -4.813773620e-14f), t.hi, 2.977758285e-13f), t.hi, -2.305387652e-12f), t.hi, 2.111152919e-11f), t.hi, -2.393353571e-10f), t.hi, 3.613838340e-09f);
+  ff y = ff_add_f(ff_make(-8.149908126e-08f, -2.827701545e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(3.368295438e-06f, 3.358971155e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-4.000022309e-04f, -1.114199271e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.993235469e-01f, 1.750196255e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_0_1(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-2.915657076e-16f, t.hi, 1.367555340e-15f), t.hi, -6.034843357e-15f), t.hi, 3.431652342e-14f), t.hi, -2.162804983e-13f), t.hi, 1.526000246e-12f), t.hi, -1.249619418e-11f), t.hi, 1.235907349e-10f), t.hi, -1.564620877e-09f);
+  ff y = ff_add_f(ff_make(2.774588914e-08f, 6.136798172e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(-8.020534210e-07f, 2.723028305e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(5.070442785e-05f, -2.454122517e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.553812250e-02f, 2.658160914e-10f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_0_2(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-8.766389510e-15f, t.hi, 5.199140746e-14f), t.hi, -3.239078385e-13f), t.hi, 2.527921015e-12f), t.hi, -2.339939527e-11f), t.hi, 2.693449908e-10f), t.hi, -4.162371336e-09f);
+  ff y = ff_add_f(ff_make(9.764687547e-08f, 6.559651842e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(-4.376802281e-06f, 1.253659042e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(6.711526657e-04f, -1.043188539e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.001131177e+00f, 5.686173665e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_0_3(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(3.101923591e-16f, t.hi, -1.459567576e-15f), t.hi, 6.471695094e-15f), t.hi, -3.696431453e-14f), t.hi, 2.342306579e-13f), t.hi, -1.664246865e-12f), t.hi, 1.375393202e-11f), t.hi, -1.377569725e-10f), t.hi, 1.776470859e-09f);
+  ff y = ff_add_f(ff_make(-3.244905145e-08f, -8.219780833e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(9.907389540e-07f, -4.501546540e-16f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-7.148936129e-05f, 1.151341609e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(4.675293341e-02f, -4.784950214e-10f), ff_mul(t, y));
+  return y;
+}
+
+// x in [16, 64): P0, (x/16) Q0, P1, (x/16) Q1 in t = 2 (s - 0.0625)/(1 - 0.0625) - 1,
+// s = (16/x)^2
+__host__ __device__ __forceinline__ ff hkff_1_0(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(2.836302529e-16f, t.hi, -3.952587769e-15f), t.hi, 6.944991186e-14f), t.hi, -1.657858204e-12f), t.hi, 5.730775923e-11f), t.hi, -3.231265921e-09f);
+  ff y = ff_add_f(ff_make(3.645652384e-07f, -3.611797191e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(-1.279068820e-04f, -3.521601847e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.998545647e-01f, 1.131000182e-09f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_1_1(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(1.226322721e-17f, t.hi, -1.268627450e-16f), t.hi, 1.549724916e-15f), t.hi, -2.415473352e-14f), t.hi, 4.898077386e-13f), t.hi, -1.379106551e-11f), t.hi, 5.932979108e-10f);
+  ff y = ff_add_f(ff_make(-4.545863774e-08f, -7.347227312e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(8.276492736e-06f, 4.070946393e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-7.803060580e-03f, -1.183232956e-10f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_1_2(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(-3.039536438e-16f, t.hi, 4.271659151e-15f), t.hi, -7.592448941e-14f), t.hi, 1.841640555e-12f), t.hi, -6.522651169e-11f), t.hi, 3.831822859e-09f);
+  ff y = ff_add_f(ff_make(-4.698935356e-07f, 8.975996284e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(2.134964743e-04f, -6.323998616e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.000242591e+00f, -1.899915603e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_1_3(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-1.301703855e-17f, t.hi, 1.354391918e-16f), t.hi, -1.667095942e-15f), t.hi, 2.623619671e-14f), t.hi, -5.391522732e-13f), t.hi, 1.547933656e-11f), t.hi, -6.869294578e-10f);
+  ff y = ff_add_f(ff_make(5.570204564e-08f, 1.382253082e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(-1.160566444e-05f, -1.586087219e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.342427522e-02f, -8.787405803e-10f), ff_mul(t, y));
+  return y;
+}
+
+// x in [64, inf): P0, (x/64) Q0, P1, (x/64) Q1 in t = 2 (s - 0.0)/(1 - 0.0) - 1,
+// s = (64/x)^2
+__host__ __device__ __forceinline__ ff hkff_2_0(ff t) {
+  const float tail = fmaf(fmaf(1.333961907e-15f, t.hi, -1.036012422e-12f), t.hi, 1.668080452e-09f);
+  ff y = ff_add_f(ff_make(-8.579729183e-06f, -3.902570541e-13f), t.hi * tail);
+  y = ff_add_fast(ff_make(9.999914169e-01f, 1.670156458e-09f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_2_1(ff t) {
+  const float tail = fmaf(fmaf(fmaf(2.279533475e-19f, t.hi, -8.343479671e-17f), t.hi, 4.876893838e-14f), t.hi, -5.273089257e-11f);
+  ff y = ff_add_f(ff_make(1.395927711e-07f, 6.645530819e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(-1.952985302e-03f, -5.282868240e-11f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_2_2(ff t) {
+  const float tail = fmaf(fmaf(-1.512234391e-15f, t.hi, 1.224637362e-12f), t.hi, -2.144998179e-09f);
+  ff y = ff_add_f(ff_make(1.430082102e-05f, 4.806670063e-14f), t.hi * tail);
+  y = ff_add_fast(ff_make(1.000014305e+00f, -2.147451994e-09f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_2_3(ff t) {
+  const float tail = fmaf(fmaf(fmaf(-2.497464547e-19f, t.hi, 9.327624092e-17f), t.hi, -5.628396376e-14f), t.hi, 6.445888961e-11f);
+  ff y = ff_add_f(ff_make(-1.954486493e-07f, -4.400672010e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(5.859179422e-03f, 6.457173685e-11f), ff_mul(t, y));
+  return y;
+}
+
+}  // namespace bem2d_gpu

@@ -2,19 +2,25 @@
 // for complex128 (double2) and complex64 (float2).  Replaces LAPACK zgetrf +
 // zgetrs as called by SolveSystem (lib/bem2d_mathroutines.cpp:323-351).
 //
-// Per panel of NB columns:
-//   panel_kernel   cooperative launch, one CTA per SM; each CTA keeps its
-//                  slice of the panel rows in shared memory.  One bounded grid
-//                  barrier per column: every CTA publishes its local pivot
-//                  candidate (value, row, whole panel row); after the barrier
-//                  all CTAs agree on the pivot, swap locally and update.
-//   laswp_kernel   applies the panel's row swaps to the trailing columns
+// Per panel of NB = 64 columns:
+//   panel_cluster_kernel  one thread-block cluster (up to 16 CTAs) holds the
+//                  panel rows in distributed shared memory; per column each CTA
+//                  writes its pivot candidate (value, row, panel row) to its own
+//                  shared memory, one cluster barrier, then every CTA reads the
+//                  candidates over DSMEM, agrees on the pivot, swaps and
+//                  updates.  Used while the panel fits in the cluster's smem.
+//   panel_kernel   the same exchange through global-memory slots with
+//                  sequence flags (bounded waits) across a cooperative grid,
+//                  for taller panels.
+//   laswp_kernel   the panel's row swaps on all other columns (LAPACK order)
 //   trsm_kernel    U12 = L11^{-1} A12
 //   gemm_kernel    A22 -= L21 U12  (register-tiled, 64 x 64 CTA tiles)
-// The swaps are not applied to the columns left of the panel; the forward
-// solve applies each panel's swaps to the right-hand side just before that
-// panel's columns of L (identical to LAPACK's P, L, U up to row storage).
+// After the factorisation: perm (the row permutation of the pivots) and the
+// inverses of the 64 x 64 diagonal blocks of L and U, so that a solve is a
+// chain of small matrix-vector products (trisolve_cluster_kernel).
 #include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
 
 #include <algorithm>
 #include <climits>
@@ -26,44 +32,7 @@ namespace bem2d_gpu {
 
 constexpr int kNB = 64;              // panel width
 constexpr int kPanelThreads = 256;
-constexpr unsigned kSpinLimit = 1u << 25;  // polls of 64 ns: ~2 s
-
-// Bounded grid-wide barrier for a cooperative launch.  A block that waits
-// longer than the limit records status = 1 and returns false; every later
-// call returns false at once, so the kernel winds down without hanging.
-__device__ bool grid_sync(unsigned* bar, unsigned nblocks, int* status) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    if (*(volatile int*)status != 0) {
-      ok = 0;
-    } else {
-      volatile unsigned* vgen = bar + 1;
-      const unsigned gen = *vgen;
-      __threadfence();
-      const unsigned arrived = atomicAdd(bar, 1u);
-      if (arrived == nblocks - 1) {
-        atomicExch(bar, 0u);
-        __threadfence();
-        atomicAdd(bar + 1, 1u);
-      } else {
-        unsigned it = 0;
-        while (*vgen == gen) {
-          if (++it > kSpinLimit) {
-            atomicExch(status, 1);
-            ok = 0;
-            break;
-          }
-          __nanosleep(64);
-        }
-      }
-      __threadfence();
-    }
-  }
-  __syncthreads();
-  return ok != 0;
-}
+constexpr unsigned kSpinLimit = 1u << 25;  // polls of >= 32 ns: > 1 s
 
 // (value, row) arg-max with ties to the smaller row, as LAPACK's izamax
 // (first maximal |re| + |im|).
@@ -97,49 +66,73 @@ __device__ void block_argmax(R& v, int& i) {
   for (int k = 1; k < (int)(blockDim.x >> 5); ++k) argmax_merge(v, i, sv[k], si[k]);
 }
 
-// Panel exchange buffers, per parity: candidate value / row / panel row of
-// each block, and the current row kc.
+// Panel exchange slots in global memory, two per block (column parity):
+// {seq, row index, |pivot| value, the block's candidate panel row}, plus a
+// slot for the current row kc from its owner.  A slot is valid for column kc
+// when its seq equals kc + 1; the slots are zeroed before each factorisation.
+constexpr int kMaxPanelBlocks = 1024;
+constexpr int kSlotHead = 16;  // int seq, int idx, 8-byte value
+
 template <typename T>
-struct PanelBufs {
-  typename CTraits<T>::R* val;  // [2][maxb]
-  int* idx;                     // [2][maxb]
-  T* cand;                      // [2][maxb][kNB]
-  T* krow;                      // [2][kNB]
+struct PanelSlots {
+  char* base;
+  __device__ __forceinline__ char* slot(int par, int b) const {
+    return base + ((size_t)par * (kMaxPanelBlocks + 1) + b) * (kSlotHead + sizeof(T) * kNB);
+  }
+  __device__ __forceinline__ char* krow(int par) const { return slot(par, kMaxPanelBlocks); }
 };
 
-constexpr int kMaxPanelBlocks = 1024;
-
-template <typename T>
-static PanelBufs<T> panel_bufs(void* scratch) {
-  typedef typename CTraits<T>::R R;
-  PanelBufs<T> b;
-  char* p = static_cast<char*>(scratch);
-  b.cand = reinterpret_cast<T*>(p);
-  p += sizeof(T) * 2 * kMaxPanelBlocks * kNB;
-  b.krow = reinterpret_cast<T*>(p);
-  p += sizeof(T) * 2 * kNB;
-  b.val = reinterpret_cast<R*>(p);
-  p += sizeof(R) * 2 * kMaxPanelBlocks;
-  b.idx = reinterpret_cast<int*>(p);
-  return b;
+size_t lu_scratch_bytes(int) {
+  return (size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + sizeof(double2) * kNB) + 256;
 }
 
-size_t lu_scratch_bytes(int) {
-  return sizeof(double2) * 2 * kMaxPanelBlocks * kNB + sizeof(double2) * 2 * kNB +
-         sizeof(double) * 2 * kMaxPanelBlocks + sizeof(int) * 2 * kMaxPanelBlocks + 256;
+static size_t slots_bytes(size_t elem) {
+  return (size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + elem * kNB);
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait (bounded) until *seq == want (acquire); returns false on timeout.
+// Spins without sleeping first: the expected wait is one L2 round trip.
+__device__ __forceinline__ bool wait_seq(const int* seq, int want, int* status) {
+  unsigned it = 0;
+  while (ld_acquire(seq) != want) {
+    if (++it > kSpinLimit || (it > 1024 && *(volatile int*)status != 0)) {
+      atomicExch(status, 1);
+      return false;
+    }
+    if (it > 256) __nanosleep(32);
+  }
+  return true;
+}
+
+// Publish `epoch` at *flag after every thread of the block has written its
+// data: bar.sync orders the block's writes before thread 0's release store.
+__device__ __forceinline__ void block_publish(int* flag, int epoch) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(flag, epoch);
+  }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads)
 panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
-             int* __restrict__ ipiv, int* info, int* status, unsigned* bar,
-             PanelBufs<T> buf) {
+             int* __restrict__ ipiv, int* info, int* status, PanelSlots<T> sl) {
   typedef typename CTraits<T>::R R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* P = reinterpret_cast<T*>(smem_raw);  // [rpb][kNB] block's panel rows
   T* prow = P + (size_t)rpb * kNB;        // [kNB] pivot row
   T* lcol = prow + kNB;                   // [rpb] multipliers
-  __shared__ int s_p, s_bw;
+  __shared__ int s_p, s_bw, s_ok;
   __shared__ R s_pv;
 
   const int nblk = gridDim.x, b = blockIdx.x;
@@ -150,10 +143,11 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
     const int c = v / nr, lr = v - c * nr;
     P[lr * kNB + c] = A[(size_t)(k0 + c) * lda + r0 + lr];
   }
+  if (threadIdx.x == 0) s_ok = 1;
   __syncthreads();
 
   for (int c = 0; c < nb; ++c) {
-    const int kc = k0 + c, par = c & 1;
+    const int kc = k0 + c, par = kc & 1, epoch = kc + 1;
     // (a) local pivot candidate among rows >= kc
     R best = -1;
     int bidx = INT_MAX;
@@ -163,59 +157,70 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
       argmax_merge(best, bidx, cabs1(P[lr * kNB + c]), gr);
     }
     block_argmax(best, bidx);
-    // (b) publish candidate and, from the owner, row kc
-    if (threadIdx.x == 0) {
-      buf.val[par * kMaxPanelBlocks + b] = best;
-      buf.idx[par * kMaxPanelBlocks + b] = bidx;
-    }
+    // (b) publish the candidate (and row kc from its owner), then the seq
+    char* my = sl.slot(par, b);
+    T* myrow = reinterpret_cast<T*>(my + kSlotHead);
     if (bidx != INT_MAX)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) myrow[j] = P[(bidx - r0) * kNB + j];
+    const bool own_k = kc >= r0 && kc < r1;
+    char* kr = sl.krow(par);
+    if (own_k)
       for (int j = threadIdx.x; j < nb; j += blockDim.x)
-        buf.cand[((size_t)par * kMaxPanelBlocks + b) * kNB + j] = P[(bidx - r0) * kNB + j];
-    if (kc >= r0 && kc < r1)
-      for (int j = threadIdx.x; j < nb; j += blockDim.x)
-        buf.krow[par * kNB + j] = P[(kc - r0) * kNB + j];
-    __threadfence();
-    if (!grid_sync(bar, nblk, status)) return;
-    // (c) agree on the pivot
-    {
-      R v = -1;
-      int i = INT_MAX, w = 0;
-      for (int q = threadIdx.x; q < nblk; q += blockDim.x) {
-        const R v2 = __ldcg(&buf.val[par * kMaxPanelBlocks + q]);
-        const int i2 = __ldcg(&buf.idx[par * kMaxPanelBlocks + q]);
-        argmax_merge(v, i, v2, i2);
+        reinterpret_cast<T*>(kr + kSlotHead)[j] = P[(kc - r0) * kNB + j];
+    if (threadIdx.x == 0) {
+      reinterpret_cast<int*>(my)[1] = bidx;
+      *reinterpret_cast<R*>(my + 8) = best;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release(reinterpret_cast<int*>(my), epoch);
+      if (own_k) st_release(reinterpret_cast<int*>(kr), epoch);
+    }
+    // (c) wait for every block's candidate, agree on the pivot
+    R v = -1;
+    int i = INT_MAX;
+    if ((int)threadIdx.x < nblk) {
+      const char* q = sl.slot(par, threadIdx.x);
+      if (!wait_seq(reinterpret_cast<const int*>(q), epoch, status)) {
+        s_ok = 0;
+      } else {
+        i = __ldcg(reinterpret_cast<const int*>(q) + 1);
+        v = __ldcg(reinterpret_cast<const R*>(q + 8));
       }
-      block_argmax(v, i);
-      if (threadIdx.x == 0) {
-        // no finite candidate (all NaN): treat as a zero pivot at row kc
-        if (i == INT_MAX || i < kc || i >= n) {
-          i = kc;
-          v = 0;
-        }
-        // the owner block of row i published it
-        w = (i - k0) / rpb;
-        s_p = i;
-        s_bw = w;
-        s_pv = v;
+    }
+    block_argmax(v, i);  // contains __syncthreads: s_ok visible after it
+    if (!s_ok) return;
+    if (threadIdx.x == 0) {
+      // no finite candidate (all NaN): treat as a zero pivot at row kc
+      if (i == INT_MAX || i < kc || i >= n) {
+        i = kc;
+        v = 0;
       }
+      s_p = i;
+      s_bw = (i - k0) / rpb;  // the owner block of row i published it
+      s_pv = v;
     }
     __syncthreads();
     const int p = s_p, bw = s_bw;
     const bool zero = !(s_pv > 0);
-    for (int j = threadIdx.x; j < nb; j += blockDim.x)
-      prow[j] = __ldcg(&buf.cand[((size_t)par * kMaxPanelBlocks + bw) * kNB + j]);
+    const T* wrow = reinterpret_cast<const T*>(sl.slot(par, bw) + kSlotHead);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) prow[j] = __ldcg(&wrow[j]);
     if (b == 0 && threadIdx.x == 0) {
       ipiv[kc] = p;
       if (zero && *info == 0) *info = kc + 1;
     }
-    __syncthreads();
-    if (!zero && p != kc) {
-      if (p >= r0 && p < r1)
-        for (int j = threadIdx.x; j < nb; j += blockDim.x)
-          P[(p - r0) * kNB + j] = __ldcg(&buf.krow[par * kNB + j]);
-      if (kc >= r0 && kc < r1)
-        for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(kc - r0) * kNB + j] = prow[j];
+    if (!zero && p != kc && p >= r0 && p < r1) {
+      if (threadIdx.x == 0 && !wait_seq(reinterpret_cast<const int*>(kr), epoch, status))
+        s_ok = 0;
+      __syncthreads();
+      if (!s_ok) return;
+      for (int j = threadIdx.x; j < nb; j += blockDim.x)
+        P[(p - r0) * kNB + j] = __ldcg(reinterpret_cast<const T*>(kr + kSlotHead) + j);
     }
+    __syncthreads();
+    if (!zero && p != kc && own_k)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(kc - r0) * kNB + j] = prow[j];
     __syncthreads();
     // (d) multipliers and rank-1 update of the block's rows below kc
     if (!zero) {
@@ -230,25 +235,27 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
       __syncthreads();
       const int w = nb - c - 1;
       if (w > 0) {
-        for (int v = threadIdx.x; v < nr * w; v += blockDim.x) {
-          const int lr = v / w, cc = c + 1 + (v - lr * w);
+        for (int u = threadIdx.x; u < nr * w; u += blockDim.x) {
+          const int lr = u / w, cc = c + 1 + (u - lr * w);
           if (r0 + lr > kc) P[lr * kNB + cc] = cfms(P[lr * kNB + cc], lcol[lr], prow[cc]);
         }
       }
     }
     __syncthreads();
   }
-  for (int v = threadIdx.x; v < nr * nb; v += blockDim.x) {
-    const int c = v / nr, lr = v - c * nr;
+  for (int v2 = threadIdx.x; v2 < nr * nb; v2 += blockDim.x) {
+    const int c = v2 / nr, lr = v2 - c * nr;
     A[(size_t)(k0 + c) * lda + r0 + lr] = P[lr * kNB + c];
   }
 }
 
+// Row swaps of panel [k0, k0+nb) on every column outside it.
 template <typename T>
-__global__ void laswp_kernel(T* __restrict__ A, long long lda, int c0, int ncols,
+__global__ void laswp_kernel(T* __restrict__ A, long long lda, int n,
                              const int* __restrict__ ipiv, int k0, int nb) {
-  const int j = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= c0 + ncols) return;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= n - nb) return;
+  const int j = v < k0 ? v : v + nb;
   T* col = A + (size_t)j * lda;
   for (int s = 0; s < nb; ++s) {
     const int p = ipiv[k0 + s];
@@ -358,165 +365,419 @@ static int panel_blocks(int H) {
   return std::max(1, std::min(nsm, (H + 63) / 64));
 }
 
+// ---- cluster panel ---------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+panel_cluster_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
+                     int* __restrict__ ipiv, int* info) {
+  typedef typename CTraits<T>::R R;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* P = reinterpret_cast<T*>(smem_raw);  // [rpb][kNB]
+  T* prow = P + (size_t)rpb * kNB;        // [kNB]
+  T* lcol = prow + kNB;                   // [rpb]
+  T* crow = lcol + rpb;                   // [2][kNB] candidate row per parity
+  T* krow = crow + 2 * kNB;               // [2][kNB] row kc per parity (owner)
+  __shared__ R cval[2];
+  __shared__ int cidx[2];
+  __shared__ int s_p, s_bw;
+  __shared__ R s_pv;
+  const int r0 = k0 + rank * rpb;
+  const int r1 = min(r0 + rpb, n);
+  const int nr = max(r1 - r0, 0);
+  for (int v = threadIdx.x; v < nr * nb; v += blockDim.x) {
+    const int c = v / nr, lr = v - c * nr;
+    P[lr * kNB + c] = A[(size_t)(k0 + c) * lda + r0 + lr];
+  }
+  cl.sync();  // every CTA of the cluster is running before any DSMEM access
+  for (int c = 0; c < nb; ++c) {
+    const int kc = k0 + c, par = c & 1;
+    R best = -1;
+    int bidx = INT_MAX;
+    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+      const int gr = r0 + lr;
+      if (gr < kc) continue;
+      argmax_merge(best, bidx, cabs1(P[lr * kNB + c]), gr);
+    }
+    block_argmax(best, bidx);
+    if (threadIdx.x == 0) {
+      cval[par] = best;
+      cidx[par] = bidx;
+    }
+    if (bidx != INT_MAX)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) crow[par * kNB + j] = P[(bidx - r0) * kNB + j];
+    const bool own_k = kc >= r0 && kc < r1;
+    if (own_k)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) krow[par * kNB + j] = P[(kc - r0) * kNB + j];
+    cl.sync();
+    if (threadIdx.x < 32) {
+      R v = -1;
+      int i = INT_MAX;
+      for (int q = threadIdx.x; q < C; q += 32) {
+        argmax_merge(v, i, *cl.map_shared_rank(&cval[par], q), *cl.map_shared_rank(&cidx[par], q));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const R v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        argmax_merge(v, i, v2, i2);
+      }
+      if (threadIdx.x == 0) {
+        if (i == INT_MAX || i < kc || i >= n) {
+          i = kc;
+          v = 0;
+        }
+        s_p = i;
+        s_bw = (i - k0) / rpb;
+        s_pv = v;
+      }
+    }
+    __syncthreads();
+    const int p = s_p, bw = s_bw;
+    const bool zero = !(s_pv > 0);
+    const T* wrow = cl.map_shared_rank(crow, bw) + par * kNB;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) prow[j] = wrow[j];
+    if (rank == 0 && threadIdx.x == 0) {
+      ipiv[kc] = p;
+      if (zero && *info == 0) *info = kc + 1;
+    }
+    if (!zero && p != kc && p >= r0 && p < r1) {
+      const T* kr = cl.map_shared_rank(krow, (kc - k0) / rpb) + par * kNB;
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(p - r0) * kNB + j] = kr[j];
+    }
+    __syncthreads();
+    if (!zero && p != kc && own_k)
+      for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(kc - r0) * kNB + j] = prow[j];
+    __syncthreads();
+    if (!zero) {
+      const T inv = crcp(prow[c]);
+      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
+        if (r0 + lr > kc) {
+          const T l = cmul(P[lr * kNB + c], inv);
+          P[lr * kNB + c] = l;
+          lcol[lr] = l;
+        }
+      }
+      __syncthreads();
+      const int w = nb - c - 1;
+      if (w > 0) {
+        for (int u = threadIdx.x; u < nr * w; u += blockDim.x) {
+          const int lr = u / w, cc = c + 1 + (u - lr * w);
+          if (r0 + lr > kc) P[lr * kNB + cc] = cfms(P[lr * kNB + cc], lcol[lr], prow[cc]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+  for (int v = threadIdx.x; v < nr * nb; v += blockDim.x) {
+    const int c = v / nr, lr = v - c * nr;
+    A[(size_t)(k0 + c) * lda + r0 + lr] = P[lr * kNB + c];
+  }
+}
+
+template <typename K, typename... Args>
+static cudaError_t launch_cluster(K kern, int C, int threads, size_t smem, cudaStream_t s,
+                                  Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+constexpr int kMaxCluster = 16;
+constexpr size_t kClusterSmem = 200 * 1024;
+
+template <typename T>
+static size_t panel_cluster_smem(int rpb) {
+  return sizeof(T) * ((size_t)rpb * kNB + kNB + rpb + 4 * kNB);
+}
+
+// Row permutation of the pivots: perm[i] = the original row that ends at i.
+__global__ void perm_kernel(int n, const int* __restrict__ ipiv, int* __restrict__ perm) {
+  extern __shared__ int sp[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sp[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) {
+      const int p = ipiv[i];
+      const int t = sp[i];
+      sp[i] = sp[p];
+      sp[p] = t;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = sp[i];
+}
+
+// Inverses of the diagonal blocks: dinv[(2 k) * 64 * 64 ...] = L_kk^{-1}
+// (unit lower), dinv[(2 k + 1) * 64 * 64 ...] = U_kk^{-1}; column-major 64 x 64.
+template <typename T>
+__global__ void __launch_bounds__(128) dinv_kernel(const T* __restrict__ LU, long long lda, int n,
+                                                   T* __restrict__ dinv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB] column-major
+  const int k0 = blockIdx.x * kNB, nb = min(kNB, n - k0);
+  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
+    const int c = v / nb, r = v - c * nb;
+    D[c * kNB + r] = LU[(size_t)(k0 + c) * lda + k0 + r];
+  }
+  __syncthreads();
+  T* Li = dinv + (size_t)(2 * blockIdx.x) * kNB * kNB;
+  T* Ui = Li + kNB * kNB;
+  const T zero = CTraits<T>::make(0, 0), one = CTraits<T>::make(1, 0);
+  const int j = threadIdx.x & 63;
+  // thread j builds column j of one inverse in place in global memory (its
+  // own column only, so the reads back hit L1)
+  if (threadIdx.x < 64) {
+    // L^{-1}: x_j = 1, x_i = -sum_{m=j}^{i-1} L_im x_m
+    T* x = Li + j * kNB;
+    for (int i = 0; i < kNB; ++i) x[i] = (i == j && j < nb) ? one : zero;
+    if (j < nb) {
+      for (int i = j + 1; i < nb; ++i) {
+        T acc = zero;
+        for (int m = j; m < i; ++m) acc = cfma(D[m * kNB + i], x[m], acc);
+        x[i] = CTraits<T>::make(-acc.x, -acc.y);
+      }
+    }
+  } else {
+    // U^{-1}: x_j = 1/U_jj, x_i = -(sum_{m=i+1}^{j} U_im x_m) / U_ii
+    T* x = Ui + j * kNB;
+    for (int i = 0; i < kNB; ++i) x[i] = zero;
+    if (j < nb) {
+      x[j] = crcp(D[j * kNB + j]);
+      for (int i = j - 1; i >= 0; --i) {
+        T acc = zero;
+        for (int m = i + 1; m <= j; ++m) acc = cfma(D[m * kNB + i], x[m], acc);
+        const T q = cmul(acc, crcp(D[i * kNB + i]));
+        x[i] = CTraits<T>::make(-q.x, -q.y);
+      }
+    }
+  }
+}
+
+size_t lu_aux_bytes(int n, size_t elem) {
+  const size_t nk = (n + kNB - 1) / kNB;
+  return sizeof(int) * (size_t)n + 2 * nk * kNB * kNB * elem + 256;
+}
+
 template <typename T>
 int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
               long long* launches) {
-  const PanelBufs<T> buf = panel_bufs<T>(w.scratch);
+  PanelSlots<T> sl;
+  sl.base = static_cast<char*>(w.scratch);
   cudaMemsetAsync(w.info, 0, sizeof(int), s);
   cudaMemsetAsync(w.status, 0, sizeof(int), s);
-  cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), s);
+  cudaMemsetAsync(sl.base, 0, slots_bytes(sizeof(T)), s);
   static bool attr = false;
+  static bool cluster16 = true;
   if (!attr) {
     cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kClusterSmem);
+    if (cudaFuncSetAttribute(panel_cluster_kernel<T>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      cluster16 = false;
+    }
     cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(T) * (kNB * kNB + kNB * 32)));
     cudaFuncSetAttribute(gemm_sub_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(T) * 2 * kNB * kGB));
+    cudaFuncSetAttribute(dinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(T) * kNB * kNB));
+    cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = std::min(kNB, n - k0);
     const int H = n - k0;
-    int nblk = panel_blocks<T>(H);
-    int rpb = (H + nblk - 1) / nblk;
-    nblk = (H + rpb - 1) / rpb;
-    const size_t smem = sizeof(T) * ((size_t)rpb * kNB + kNB + rpb);
-    if (smem > 200 * 1024) return BEM2D_ERR_ARG;
-    void* args[] = {(void*)&A, (void*)&lda, (void*)&n, (void*)&k0, (void*)&nb, (void*)&rpb,
-                    (void*)&w.ipiv, (void*)&w.info, (void*)&w.status, (void*)&w.barrier,
-                    (void*)&buf};
-    cudaError_t e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(nblk),
-                                                dim3(kPanelThreads), args, smem, s);
-    if (e != cudaSuccess) return BEM2D_ERR_CUDA;
+    // cluster panel: 64 rows or more per CTA, at most 16 (8 portable) CTAs
+    bool done = false;
+    for (int cmax : {cluster16 ? kMaxCluster : 8, 8}) {
+      const int C = std::max(1, std::min(cmax, (H + 63) / 64));
+      const int rpb = (H + C - 1) / C;
+      const size_t smem = panel_cluster_smem<T>(rpb);
+      if (smem > kClusterSmem) continue;
+      cudaError_t e = launch_cluster(panel_cluster_kernel<T>, C, kPanelThreads, smem, s, A, lda,
+                                     n, k0, nb, rpb, w.ipiv, w.info);
+      if (e == cudaSuccess) {
+        done = true;
+        break;
+      }
+      cudaGetLastError();
+      if (cmax > 8) cluster16 = false;
+    }
+    if (!done) {
+      int nblk = panel_blocks<T>(H);
+      int rpb = (H + nblk - 1) / nblk;
+      nblk = (H + rpb - 1) / rpb;
+      const size_t smem = sizeof(T) * ((size_t)rpb * kNB + kNB + rpb);
+      if (smem > 200 * 1024) return BEM2D_ERR_ARG;
+      void* args[] = {(void*)&A, (void*)&lda, (void*)&n, (void*)&k0, (void*)&nb, (void*)&rpb,
+                      (void*)&w.ipiv, (void*)&w.info, (void*)&w.status, (void*)&sl};
+      cudaError_t e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(nblk),
+                                                  dim3(kPanelThreads), args, smem, s);
+      if (e != cudaSuccess) return BEM2D_ERR_CUDA;
+    }
     ++*launches;
+    if (n > nb) {
+      laswp_kernel<T><<<(n - nb + 127) / 128, 128, 0, s>>>(A, lda, n, w.ipiv, k0, nb);
+      ++*launches;
+    }
     const int c0 = k0 + nb, nc = n - c0;
     if (nc > 0) {
-      laswp_kernel<T><<<(nc + 127) / 128, 128, 0, s>>>(A, lda, c0, nc, w.ipiv, k0, nb);
       trsm_kernel<T><<<(nc + 31) / 32, 256, sizeof(T) * (kNB * kNB + kNB * 32), s>>>(
           A, lda, k0, nb, c0, nc);
       dim3 g((nc + kGB - 1) / kGB, (nc + kGB - 1) / kGB);
       gemm_sub_kernel<T><<<g, 256, sizeof(T) * 2 * kNB * kGB, s>>>(
           A + (size_t)k0 * lda + c0, lda, A + (size_t)c0 * lda + k0, lda,
           A + (size_t)c0 * lda + c0, lda, nc, nc, nb);
-      *launches += 3;
+      *launches += 2;
     }
   }
+  // solve aids: permutation and diagonal-block inverses
+  const int nk = (n + kNB - 1) / kNB;
+  perm_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, w.ipiv, w.perm);
+  dinv_kernel<T><<<nk, 128, sizeof(T) * kNB * kNB, s>>>(A, lda, n, reinterpret_cast<T*>(w.dinv));
+  *launches += 2;
   return BEM2D_OK;
 }
 
 // ---- triangular solves ----------------------------------------------------
-// Forward step of panel k0: swaps of the panel applied to b, then
-// y = L11^{-1} b[k0:k0+nb].  The nb x nb diagonal block is staged in shared
-// memory first (coalesced), so the sequential sweep reads only smem.
+// x = U^{-1} L^{-1} P b in one cluster launch.  CTA r owns rows
+// [r rpb, (r+1) rpb) of b in shared memory (rpb a multiple of 64).  Step k of
+// the forward sweep: the owner of block k forms y_k = L_kk^{-1} b_k from the
+// stored inverse; one cluster barrier; every CTA reads y_k over DSMEM and
+// updates its rows below the block.  The backward sweep is the mirror with
+// U_kk^{-1}.  One cluster barrier per block step.
 template <typename T>
-__global__ void fwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0, int nb,
-                                const int* __restrict__ ipiv, T* b) {
+__global__ void __launch_bounds__(256)
+trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
+                        const int* __restrict__ perm, const T* __restrict__ dinv,
+                        const T* __restrict__ bin, T* __restrict__ xout, int rpb) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* D = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB]
-  T* y = D + kNB * kNB;                   // [kNB]
-  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
-    const int s = v / nb, r = v - s * nb;
-    D[s * kNB + r] = LU[(size_t)(k0 + s) * lda + k0 + r];
-  }
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < nb; ++s) {
-      const int p = ipiv[k0 + s];
-      if (p != k0 + s) {
-        const T t = b[k0 + s];
-        b[k0 + s] = b[p];
-        b[p] = t;
+  T* bc = reinterpret_cast<T*>(smem_raw);  // [rpb] this CTA's rows of b
+  T* ys = bc + rpb;                         // [kNB] the current block solution
+  T* ps = ys + kNB;                         // [4][max(rpb, kNB)] partial sums
+  const int r0 = rank * rpb, r1 = min(n, r0 + rpb), nr = max(r1 - r0, 0);
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) bc[i] = bin[perm[r0 + i]];
+  const int nk = (n + kNB - 1) / kNB;
+  cl.sync();
+  for (int step = 0; step < 2 * nk; ++step) {
+    const bool fwd = step < nk;
+    const int kb = fwd ? step : 2 * nk - 1 - step;
+    const int k0 = kb * kNB, nb = min(kNB, n - k0);
+    const int owner = k0 / rpb;
+    if (rank == owner) {
+      // y = D_k^{-1} b_k: four column groups of 16 per row, partial sums in ps
+      const T* Di = dinv + (size_t)(2 * kb + (fwd ? 0 : 1)) * kNB * kNB;
+      const T* bk = bc + (k0 - r0);
+      const int r = threadIdx.x & 63, g = threadIdx.x >> 6;
+      T acc = CTraits<T>::make(0, 0);
+      if (r < nb) {
+        T l[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) l[u] = Di[(g * 16 + u) * kNB + r];
+#pragma unroll
+        for (int u = 0; u < 16; ++u)
+          if (g * 16 + u < nb) acc = cfma(l[u], bk[g * 16 + u], acc);
+      }
+      ps[g * kNB + r] = acc;
+      __syncthreads();
+      if ((int)threadIdx.x < nb) {
+        const int t = threadIdx.x;
+        T v = ps[t];
+        v.x += ps[kNB + t].x + ps[2 * kNB + t].x + ps[3 * kNB + t].x;
+        v.y += ps[kNB + t].y + ps[2 * kNB + t].y + ps[3 * kNB + t].y;
+        bc[k0 - r0 + t] = v;
       }
     }
-  }
-  __syncthreads();
-  if (threadIdx.x < nb) y[threadIdx.x] = b[k0 + threadIdx.x];
-  for (int s = 0; s < nb; ++s) {
+    cl.sync();
+    const T* yk = cl.map_shared_rank(bc, owner) + (k0 - owner * rpb);
+    if ((int)threadIdx.x < nb) ys[threadIdx.x] = yk[threadIdx.x];
     __syncthreads();
-    const T ys = y[s];
-    const int r = threadIdx.x;
-    if (r > s && r < nb) y[r] = cfms(y[r], D[s * kNB + r], ys);
-  }
-  __syncthreads();
-  if (threadIdx.x < nb) b[k0 + threadIdx.x] = y[threadIdx.x];
-}
-
-// b[r] -= sum_s LU[r, c0+s] * b[c0+s] for rows r in [r0, r1), s < nb.
-template <typename T>
-__global__ void gemv_sub_kernel(const T* __restrict__ LU, long long lda, int c0, int nb,
-                                int r0, int r1, T* b) {
-  __shared__ T y[kNB];
-  if (threadIdx.x < nb) y[threadIdx.x] = b[c0 + threadIdx.x];
-  __syncthreads();
-  const int r = r0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= r1) return;
-  T acc = b[r];
-  for (int s = 0; s < nb; ++s) acc = cfms(acc, LU[(size_t)(c0 + s) * lda + r], y[s]);
-  b[r] = acc;
-}
-
-template <typename T>
-__global__ void bwd_diag_kernel(const T* __restrict__ LU, long long lda, int k0, int nb, T* b) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* D = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB]
-  T* rd = D + kNB * kNB;                  // [kNB]
-  T* y = rd + kNB;                        // [kNB]
-  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
-    const int s = v / nb, r = v - s * nb;
-    D[s * kNB + r] = LU[(size_t)(k0 + s) * lda + k0 + r];
-  }
-  __syncthreads();
-  if (threadIdx.x < nb) {
-    rd[threadIdx.x] = crcp(D[threadIdx.x * kNB + threadIdx.x]);
-    y[threadIdx.x] = b[k0 + threadIdx.x];
-  }
-  for (int s = nb - 1; s >= 0; --s) {
+    // rows below (forward) / above (backward) the block: work items
+    // (row, group of 16 columns), 16 independent loads in flight per item
+    const int lo = fwd ? max(r0, k0 + nb) : r0;
+    const int hi = fwd ? r1 : min(r1, k0);
+    const int nrows = max(hi - lo, 0);
+    for (int it = threadIdx.x; it < 4 * nrows; it += blockDim.x) {
+      const int g = it / nrows, r = lo + (it - g * nrows);
+      const T* col = LU + (size_t)(k0 + g * 16) * lda + r;
+      T l[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        l[u] = (g * 16 + u < nb) ? col[(size_t)u * lda] : CTraits<T>::make(0, 0);
+      T acc = CTraits<T>::make(0, 0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc = cfma(l[u], ys[(g * 16 + u) & (kNB - 1)], acc);
+      ps[g * rpb + (r - r0)] = acc;
+    }
     __syncthreads();
-    const T xs = cmul(y[s], rd[s]);
-    const int r = threadIdx.x;
-    if (r < s) y[r] = cfms(y[r], D[s * kNB + r], xs);
+    for (int r = lo + threadIdx.x; r < hi; r += blockDim.x) {
+      const int i = r - r0;
+      T v = bc[i];
+      v.x -= ps[i].x + ps[rpb + i].x + ps[2 * rpb + i].x + ps[3 * rpb + i].x;
+      v.y -= ps[i].y + ps[rpb + i].y + ps[2 * rpb + i].y + ps[3 * rpb + i].y;
+      bc[i] = v;
+    }
     __syncthreads();
-    if (r == s) y[s] = xs;
   }
-  __syncthreads();
-  if (threadIdx.x < nb) b[k0 + threadIdx.x] = y[threadIdx.x];
+  cl.sync();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[r0 + i] = bc[i];
 }
 
 template <typename T>
-void lu_solve(const T* LU, long long lda, int n, const int* ipiv, T* b, cudaStream_t s,
-              long long* launches) {
-  const size_t dsm = sizeof(T) * (kNB * kNB + 2 * kNB);
+int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+             cudaStream_t s, long long* launches) {
   static bool attr = false;
+  static int cmax = kMaxCluster;
   if (!attr) {
-    cudaFuncSetAttribute(fwd_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
-    cudaFuncSetAttribute(bwd_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm);
+    cudaFuncSetAttribute(trisolve_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kClusterSmem);
+    if (cudaFuncSetAttribute(trisolve_cluster_kernel<T>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      cmax = 8;
+    }
     attr = true;
   }
-  for (int k0 = 0; k0 < n; k0 += kNB) {
-    const int nb = std::min(kNB, n - k0);
-    fwd_diag_kernel<T><<<1, kNB, dsm, s>>>(LU, lda, k0, nb, ipiv, b);
-    ++*launches;
-    const int r0 = k0 + nb;
-    if (r0 < n) {
-      gemv_sub_kernel<T><<<(n - r0 + 127) / 128, 128, 0, s>>>(LU, lda, k0, nb, r0, n, b);
-      ++*launches;
-    }
+  for (;;) {
+    const int nk = (n + kNB - 1) / kNB;
+    const int C = std::max(1, std::min(cmax, nk));
+    const int rpb = ((nk + C - 1) / C) * kNB;
+    const size_t smem = sizeof(T) * ((size_t)rpb + kNB + 4 * (size_t)std::max(rpb, kNB));
+    if (smem > kClusterSmem) return BEM2D_ERR_ARG;
+    cudaError_t e = launch_cluster(trisolve_cluster_kernel<T>, C, 256, smem, s, LU, lda, n,
+                                   (const int*)w.perm, (const T*)w.dinv, b, x, rpb);
+    if (e == cudaSuccess) break;
+    cudaGetLastError();
+    if (cmax == 8) return BEM2D_ERR_CUDA;
+    cmax = 8;
   }
-  const int last = ((n - 1) / kNB) * kNB;
-  for (int k0 = last; k0 >= 0; k0 -= kNB) {
-    const int nb = std::min(kNB, n - k0);
-    bwd_diag_kernel<T><<<1, kNB, dsm, s>>>(LU, lda, k0, nb, b);
-    ++*launches;
-    if (k0 > 0) {
-      gemv_sub_kernel<T><<<(k0 + 127) / 128, 128, 0, s>>>(LU, lda, k0, nb, 0, k0, b);
-      ++*launches;
-    }
-  }
+  ++*launches;
+  return BEM2D_OK;
 }
 
 template int lu_factor<double2>(double2*, long long, int, const LuWork&, cudaStream_t, long long*);
 template int lu_factor<float2>(float2*, long long, int, const LuWork&, cudaStream_t, long long*);
-template void lu_solve<double2>(const double2*, long long, int, const int*, double2*, cudaStream_t, long long*);
-template void lu_solve<float2>(const float2*, long long, int, const int*, float2*, cudaStream_t, long long*);
+template int lu_solve<double2>(const double2*, long long, int, const LuWork&, const double2*,
+                               double2*, cudaStream_t, long long*);
+template int lu_solve<float2>(const float2*, long long, int, const LuWork&, const float2*, float2*,
+                              cudaStream_t, long long*);
 
 // ---- refinement helpers -----------------------------------------------------
 // r = b - A x in FP64; column chunks of 256 give partial sums per row.

@@ -127,12 +127,22 @@ int bem2d_gauss(int n, double* x, double* w);
  * alpha = 2, beta = 1, kernel = COMBINED, the matrix of
  * SoundSoftScattering::DiscretizeMatrix (lib/bem2d_soundsoftscattering.h:95-103).
  * eta is the coupling of COMBINED (CombinedSingleConjDouble(k) uses eta = k).
- * precision: BEM2D_PREC_FP64 only (the mixed solver consumes FP64 matrices).
- * out: complex128 n_unk x n_unk, leading dimension ld >= n_unk. */
+ * All arithmetic FP64.  out: complex128 n_unk x n_unk, ld >= n_unk. */
 int bem2d_discrete_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom,
                           const bem2d_quad* quad, int kernel, double k_re,
                           double k_im, double eta, double alpha, double beta,
                           void* out, int64_t ld);
+
+/* Mixed-precision variant of bem2d_discrete_kernel: same matrix, with the
+ * far-field bulk evaluated in compensated single-single (float-float)
+ * arithmetic on the FP32 pipe (~1e-14 relative per kernel evaluation) and
+ * the near-field, self and small-argument (k|x-y| <= 8) entries in FP64.
+ * Writes complex128 (out, ld) and its complex64 rounding (out32, ld32):
+ * the residual and LU inputs of the mixed solver.  Requires k > 0. */
+int bem2d_discrete_kernel_mixed(bem2d_ctx* ctx, const bem2d_geometry* geom,
+                                const bem2d_quad* quad, int kernel, double k_re,
+                                double k_im, double eta, double alpha, double beta,
+                                void* out, int64_t ld, void* out32, int64_t ld32);
 
 /* out = mass matrix: replaces EvalIdent (lib/bem2d_quadrature.cpp:79-127). */
 int bem2d_eval_ident(bem2d_ctx* ctx, const bem2d_geometry* geom,
@@ -163,7 +173,9 @@ int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
 /* SoundSoftScattering::Discretize() + Solve() in one call
  * (lib/bem2d_soundsoftscattering.h:95-126): A = Id + 2 K_combined(k, eta),
  * b = 2 <CombinedPlaneWave(dir, k, eta), phi_i>, x = A^{-1} b.  A and b stay
- * in the context's device workspace; only x (n_unk complex128) is written. */
+ * in the context's device workspace; only x (n_unk complex128) is written.
+ * BEM2D_PREC_MIXED assembles with bem2d_discrete_kernel_mixed's arithmetic
+ * and solves as bem2d_solve_system's mixed mode. */
 int bem2d_scattering_solve(bem2d_ctx* ctx, const bem2d_geometry* geom,
                            const bem2d_quad* quad, double k_re, double k_im,
                            double eta, double dir_x, double dir_y,

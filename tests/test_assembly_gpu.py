@@ -124,3 +124,36 @@ def test_oracle_at_kite_config_size(ctx):
     assert rel(A[rows, :], R) < max(TOL_MAT, 3 * floor), floor
     b = ctx.rhs(g, 100.0, d, 100.0, QUAD)
     assert rel(b, O.rhs(g, 100.0, d, 100.0)) < TOL_MAT
+
+
+MIXED_CASES = ["disk160", "kite128", "ellipsearc100", "trefoil48", "invellipse48",
+               "square_graded", "lshape_graded", "square_poly2", "triangle_lin", "two_squares"]
+
+
+@pytest.mark.parametrize("name", MIXED_CASES)
+def test_mixed_assembly_matches_fp64(ctx, name):
+    """Far field in float-float on the FP32 pipe: within 1e-12 of the FP64
+    assembly (relative Frobenius); the complex64 copy is its rounding."""
+    spec = CASES[name]
+    g = spec["geom"]()
+    k, eta = spec["k"], spec["eta"]
+    for kn in ("combined",) + tuple(spec.get("kernels", ())):
+        a, b = (2.0, 1.0) if kn == "combined" else (1.0, 0.0)
+        A64 = ctx.discrete_kernel(g, kn, k, eta, QUAD, alpha=a, beta=b)
+        Am, A32 = ctx.discrete_kernel_mixed(g, kn, k, eta, QUAD, alpha=a, beta=b)
+        if np.linalg.norm(A64) == 0:
+            assert np.abs(Am).max() < 1e-15
+            continue
+        assert rel(Am, A64) < 1e-12, kn
+        assert rel(A32.astype(np.complex128), Am) < 1e-7
+
+
+def test_mixed_assembly_kite_config(ctx):
+    """Kite N = 2048, k = 100: the mixed assembly against the FP64 one."""
+    from bem2d_gb300 import geometry as G
+    g = G.kite(2048).add_poly_basis(0)
+    A64 = ctx.discrete_kernel(g, "combined", 100.0, 100.0, QUAD, alpha=2.0, beta=1.0)
+    Am, A32 = ctx.discrete_kernel_mixed(g, "combined", 100.0, 100.0, QUAD, alpha=2.0, beta=1.0)
+    assert rel(Am, A64) < 1e-12
+    # entry-wise: no entry off by more than 1e-12 of the largest
+    assert np.abs(Am - A64).max() < 1e-12 * np.abs(A64).max()
