@@ -29,7 +29,9 @@ EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_gauss", "bem2d_discrete_kernel", "bem2d_discrete_kernel_mixed",
            "bem2d_eval_ident",
            "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
-           "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer"]
+           "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer",
+           "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_num_range",
+           "bem2d_eval_kernel"]
 
 
 class Bem2dError(RuntimeError):
@@ -92,6 +94,11 @@ def load():
         lib.bem2d_solve_system.argtypes = [vp, i32, vp, i64, vp, vp, i32, d, vp]
         lib.bem2d_scattering_solve.argtypes = [vp, vp, vp, d, d, d, d, d, i32, d, vp, vp]
         lib.bem2d_fma_peak.argtypes = [i32, ctypes.POINTER(d)]
+        lib.bem2d_change_basis.argtypes = [vp, i32, vp, i64, vp, i64, vp, i32, vp, i64]
+        lib.bem2d_l2_norm_cond.argtypes = [vp, i32, vp, i64, d, ctypes.POINTER(d),
+                                           ctypes.POINTER(d)]
+        lib.bem2d_num_range.argtypes = [vp, i32, vp, i64, i32, vp, d, vp]
+        lib.bem2d_eval_kernel.argtypes = [vp, vp, vp, i32, d, d, d, vp, i32, vp, vp]
         lib.bem2d_ctx_enable_timers.argtypes = [vp, i32]
         lib.bem2d_ctx_timer.argtypes = [vp, i32, ctypes.POINTER(d), ctypes.POINTER(i64)]
         _LIB = lib
@@ -240,6 +247,49 @@ class Context:
         self._check(self.lib.bem2d_solve_system(self.h, n, _ptr(A), lda, _ptr(b), _ptr(out),
                                                 PREC[precision], float(tol), ctypes.byref(info)))
         self.last_info = (info.info, info.iterations, info.residual)
+        return out
+
+    # -- dense operators ---------------------------------------------------
+    def change_basis(self, K, M, bstart):
+        """U^{-H} K U^{-1} with M = U^H U block diagonal (blocks at bstart)."""
+        n = K.shape[0]
+        K = np.asfortranarray(K, dtype=np.complex128)
+        M = np.asfortranarray(M, dtype=np.complex128)
+        bs = np.ascontiguousarray(bstart, dtype=np.int32)
+        out = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._check(self.lib.bem2d_change_basis(self.h, n, _ptr(K), n, _ptr(M), n, _ptr(bs),
+                                                len(bs) - 1, _ptr(out), n))
+        return out
+
+    def norm_cond(self, A, tol=0.0):
+        """(sigma_max, sigma_max / sigma_min) of A."""
+        n = A.shape[0]
+        A = np.asfortranarray(A, dtype=np.complex128)
+        nrm, cond = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.bem2d_l2_norm_cond(self.h, n, _ptr(A), n, float(tol),
+                                                ctypes.byref(nrm), ctypes.byref(cond)))
+        return nrm.value, cond.value
+
+    def num_range_lmax(self, A, thetas, tol=0.0):
+        """lambda_max of (e^{i th} A + e^{-i th} A^H)/2 for each angle."""
+        n = A.shape[0]
+        A = np.asfortranarray(A, dtype=np.complex128)
+        th = np.ascontiguousarray(thetas, dtype=np.float64)
+        out = np.zeros(len(th))
+        self._check(self.lib.bem2d_num_range(self.h, n, _ptr(A), n, len(th), _ptr(th),
+                                             float(tol), _ptr(out)))
+        return out
+
+    def potential(self, g, coeffs, points, kernel="single", k=10.0, eta=0.0, q=(3, 5, 0.15)):
+        """sum_u c_u int K(p, y) phi_u(y) ds(y) at the points (EvalKernel)."""
+        gh = _GeomHold(g)
+        c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
+        out = np.zeros(len(pts), dtype=np.complex128)
+        qq = quad(q)
+        self._check(self.lib.bem2d_eval_kernel(self.h, ctypes.byref(gh.c), ctypes.byref(qq),
+                                               KERNEL[kernel], float(k), 0.0, float(eta),
+                                               _ptr(c), len(pts), _ptr(pts), _ptr(out)))
         return out
 
     def scattering_solve(self, g, k, direction, eta=None, q=(3, 5, 0.15), precision="fp64",

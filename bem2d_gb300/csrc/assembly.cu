@@ -351,4 +351,68 @@ void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
                                                    eta, scale, out);
 }
 
+// ---------------------------------------------------------------------------
+// Potential of a density at points (EvalKernel, lib/bem2d_quadrature.h:184-228):
+// out[p] = sum_u c_u sum_q K(x_p, y_uq) W_uq, both normals the source node's.
+// One thread per point; unknowns staged through shared memory in chunks.
+template <int KERNEL>
+__global__ void __launch_bounds__(128)
+potential_kernel(int nunk, NodeTable t, int ng, double k, double eta,
+                 const double2* __restrict__ coef, int npts, const double* __restrict__ pts,
+                 double2* __restrict__ out) {
+  __shared__ double sx[128], sy[128], snx[128], sny[128], sw[128];
+  __shared__ double2 sc[128];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const double px = p < npts ? pts[2 * p] : 0.0, py = p < npts ? pts[2 * p + 1] : 0.0;
+  const double kq = 0.25 * k, eq = 0.25 * eta;
+  double ar = 0.0, ai = 0.0;
+  const int total = nunk * ng;
+  for (int base = 0; base < total; base += 128) {
+    const int v = base + threadIdx.x;
+    __syncthreads();
+    if (v < total) {
+      sx[threadIdx.x] = t.x[v];
+      sy[threadIdx.x] = t.y[v];
+      snx[threadIdx.x] = t.nx[v];
+      sny[threadIdx.x] = t.ny[v];
+      sw[threadIdx.x] = t.w[v];
+      sc[threadIdx.x] = coef[v / ng];
+    }
+    __syncthreads();
+    const int cnt = min(128, total - base);
+    if (p < npts) {
+      for (int i = 0; i < cnt; ++i) {
+        double kr, ki;
+        kernel_d<KERNEL>(k, kq, eq, px, py, sx[i], sy[i], snx[i], sny[i], snx[i], sny[i], &kr,
+                         &ki);
+        // coefficient * kernel * weight
+        const double2 c = sc[i];
+        const double vr = (c.x * kr - c.y * ki) * sw[i], vi = (c.x * ki + c.y * kr) * sw[i];
+        ar += vr;
+        ai += vi;
+      }
+    }
+  }
+  if (p < npts) out[p] = make_double2(ar, ai);
+}
+
+void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                      double eta, const double2* coef, int npts, const double* pts,
+                      double2* out, cudaStream_t s) {
+  const int blocks = (npts + 127) / 128;
+  switch (kernel) {
+    case BEM2D_KERNEL_SINGLE:
+      potential_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      break;
+    case BEM2D_KERNEL_DOUBLE:
+      potential_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      break;
+    case BEM2D_KERNEL_CONJDOUBLE:
+      potential_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      break;
+    default:
+      potential_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+  }
+}
+
 }  // namespace bem2d_gpu

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -14,6 +15,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "dense.cuh"
 
 namespace bem2d_gpu {
 
@@ -885,6 +887,388 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
     CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   }
+  return BEM2D_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Norms, change of basis, numerical range, potentials
+// ===========================================================================
+namespace bem2d_gpu {
+
+static double2* dev_out(bem2d_ctx* c, void* p, size_t elems, const char* name, int* rc) {
+  if (is_device_ptr(p)) return static_cast<double2*>(p);
+  return static_cast<double2*>(ws(c, name, sizeof(double2) * elems, rc));
+}
+
+// Deterministic start vector of unit norm (the same on every run).
+static std::vector<std::complex<double>> start_vector(int n) {
+  std::vector<std::complex<double>> v(n);
+  unsigned long long s = 0x9E3779B97F4A7C15ull;
+  double nrm = 0;
+  for (int i = 0; i < n; ++i) {
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    const double a = ((s >> 11) & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0) - 0.5;
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    const double b = ((s >> 11) & ((1ull << 53) - 1)) * (1.0 / 9007199254740992.0) - 0.5;
+    v[i] = std::complex<double>(a + 1.0, b);
+    nrm += std::norm(v[i]);
+  }
+  nrm = std::sqrt(nrm);
+  for (auto& x : v) x /= nrm;
+  return v;
+}
+
+// Largest singular value of an operator given y = op(x) and y = op^H(x), by
+// Golub-Kahan-Lanczos bidiagonalisation with two-pass Gram-Schmidt
+// reorthogonalisation of both bases.
+template <typename Op, typename OpH>
+static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const char* tag,
+                        double* sigma) {
+  int rc = 0;
+  const int mmax = std::min(n, 300);
+  double2* V = static_cast<double2*>(ws(c, (std::string(tag) + "V").c_str(),
+                                         sizeof(double2) * (size_t)n * (mmax + 1), &rc));
+  double2* U = static_cast<double2*>(ws(c, (std::string(tag) + "U").c_str(),
+                                         sizeof(double2) * (size_t)n * (mmax + 1), &rc));
+  double2* h = static_cast<double2*>(ws(c, "gk_h", sizeof(double2) * (mmax + 2), &rc));
+  double* nrm = static_cast<double*>(ws(c, "gk_nrm", sizeof(double) * 4, &rc));
+  if (!V || !U || !h || !nrm) return rc;
+  const std::vector<std::complex<double>> v0 = start_vector(n);
+  CUDA_TRY(c, cudaMemcpyAsync(V, v0.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+  std::vector<double> alpha, beta;
+  auto norm_of = [&](double2* w, double* out) -> int {
+    launch_batched_norm2(n, w, n, nrm, 1, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(out, nrm, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    *out = std::sqrt(*out);
+    return BEM2D_OK;
+  };
+  auto reorth = [&](double2* Q, int j, double2* w) {
+    for (int pass = 0; pass < 2; ++pass) {
+      launch_batched_dots(Q, 0, n, j, w, 0, h, 0, 1, c->stream);
+      launch_batched_sub(Q, 0, n, j, w, 0, h, 0, 1, c->stream);
+    }
+  };
+  auto normalize = [&](double2* w, double a) -> int {
+    std::vector<double> inv(1, 1.0 / a);
+    CUDA_TRY(c, cudaMemcpyAsync(nrm + 2, inv.data(), sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    launch_batched_scale(n, w, 0, nrm + 2, w, 0, 1, c->stream);
+    return BEM2D_OK;
+  };
+  // u_0 = op(v_0) / alpha_0
+  if ((rc = op(V, U))) return rc;
+  double a = 0;
+  if ((rc = norm_of(U, &a))) return rc;
+  if (!(a > 0) || !std::isfinite(a)) {
+    *sigma = a;
+    return std::isfinite(a) ? BEM2D_OK : fail(c, BEM2D_ERR_NONFINITE, "non-finite operator norm");
+  }
+  alpha.push_back(a);
+  if ((rc = normalize(U, a))) return rc;
+  double prev = -1, sig = a;
+  int stable = 0;
+  for (int j = 0; j < mmax; ++j) {
+    double2* vn = V + (size_t)(j + 1) * n;
+    double2* un = U + (size_t)(j + 1) * n;
+    // v_{j+1} = (op^H u_j - alpha_j v_j) / beta_j
+    if ((rc = oph(U + (size_t)j * n, vn))) return rc;
+    launch_axpy_real(n, alpha[j], V + (size_t)j * n, vn, c->stream);
+    reorth(V, j + 1, vn);
+    double b = 0;
+    if ((rc = norm_of(vn, &b))) return rc;
+    if (!(b > 1e-300)) break;
+    beta.push_back(b);
+    if ((rc = normalize(vn, b))) return rc;
+    // u_{j+1} = (op v_{j+1} - beta_j u_j) / alpha_{j+1}
+    if ((rc = op(vn, un))) return rc;
+    launch_axpy_real(n, b, U + (size_t)j * n, un, c->stream);
+    reorth(U, j + 1, un);
+    if ((rc = norm_of(un, &a))) return rc;
+    if (!(a > 1e-300)) break;
+    alpha.push_back(a);
+    if ((rc = normalize(un, a))) return rc;
+    // largest eigenvalue of B^T B (B: alpha on the diagonal, beta above)
+    const int k = (int)alpha.size();
+    std::vector<double> d(k), e(k, 0.0), ev;
+    for (int i = 0; i < k; ++i) {
+      d[i] = alpha[i] * alpha[i] + (i > 0 ? beta[i - 1] * beta[i - 1] : 0.0);
+      if (i + 1 < k) e[i] = alpha[i] * beta[i];
+    }
+    if (!tridiag_eigenvalues(d, e, &ev)) return fail(c, BEM2D_ERR_NOCONV, "tridiagonal QL failed");
+    sig = std::sqrt(*std::max_element(ev.begin(), ev.end()));
+    if (prev > 0 && std::fabs(sig - prev) <= tol * sig) {
+      if (++stable >= 2 && j >= 3) break;
+    } else {
+      stable = 0;
+    }
+    prev = sig;
+  }
+  *sigma = sig;
+  return BEM2D_OK;
+}
+
+}  // namespace bem2d_gpu
+
+extern "C" {
+
+int bem2d_change_basis(bem2d_ctx* c, int n, const void* K, int64_t ldk, const void* M,
+                       int64_t ldm, const int32_t* bstart, int nblk, void* out, int64_t ldo) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !K || !M || !out || !bstart || nblk < 1 || ldk < n || ldm < n || ldo < n)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (bstart[0] != 0 || bstart[nblk] != n) return fail(c, BEM2D_ERR_ARG, "blocks must cover 0..n");
+  std::vector<int> bs_of(n), bz_of(n);
+  for (int b = 0; b < nblk; ++b) {
+    const int s0 = bstart[b], s1 = bstart[b + 1];
+    if (s1 <= s0 || s1 - s0 > 16) return fail(c, BEM2D_ERR_ARG, "block %d has size %d", b, s1 - s0);
+    for (int i = s0; i < s1; ++i) {
+      bs_of[i] = s0;
+      bz_of[i] = s1 - s0;
+    }
+  }
+  cudaSetDevice(c->device);
+  int rc = 0;
+  int* dmeta = static_cast<int*>(ws(c, "cb_meta", sizeof(int) * 2 * (size_t)n, &rc));
+  double2* blk = static_cast<double2*>(ws(c, "cb_blk", sizeof(double2) * 16 * (size_t)n, &rc));
+  if (!dmeta || !blk) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(dmeta, bs_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dmeta + n, bz_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
+  // the mass blocks on the host (columns: hb[i*16 + p] = M[start_i + p, i])
+  std::vector<std::complex<double>> hb((size_t)16 * n);
+  if (is_device_ptr(M)) {
+    launch_gather_blocks(n, static_cast<const double2*>(M), ldm, dmeta, dmeta + n, blk, c->stream);
+    ++c->launches;
+    CUDA_TRY(c, cudaMemcpyAsync(hb.data(), blk, sizeof(double2) * 16 * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  } else {
+    const std::complex<double>* Mh = static_cast<const std::complex<double>*>(M);
+    for (int i = 0; i < n; ++i)
+      for (int p = 0; p < bz_of[i]; ++p) hb[(size_t)i * 16 + p] = Mh[(size_t)i * ldm + bs_of[i] + p];
+  }
+  // per block: M_b = U^H U (upper Cholesky), then U^{-1}
+  std::vector<std::complex<double>> ui((size_t)16 * n);
+  for (int b = 0; b < nblk; ++b) {
+    const int s0 = bstart[b], m = bstart[b + 1] - s0;
+    std::complex<double> Uc[16][16] = {}, Ui[16][16] = {};
+    auto Mb = [&](int r, int col) { return hb[(size_t)(s0 + col) * 16 + r]; };
+    for (int j = 0; j < m; ++j) {
+      double dj = Mb(j, j).real();
+      for (int k = 0; k < j; ++k) dj -= std::norm(Uc[k][j]);
+      if (!(dj > 0)) return fail(c, BEM2D_ERR_ARG, "mass block %d is not positive definite", b);
+      Uc[j][j] = std::sqrt(dj);
+      for (int l = j + 1; l < m; ++l) {
+        std::complex<double> v = Mb(j, l);
+        for (int k = 0; k < j; ++k) v -= std::conj(Uc[k][j]) * Uc[k][l];
+        Uc[j][l] = v / Uc[j][j];
+      }
+    }
+    for (int j = 0; j < m; ++j) {  // column j of U^{-1}
+      Ui[j][j] = 1.0 / Uc[j][j];
+      for (int i = j - 1; i >= 0; --i) {
+        std::complex<double> v = 0;
+        for (int k = i + 1; k <= j; ++k) v += Uc[i][k] * Ui[k][j];
+        Ui[i][j] = -v / Uc[i][i];
+      }
+    }
+    for (int j = 0; j < m; ++j)
+      for (int p = 0; p < m; ++p) ui[(size_t)(s0 + j) * 16 + p] = Ui[p][j];
+  }
+  double2* dui = static_cast<double2*>(ws(c, "cb_uinv", sizeof(double2) * 16 * (size_t)n, &rc));
+  if (!dui) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(dui, ui.data(), sizeof(double2) * 16 * n, cudaMemcpyHostToDevice, c->stream));
+  long long lk = 0;
+  const double2* dK = dev_in(c, K, n, n, ldk, "in_A", &lk, &rc);
+  if (!dK) return rc;
+  const bool odev = is_device_ptr(out);
+  double2* dO = dev_out(c, out, (size_t)n * n, "out", &rc);
+  if (!dO) return rc;
+  const long long lo = odev ? ldo : n;
+  launch_change_basis(n, dK, lk, dmeta, dmeta + n, dui, dO, lo, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  if (!odev)
+    CUDA_TRY(c, cudaMemcpy2DAsync(out, sizeof(double2) * ldo, dO, sizeof(double2) * n,
+                                  sizeof(double2) * n, n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEM2D_OK;
+}
+
+int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double tol, double* norm,
+                       double* cond) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !norm || !cond || lda < n) return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (!(tol > 0)) tol = 1e-13;
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "nc_A", &la, &rc);
+  if (!dA) return rc;
+  double2* part = static_cast<double2*>(ws(c, "mv_part", mv_part_bytes(n), &rc));
+  if (!part) return rc;
+  auto op = [&](const double2* x, double2* y) -> int {
+    launch_mv(dA, la, n, x, y, part, c->stream);
+    c->launches += 2;
+    return BEM2D_OK;
+  };
+  auto oph = [&](const double2* x, double2* y) -> int {
+    launch_mvh(dA, la, n, x, y, c->stream);
+    c->launches += 1;
+    return BEM2D_OK;
+  };
+  double smax = 0, inv_smin = 0;
+  if ((rc = gk_sigma_max(c, n, op, oph, tol, "gka", &smax))) return rc;
+  // sigma_min = 1 / sigma_max(A^{-1}) through a complex128 LU
+  LuWork w;
+  int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
+  if (!ints) return rc;
+  w.ipiv = ints + 8;
+  w.info = ints;
+  w.status = ints + 1;
+  w.scratch_bytes = lu_scratch_bytes(n);
+  w.scratch = ws(c, "lu_scratch", w.scratch_bytes, &rc);
+  char* aux = static_cast<char*>(ws(c, "lu_aux", lu_aux_bytes(n, sizeof(double2)), &rc));
+  double2* LU = static_cast<double2*>(ws(c, "lu64", sizeof(double2) * (size_t)n * n, &rc));
+  if (!w.scratch || !aux || !LU) return rc;
+  w.dinv = aux;
+  w.perm = reinterpret_cast<int*>(aux + (lu_aux_bytes(n, sizeof(double2)) - 256 - sizeof(int) * (size_t)n));
+  CUDA_TRY(c, cudaMemcpy2DAsync(LU, sizeof(double2) * n, dA, sizeof(double2) * la, sizeof(double2) * n,
+                                n, cudaMemcpyDeviceToDevice, c->stream));
+  if ((rc = lu_factor<double2>(LU, n, n, w, c->stream, &c->launches)))
+    return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+  int hinfo[2];
+  CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "LU panel wait timed out");
+  if (hinfo[0]) {
+    // singular: sigma_min = 0
+    *norm = smax;
+    *cond = INFINITY;
+    return fail(c, hinfo[0], "zero pivot at column %d", hinfo[0]);
+  }
+  double2* tmp = static_cast<double2*>(ws(c, "nc_tmp", sizeof(double2) * n, &rc));
+  if (!tmp) return rc;
+  auto iop = [&](const double2* x, double2* y) -> int {
+    int r = lu_solve<double2>(LU, n, n, w, x, y, c->stream, &c->launches);
+    return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+  };
+  auto ioph = [&](const double2* x, double2* y) -> int {
+    int r = lu_solve_h<double2>(LU, n, n, w, x, y, c->stream, &c->launches);
+    return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+  };
+  if ((rc = gk_sigma_max(c, n, iop, ioph, tol, "gkb", &inv_smin))) return rc;
+  *norm = smax;
+  *cond = smax * inv_smin;
+  return BEM2D_OK;
+}
+
+int bem2d_num_range(bem2d_ctx* c, int n, const void* A, int64_t lda, int nang,
+                    const double* theta, double tol, double* lmax) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || nang < 1 || !theta || !lmax || lda < n)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (!(tol > 0)) tol = 1e-13;
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "nr_A", &la, &rc);
+  if (!dA) return rc;
+  const int mmax = std::min(n, 160);
+  const long long qs = (long long)n * (mmax + 1);  // per-angle basis stride
+  double2* Q = static_cast<double2*>(ws(c, "nr_Q", sizeof(double2) * (size_t)qs * nang, &rc));
+  double2* Y1 = static_cast<double2*>(ws(c, "nr_Y1", sizeof(double2) * (size_t)n * nang, &rc));
+  double2* Y2 = static_cast<double2*>(ws(c, "nr_Y2", sizeof(double2) * (size_t)n * nang, &rc));
+  double2* W = static_cast<double2*>(ws(c, "nr_W", sizeof(double2) * (size_t)n * nang, &rc));
+  double2* h = static_cast<double2*>(ws(c, "nr_h", sizeof(double2) * (size_t)(mmax + 2) * nang, &rc));
+  double* sc = static_cast<double*>(ws(c, "nr_sc", sizeof(double) * 2 * nang + 64, &rc));
+  if (!Q || !Y1 || !Y2 || !W || !h || !sc) return rc;
+  double* dth = sc + nang;
+  CUDA_TRY(c, cudaMemcpyAsync(dth, theta, sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
+  const std::vector<std::complex<double>> v0 = start_vector(n);
+  for (int a = 0; a < nang; ++a)
+    CUDA_TRY(c, cudaMemcpyAsync(Q + (size_t)a * qs, v0.data(), sizeof(double2) * n,
+                                cudaMemcpyHostToDevice, c->stream));
+  std::vector<std::vector<double>> al(nang), be(nang);
+  std::vector<double> lam(nang, 0.0), prev(nang, NAN);
+  std::vector<int> stable(nang, 0);
+  std::vector<std::complex<double>> hh((size_t)(mmax + 2) * nang);
+  std::vector<double> nn(nang), inv(nang);
+  const int ldh = mmax + 2;
+  for (int j = 0; j < mmax; ++j) {
+    const double2* Qj = Q + (size_t)j * n;
+    launch_zgemm(false, dA, la, n, Qj, qs, nang, Y1, n, c->stream);
+    launch_zgemm(true, dA, la, n, Qj, qs, nang, Y2, n, c->stream);
+    launch_herm_combine(n, Y1, Y2, n, dth, W, n, nang, c->stream);
+    // two Gram-Schmidt passes against q_0..q_j; alpha_j = Re(<q_j, H q_j>)
+    launch_batched_dots(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(hh.data(), h, sizeof(double2) * (size_t)ldh * nang, cudaMemcpyDeviceToHost, c->stream));
+    launch_batched_sub(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
+    launch_batched_dots(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
+    launch_batched_sub(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
+    launch_batched_norm2(n, W, n, sc, nang, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * nang, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->launches += 8;
+    CHECK_LAUNCH(c);
+    bool all = true;
+    for (int a = 0; a < nang; ++a) {
+      al[a].push_back(hh[(size_t)a * ldh + j].real());
+      const double b = std::sqrt(nn[a]);
+      inv[a] = b > 1e-300 ? 1.0 / b : 0.0;
+      std::vector<double> d(al[a]), e(be[a]), ev;
+      e.resize(d.size(), 0.0);
+      if (!tridiag_eigenvalues(d, e, &ev)) return fail(c, BEM2D_ERR_NOCONV, "tridiagonal QL failed");
+      lam[a] = *std::max_element(ev.begin(), ev.end());
+      const double scale = std::max(std::fabs(lam[a]), 1e-300);
+      if (std::fabs(lam[a] - prev[a]) <= tol * scale || b <= 1e-300) {
+        ++stable[a];
+      } else {
+        stable[a] = 0;
+      }
+      prev[a] = lam[a];
+      be[a].push_back(b);
+      if (stable[a] < 2 || j < 3) all = false;
+    }
+    if (all) break;
+    // q_{j+1} = w / beta
+    CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
+    launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, nang, c->stream);
+    ++c->launches;
+  }
+  for (int a = 0; a < nang; ++a) lmax[a] = lam[a];
+  return BEM2D_OK;
+}
+
+int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
+                      int kernel, double k_re, double k_im, double eta, const void* coeffs,
+                      int npts, const double* points, void* out) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (kernel < BEM2D_KERNEL_SINGLE || kernel > BEM2D_KERNEL_COMBINED)
+    return fail(c, BEM2D_ERR_ARG, "unknown kernel %d", kernel);
+  if (npts < 0 || (npts > 0 && (!points || !out)) || !coeffs)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  int rc = check_k(c, k_re, k_im);
+  if (rc) return rc;
+  if (npts == 0) return BEM2D_OK;
+  cudaSetDevice(c->device);
+  Staged st;
+  if ((rc = stage(c, geom, quad, true, false, &st))) return rc;
+  long long l = 0;
+  const double2* dc = dev_in(c, coeffs, geom->n_unk, 1, geom->n_unk, "ek_c", &l, &rc);
+  if (!dc) return rc;
+  double* dp = static_cast<double*>(ws(c, "ek_p", sizeof(double) * 2 * (size_t)npts, &rc));
+  if (!dp) return rc;
+  CUDA_TRY(c, cudaMemcpyAsync(dp, points, sizeof(double) * 2 * npts, cudaMemcpyDefault, c->stream));
+  const bool odev = is_device_ptr(out);
+  double2* dO = dev_out(c, out, (size_t)npts, "ek_o", &rc);
+  if (!dO) return rc;
+  launch_potential(st.g, st.t, st.r.ng, kernel, k_re, eta, dc, npts, dp, dO, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  if (!odev)
+    CUDA_TRY(c, cudaMemcpyAsync(out, dO, sizeof(double2) * npts, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return BEM2D_OK;
 }
 

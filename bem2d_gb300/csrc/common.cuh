@@ -264,6 +264,10 @@ void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
                 double dx, double dy, double eta, double scale, double2* out,
                 cudaStream_t s);
 
+void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                      double eta, const double2* coef, int npts, const double* pts,
+                      double2* out, cudaStream_t s);
+
 // ---- launch interfaces (lu.cu) --------------------------------------------
 struct LuWork {
   int* ipiv;             // [n] pivot rows (0-based): row i was swapped with ipiv[i]
@@ -289,6 +293,11 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
 template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
              cudaStream_t s, long long* launches);
+
+// x = A^{-H} b with the factor of lu_factor (b and x must differ).
+template <typename T>
+int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+               cudaStream_t s, long long* launches);
 
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);

@@ -772,6 +772,122 @@ int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* 
   return BEM2D_OK;
 }
 
+// x = A^{-H} b = P^T L^{-H} U^{-H} b in one cluster launch.  Forward sweep
+// with U^H (lower), backward with L^H (upper, unit diagonal).  Per step
+// every CTA forms the partial sums sum_r conj(M[r, k0+c]) x_r over its own,
+// already final rows; one cluster barrier; the owner of block k adds the
+// partials over DSMEM and applies the conjugate transpose of the stored
+// diagonal-block inverse.  Partial buffers alternate by step parity.
+template <typename T>
+__global__ void __launch_bounds__(256)
+trisolve_h_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
+                          const int* __restrict__ perm, const T* __restrict__ dinv,
+                          const T* __restrict__ bin, T* __restrict__ xout, int rpb) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* bc = reinterpret_cast<T*>(smem_raw);  // [rpb]
+  T* part = bc + rpb;                       // [2][kNB]
+  T* v = part + 2 * kNB;                    // [kNB]
+  const int r0 = rank * rpb, r1 = min(n, r0 + rpb), nr = max(r1 - r0, 0);
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) bc[i] = bin[r0 + i];
+  const int nk = (n + kNB - 1) / kNB;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  cl.sync();
+  for (int step = 0; step < 2 * nk; ++step) {
+    const bool fwd = step < nk;
+    const int kb = fwd ? step : 2 * nk - 1 - step;
+    const int k0 = kb * kNB, nb = min(kNB, n - k0), par = step & 1;
+    const int lo = fwd ? r0 : max(r0, k0 + nb);
+    const int hi = fwd ? min(r1, k0) : r1;
+    for (int c = warp * 8; c < warp * 8 + 8; ++c) {
+      double sr = 0, si = 0;
+      if (c < nb) {
+        const T* col = LU + (size_t)(k0 + c) * lda;
+        for (int r = lo + lane; r < hi; r += 32) {
+          const T a = col[r], b = bc[r - r0];
+          sr += (double)a.x * b.x + (double)a.y * b.y;
+          si += (double)a.x * b.y - (double)a.y * b.x;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+      }
+      if (lane == 0) part[par * kNB + c] = CTraits<T>::make(sr, si);
+    }
+    cl.sync();
+    const int owner = k0 / rpb;
+    if (rank == owner) {
+      const int t = threadIdx.x;
+      if (t < nb) {
+        T acc = bc[k0 - r0 + t];
+        for (int q = 0; q < C; ++q) {
+          const T pq = cl.map_shared_rank(part, q)[par * kNB + t];
+          acc.x -= pq.x;
+          acc.y -= pq.y;
+        }
+        v[t] = acc;
+      }
+      __syncthreads();
+      // x_k = D^{-H} v with D^{-1} = (U or L)_kk^{-1} stored column-major
+      const T* Di = dinv + (size_t)(2 * kb + (fwd ? 1 : 0)) * kNB * kNB;
+      if (t < nb) {
+        T acc = CTraits<T>::make(0, 0);
+        for (int m = 0; m < nb; ++m) {
+          const T d = Di[t * kNB + m];  // D^{-1}[m, t]
+          // conj(d) * v[m]
+          acc.x += d.x * v[m].x + d.y * v[m].y;
+          acc.y += d.x * v[m].y - d.y * v[m].x;
+        }
+        bc[k0 - r0 + t] = acc;
+      }
+      __syncthreads();
+    }
+  }
+  cl.sync();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[perm[r0 + i]] = bc[i];
+}
+
+template <typename T>
+int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+               cudaStream_t s, long long* launches) {
+  static bool attr = false;
+  static int cmax = kMaxCluster;
+  if (!attr) {
+    cudaFuncSetAttribute(trisolve_h_cluster_kernel<T>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem);
+    if (cudaFuncSetAttribute(trisolve_h_cluster_kernel<T>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      cmax = 8;
+    }
+    attr = true;
+  }
+  if (b == x) return BEM2D_ERR_ARG;  // the scatter at the end needs distinct buffers
+  for (;;) {
+    const int nk = (n + kNB - 1) / kNB;
+    const int C = std::max(1, std::min(cmax, nk));
+    const int rpb = ((nk + C - 1) / C) * kNB;
+    const size_t smem = sizeof(T) * ((size_t)rpb + 3 * kNB);
+    if (smem > kClusterSmem) return BEM2D_ERR_ARG;
+    cudaError_t e = launch_cluster(trisolve_h_cluster_kernel<T>, C, 256, smem, s, LU, lda, n,
+                                   (const int*)w.perm, (const T*)w.dinv, b, x, rpb);
+    if (e == cudaSuccess) break;
+    cudaGetLastError();
+    if (cmax == 8) return BEM2D_ERR_CUDA;
+    cmax = 8;
+  }
+  ++*launches;
+  return BEM2D_OK;
+}
+
+template int lu_solve_h<double2>(const double2*, long long, int, const LuWork&, const double2*,
+                                 double2*, cudaStream_t, long long*);
+template int lu_solve_h<float2>(const float2*, long long, int, const LuWork&, const float2*,
+                                float2*, cudaStream_t, long long*);
+
 template int lu_factor<double2>(double2*, long long, int, const LuWork&, cudaStream_t, long long*);
 template int lu_factor<float2>(float2*, long long, int, const LuWork&, cudaStream_t, long long*);
 template int lu_solve<double2>(const double2*, long long, int, const LuWork&, const double2*,

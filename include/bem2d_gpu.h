@@ -170,6 +170,41 @@ int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
                        const void* b, void* x, int precision, double tol,
                        bem2d_solve_info* info);
 
+/* ---- norms, change of basis, numerical range, potentials --------------- */
+/* out = U^{-H} K U^{-1} where M = U^H U: replaces ChangeBasis
+ * (lib/bem2d_mathroutines.cpp:534-588, zpotrf + two ztrsm).  M must be block
+ * diagonal, as mass matrices are: nblk blocks starting at bstart[0..nblk-1]
+ * (bstart[0] = 0, bstart[nblk] = n, block sizes 1..16); entries of M outside
+ * the blocks are ignored.  BEM2D_ERR_ARG if a block is not positive
+ * definite (the reference would throw LapackError from zpotrf). */
+int bem2d_change_basis(bem2d_ctx* ctx, int n, const void* K, int64_t ldk, const void* M,
+                       int64_t ldm, const int32_t* bstart, int nblk, void* out,
+                       int64_t ldo);
+
+/* norm = sigma_max(A), cond = sigma_max / sigma_min: replaces L2NormCond
+ * (lib/bem2d_mathroutines.cpp:208-266, zgesvd).  Golub-Kahan-Lanczos
+ * bidiagonalisation with full reorthogonalisation, on A for sigma_max and on
+ * A^{-1} (complex128 LU, solves with A and A^H) for sigma_min, until the
+ * estimates change by less than tol (tol <= 0 selects 1e-13). */
+int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
+                       double* norm, double* cond);
+
+/* lmax[j] = largest eigenvalue of (e^{i th_j} A + e^{-i th_j} A^H) / 2 for
+ * nang angles th_j: the eigenvalue step of NumRange
+ * (lib/bem2d_mathroutines.cpp:590-653, zheev per angle; the smallest
+ * eigenvalue at th is -lmax at th + pi).  Lanczos with full
+ * reorthogonalisation, all angles in one block of matrix products. */
+int bem2d_num_range(bem2d_ctx* ctx, int n, const void* A, int64_t lda, int nang,
+                    const double* theta, double tol, double* lmax);
+
+/* out[j] = sum_u c_u sum_q K(p_j, y_uq) |J(y_uq)| phi_u(y_uq) w_q: the
+ * potential of the density c at npts points p (x0 y0 x1 y1 ...): replaces
+ * EvalKernel (lib/bem2d_quadrature.h:184-228; both normals are the source
+ * element's, as there).  out is complex128[npts], overwritten. */
+int bem2d_eval_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom, const bem2d_quad* quad,
+                      int kernel, double k_re, double k_im, double eta, const void* coeffs,
+                      int npts, const double* points, void* out);
+
 /* SoundSoftScattering::Discretize() + Solve() in one call
  * (lib/bem2d_soundsoftscattering.h:95-126): A = Id + 2 K_combined(k, eta),
  * b = 2 <CombinedPlaneWave(dir, k, eta), phi_i>, x = A^{-1} b.  A and b stay

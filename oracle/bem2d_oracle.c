@@ -570,3 +570,35 @@ int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
   }
   return 0;
 }
+
+/* EvalKernel (lib/bem2d_quadrature.h:184-228): out[j] = sum_u c_u sum_q
+ * K(p_j, y_uq) |J| phi_u(y_uq) w_q, both normals set to the source normal. */
+int orc_potential(const orc_geometry* g, int N, int kernel, double k, double eta,
+                  const double* coeffs, int npts, const double* pts, double* out) {
+  double xt[64], wt[64];
+  if (N < 1 || N > 64) return -1;
+  if (orc_gauss(N, xt, wt)) return -2;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (int j = 0; j < npts; ++j) {
+    double ar = 0, ai = 0;
+    for (int u = 0; u < g->n_unk; ++u) {
+      const int e = g->unk_elem[u];
+      for (int q = 0; q < N; ++q) {
+        elem_pt p = elem_eval(g, e, xt[q]);
+        double nx, ny;
+        normal_of(&p, &nx, &ny);
+        cplx v = kernel_eval(kernel, k, eta, pts[2 * j], pts[2 * j + 1], p.mx, p.my, nx, ny,
+                             nx, ny);
+        const double w = plength(p.dx, p.dy) * basis_eval(g, u, xt[q]) * wt[q];
+        const double cr = coeffs[2 * u], ci = coeffs[2 * u + 1];
+        ar += (cr * v.re - ci * v.im) * w;
+        ai += (cr * v.im + ci * v.re) * w;
+      }
+    }
+    out[2 * j] = ar;
+    out[2 * j + 1] = ai;
+  }
+  return 0;
+}

@@ -51,6 +51,11 @@ int orc_eval_ident(const orc_geometry* g, int N, double* out);
 int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
             double dy, double eta, double scale, double* out);
 
+/* potential of the density coeffs (complex128[n_unk]) at npts points
+ * (x0 y0 x1 y1 ...): EvalKernel. */
+int orc_potential(const orc_geometry* g, int N, int kernel, double k, double eta,
+                  const double* coeffs, int npts, const double* pts, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,3 +157,18 @@ def numrange_lmax(A, thetas):
         H = 0.5 * (m + m.conj().T)
         out.append(eigh(H, eigvals_only=True, driver="ev", check_finite=False)[-1])
     return np.array(out)
+
+
+def potential(g, coeffs, points, kernel="single", k=10.0, eta=0.0, N=5):
+    """EvalKernel: sum_u c_u int K(p, y) phi_u(y) ds(y) at the points."""
+    s, keep = _geom(g)
+    c = np.ascontiguousarray(coeffs, dtype=np.complex128)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
+    out = np.zeros(len(pts), dtype=np.complex128)
+    rc = lib().orc_potential(ctypes.byref(s), ctypes.c_int(N), ctypes.c_int(KERNELS[kernel]),
+                             ctypes.c_double(k), ctypes.c_double(eta),
+                             c.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(len(pts)),
+                             pts.ctypes.data_as(ctypes.c_void_p),
+                             out.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0
+    return out

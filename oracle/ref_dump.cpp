@@ -20,6 +20,7 @@
 //   op numrange KRE KIM ETA NANG OUTFILE     (NumRange of ChangeBasis(A,Id))
 //   op singvals KRE KIM ETA OUTFILE          (SingularValues of ChangeBasis(A,Id))
 //   op timing KRE KIM DX DY ETA OUTFILE      (wall-clock seconds: assemble, solve)
+//   op evalsol KRE KIM DX DY ETA OUTFILE X0 Y0 X1 Y1 ...  (EvalSol at the points)
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -181,6 +182,25 @@ int main(int argc, char** argv) {
       nc.push_back(norm);
       nc.push_back(cond);
       WriteDoubles(prefix + "_normcond.bin", nc);
+    } else if (what == "evalsol") {
+      double kre, kim, dx, dy, eta;
+      std::string out;
+      ss >> kre >> kim >> dx >> dy >> eta >> out;
+      std::vector<Point> pts;
+      double px, py;
+      while (ss >> px >> py) pts.push_back(Point(px, py));
+      freqtype k = {kre, kim};
+      Point dir(dx, dy);
+      PlaneWave pw(dir, k);
+      CombinedPlaneWave cpw(dir, k, eta);
+      SoundSoftScattering<PlaneWave, CombinedPlaneWave> s3(c.geom, k, pw, cpw);
+      s3.SetQuadOption(c.quad.L, c.quad.N, c.quad.sigma);
+      s3.Discretize();
+      s3.Solve();
+      pcvector v = s3.EvalSol(pts);
+      Matrix m((int)pts.size(), 1);
+      *m.data = *v;
+      WriteComplex(out, m);
     } else if (what == "numrange" || what == "singvals") {
       double kre, kim, eta;
       int nang = 0;

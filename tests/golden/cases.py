@@ -37,11 +37,13 @@ CASES = {
     # BASELINE config 1: unit disk, 160 equal-arc elements, k = 10, d = (1,0)
     "disk160": dict(geom=lambda: G.curve_equispaced(G.CIRCLE, 160).add_poly_basis(0),
                     k=10.0, direction=(1.0, 0.0), eta=10.0, full=True,
-                    kernels=("single", "double", "conjdouble")),
+                    kernels=("single", "double", "conjdouble"),
+                    evalsol=[(-1.5, 0.0), (2.0, 1.0), (0.0, -3.0), (1.2, 0.4)]),
     "diskchords64": dict(geom=lambda: G.disk_chords(64, 1.0).add_poly_basis(0),
                          k=5.0, direction=(1.0, 0.0), eta=5.0, full=True),
     "kite128": dict(geom=lambda: G.kite(128).add_poly_basis(0), k=15.0,
-                    direction=_dir(seeded_angle(0)), eta=15.0, full=True),
+                    direction=_dir(seeded_angle(0)), eta=15.0, full=True,
+                    evalsol=[(2.0, 0.0), (-2.5, 1.0), (0.3, 2.2)]),
     "ellipsearc100": dict(geom=lambda: G.ellipse_arc_closed(100).add_poly_basis(0),
                           k=10.0, direction=(0.0, 1.0), eta=10.0, full=True),
     "trefoil48": dict(geom=lambda: G.curve_equispaced(G.TREFOIL, 48).add_poly_basis(0),

@@ -63,6 +63,11 @@ def run_case(name, spec):
                          % (k, eta, spec["numrange"], tmp))
         if spec.get("singvals"):
             lines.append("op singvals %.17g 0 %.17g %s/singvals.bin" % (k, eta, tmp))
+        if spec.get("evalsol"):
+            pts = spec["evalsol"]
+            lines.append("op evalsol %.17g 0 %.17g %.17g %.17g %s/evalsol.bin %s"
+                         % (k, d[0], d[1], eta, tmp,
+                            " ".join("%.17g %.17g" % p for p in pts)))
         with open(os.path.join(tmp, "case.txt"), "w") as f:
             f.write("\n".join(lines) + "\n")
         subprocess.run([REF_DUMP, os.path.join(tmp, "case.txt")], check=True,
@@ -79,6 +84,9 @@ def run_case(name, spec):
                 out.update(probes(A, 1234))
         for kn in spec.get("kernels", ()):
             out["K_" + kn] = read_c("%s/k_%s.bin" % (tmp, kn), (n, n))
+        if spec.get("evalsol"):
+            out["evalsol_points"] = np.array(spec["evalsol"], dtype=np.float64)
+            out["evalsol"] = np.fromfile(tmp + "/evalsol.bin", dtype=np.complex128)
         if spec.get("numrange"):
             pts = np.loadtxt(tmp + "/numrange.txt")
             out["numrange"] = pts[:, 0] + 1j * pts[:, 1]
@@ -90,6 +98,7 @@ def run_case(name, spec):
 
 
 def main():
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"],
                    check=True, stdout=subprocess.DEVNULL)
     names = sys.argv[1:] or list(CASES)

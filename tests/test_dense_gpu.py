@@ -1,0 +1,126 @@
+"""GPU dense operators through the C ABI: ChangeBasis, L2NormCond (Lanczos
+extreme singular values), NumRange eigenvalues and EvalKernel potentials,
+against the reference's outputs (tests/golden) and the CPU oracle."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from golden.cases import CASES, QUAD
+
+pytestmark = pytest.mark.gpu
+
+
+def _load(name):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    return z, json.loads(str(z["meta"]))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from bem2d_gb300 import capi
+    c = capi.Context(0)
+    yield c
+    c.close()
+
+
+def blocks_of(g):
+    """Unknown ranges per element (the mass matrix's diagonal blocks)."""
+    ue = g.arrays()["unk_elem"]
+    starts = [0] + [i for i in range(1, len(ue)) if ue[i] != ue[i - 1]] + [len(ue)]
+    return np.array(starts, dtype=np.int32)
+
+
+@pytest.mark.parametrize("name", ["disk160", "kite128", "square_poly2", "triangle_lin"])
+def test_change_basis_matches_oracle(ctx, name):
+    from oracle import oracle as O
+    spec = CASES[name]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    M = ctx.eval_ident(g, QUAD)
+    B = ctx.change_basis(A, M, blocks_of(g))
+    R = O.change_basis(A, M)
+    assert rel(B, R) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["disk160", "diskchords64", "kite128", "ellipsearc100",
+                                  "square_graded", "square_poly2", "two_squares",
+                                  "square_numrange"])
+def test_norm_cond_matches_reference(ctx, name):
+    """SoundSoftScattering::NormCond = L2NormCond(ChangeBasis(A, Id))."""
+    z, meta = _load(name)
+    spec = CASES[name]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    nrm, cond = ctx.norm_cond(B)
+    ref_n, ref_c = z["normcond"]
+    assert abs(nrm - ref_n) < 1e-11 * ref_n
+    assert abs(cond - ref_c) < 1e-9 * ref_c
+
+
+def test_norm_cond_random(ctx):
+    rng = np.random.default_rng(5)
+    n = 300
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 3 * np.sqrt(n) * np.eye(n)
+    s = np.linalg.svd(A, compute_uv=False)
+    nrm, cond = ctx.norm_cond(A)
+    assert abs(nrm - s[0]) < 1e-12 * s[0]
+    assert abs(cond - s[0] / s[-1]) < 1e-10 * cond
+
+
+def test_num_range_matches_reference(ctx):
+    """lambda_max per angle vs zheev (oracle), and the reference's NumRange
+    boundary points (written with 6 digits)."""
+    from oracle import oracle as O
+    z, meta = _load("square_numrange")
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    n = spec["numrange"]
+    th = np.concatenate([np.arange(n) * np.pi / n, np.arange(n) * np.pi / n + np.pi])
+    lm = ctx.num_range_lmax(B, th)
+    ref = O.numrange_lmax(B, th)
+    assert np.abs(lm - ref).max() < 1e-12 * np.abs(ref).max()
+    steps = np.arange(n) * np.pi / n
+    eigs = np.concatenate([-lm[n:], lm[:n], [-lm[n]]])
+    st = np.concatenate([steps, steps, [0.0]])
+    pts = []
+    for i in range(2 * n):
+        c1, c2, s1, s2 = np.cos(st[i]), np.cos(st[i + 1]), np.sin(st[i]), np.sin(st[i + 1])
+        t1 = (eigs[i + 1] - eigs[i] * (c1 * c2 + s1 * s2)) / (s1 * c2 - s2 * c1)
+        pts.append(np.exp(-1j * st[i]) * (eigs[i] + 1j * t1))
+    pts.append(pts[0])
+    assert np.abs(np.array(pts) - z["numrange"]).max() < 1e-5 * np.abs(z["numrange"]).max()
+
+
+@pytest.mark.parametrize("name", ["disk160", "kite128"])
+def test_evalsol_matches_reference(ctx, name):
+    """u = u_inc - S phi at field points (SoundSoftScattering::EvalSol)."""
+    z, meta = _load(name)
+    spec = CASES[name]
+    g = spec["geom"]()
+    k, d = spec["k"], spec["direction"]
+    x = ctx.scattering_solve(g, k, d, spec["eta"], QUAD, precision="fp64")
+    pts = z["evalsol_points"]
+    pot = ctx.potential(g, x, pts, "single", k)
+    uinc = np.exp(1j * k * (d[0] * pts[:, 0] + d[1] * pts[:, 1]))
+    assert rel(uinc - pot, z["evalsol"]) < 1e-11
+
+
+@pytest.mark.parametrize("kernel", ["single", "double", "conjdouble", "combined"])
+def test_potential_matches_oracle(ctx, kernel):
+    from oracle import oracle as O
+    g = CASES["square_poly2"]["geom"]()
+    rng = np.random.default_rng(9)
+    c = rng.standard_normal(g.n_unknowns) + 1j * rng.standard_normal(g.n_unknowns)
+    pts = rng.uniform(-1.0, 2.0, (257, 2))
+    out = ctx.potential(g, c, pts, kernel, 7.0, 3.0)
+    ref = O.potential(g, c, pts, kernel, 7.0, 3.0)
+    assert rel(out, ref) < 1e-12
