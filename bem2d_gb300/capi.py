@@ -31,7 +31,9 @@ EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
            "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer",
            "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_num_range",
-           "bem2d_eval_kernel"]
+           "bem2d_eval_kernel", "bem2d_solve_system_noalloc"]
+
+NOALLOC_MAX_N = 1024  # BEM2D_NOALLOC_MAX_N
 
 
 class Bem2dError(RuntimeError):
@@ -92,6 +94,7 @@ def load():
         lib.bem2d_eval_ident.argtypes = [vp, vp, vp, vp, i64]
         lib.bem2d_dot_prod_basfuns.argtypes = [vp, vp, vp, i32, d, d, d, d, d, d, vp]
         lib.bem2d_solve_system.argtypes = [vp, i32, vp, i64, vp, vp, i32, d, vp]
+        lib.bem2d_solve_system_noalloc.argtypes = [vp, i32, vp, i64, vp, vp, vp]
         lib.bem2d_scattering_solve.argtypes = [vp, vp, vp, d, d, d, d, d, i32, d, vp, vp]
         lib.bem2d_fma_peak.argtypes = [i32, ctypes.POINTER(d)]
         lib.bem2d_change_basis.argtypes = [vp, i32, vp, i64, vp, i64, vp, i32, vp, i64]
@@ -246,6 +249,24 @@ class Context:
         info = SolveInfo_c()
         self._check(self.lib.bem2d_solve_system(self.h, n, _ptr(A), lda, _ptr(b), _ptr(out),
                                                 PREC[precision], float(tol), ctypes.byref(info)))
+        self.last_info = (info.info, info.iterations, info.residual)
+        return out
+
+    def solve_noalloc(self, A, b, out=None):
+        """FP64 solve through bem2d_solve_system_noalloc (no device allocation,
+        n <= NOALLOC_MAX_N)."""
+        n = A.shape[0]
+        if out is None:
+            out = np.zeros(n, dtype=np.complex128)
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
+            b = np.ascontiguousarray(b, dtype=np.complex128)
+            lda = n
+        else:
+            lda = A.stride(1)
+        info = SolveInfo_c()
+        self._check(self.lib.bem2d_solve_system_noalloc(self.h, n, _ptr(A), lda, _ptr(b),
+                                                        _ptr(out), ctypes.byref(info)))
         self.last_info = (info.info, info.iterations, info.residual)
         return out
 

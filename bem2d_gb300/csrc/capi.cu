@@ -1273,3 +1273,12 @@ int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Context accessors for entry points defined in other translation units.
+namespace bem2d_gpu {
+int ctx_device(const bem2d_ctx* c) { return c->device; }
+cudaStream_t ctx_stream(const bem2d_ctx* c) { return c->stream; }
+long long* ctx_launches(bem2d_ctx* c) { return &c->launches; }
+int ctx_fail(bem2d_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
+}  // namespace bem2d_gpu

@@ -268,6 +268,13 @@ void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, 
                       double eta, const double2* coef, int npts, const double* pts,
                       double2* out, cudaStream_t s);
 
+// ---- context accessors (capi.cu) ------------------------------------------
+int ctx_device(const bem2d_ctx* c);
+cudaStream_t ctx_stream(const bem2d_ctx* c);
+long long* ctx_launches(bem2d_ctx* c);
+// Records msg as the context's last error and returns code.
+int ctx_fail(bem2d_ctx* c, int code, const char* msg);
+
 // ---- launch interfaces (lu.cu) --------------------------------------------
 struct LuWork {
   int* ipiv;             // [n] pivot rows (0-based): row i was swapped with ipiv[i]

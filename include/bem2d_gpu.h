@@ -170,6 +170,28 @@ int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
                        const void* b, void* x, int precision, double tol,
                        bem2d_solve_info* info);
 
+/* Largest n bem2d_solve_system_noalloc accepts. */
+#define BEM2D_NOALLOC_MAX_N 1024
+
+/* x = A^{-1} b as bem2d_solve_system with BEM2D_PREC_FP64, without allocating
+ * device memory.  No counterpart in the reference.  For callers that may not
+ * call cudaMalloc: a solver inside an application whose memory pool owns the
+ * device, or a loop that cannot afford cudaMalloc/cudaFree synchronising the
+ * device.  It calls no cudaMalloc, cudaFree or allocating library routine;
+ * its work buffers live in one static device array of 21 MiB that the CUDA
+ * runtime reserves with this library's device code.
+ *   n <= BEM2D_NOALLOC_MAX_N, else BEM2D_ERR_ARG (message names the limit).
+ *   A, b, x: host or device memory; A and b are not modified.
+ *   The first call on each device looks up the array's address
+ *   (cudaGetSymbolAddress) and caches it; make that call before any stream
+ *   capture.  The array is shared by all calls on a device and keeps the
+ *   last call's contents (what must start at zero is cleared on every
+ *   call): calls whose GPU work overlaps race, so serialise them.
+ *   The context supplies the stream and the error message; it must have
+ *   been created beforehand (bem2d_ctx_create allocates no device memory). */
+int bem2d_solve_system_noalloc(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
+                               const void* b, void* x, bem2d_solve_info* info);
+
 /* ---- norms, change of basis, numerical range, potentials --------------- */
 /* out = U^{-H} K U^{-1} where M = U^H U: replaces ChangeBasis
  * (lib/bem2d_mathroutines.cpp:534-588, zpotrf + two ztrsm).  M must be block
