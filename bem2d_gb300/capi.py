@@ -31,7 +31,8 @@ EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
            "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer",
            "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_num_range",
-           "bem2d_eval_kernel", "bem2d_solve_system_noalloc"]
+           "bem2d_eval_kernel", "bem2d_solve_system_noalloc",
+           "bem2d_sweep_solve"]
 
 NOALLOC_MAX_N = 1024  # BEM2D_NOALLOC_MAX_N
 
@@ -95,6 +96,7 @@ def load():
         lib.bem2d_dot_prod_basfuns.argtypes = [vp, vp, vp, i32, d, d, d, d, d, d, vp]
         lib.bem2d_solve_system.argtypes = [vp, i32, vp, i64, vp, vp, i32, d, vp]
         lib.bem2d_solve_system_noalloc.argtypes = [vp, i32, vp, i64, vp, vp, vp]
+        lib.bem2d_sweep_solve.argtypes = [vp, i32, vp, vp, vp, vp, d, d, i32, d, i32, vp, vp]
         lib.bem2d_scattering_solve.argtypes = [vp, vp, vp, d, d, d, d, d, i32, d, vp, vp]
         lib.bem2d_fma_peak.argtypes = [i32, ctypes.POINTER(d)]
         lib.bem2d_change_basis.argtypes = [vp, i32, vp, i64, vp, i64, vp, i32, vp, i64]
@@ -327,6 +329,28 @@ class Context:
             ctypes.byref(info)))
         self.last_info = (info.info, info.iterations, info.residual)
         return out
+
+    def sweep_solve(self, geoms, ks, direction, etas=None, q=(3, 5, 0.15), precision="mixed",
+                    tol=0.0, nworkers=0, outs=None):
+        """Batched bem2d_sweep_solve over (geoms[i], ks[i]); returns the list of
+        solutions (numpy, or the given `outs`, which may be CUDA tensors)."""
+        nk = len(geoms)
+        holds = [g if isinstance(g, _GeomHold) else _GeomHold(g) for g in geoms]
+        garr = (Geometry_c * max(nk, 1))(*[h.c for h in holds])
+        kk = np.ascontiguousarray(ks, dtype=np.float64)
+        ee = None if etas is None else np.ascontiguousarray(etas, dtype=np.float64)
+        if outs is None:
+            outs = [np.zeros(h.n, dtype=np.complex128) for h in holds]
+        xptr = (ctypes.c_void_p * max(nk, 1))(*[_ptr(o).value for o in outs])
+        infos = (SolveInfo_c * max(nk, 1))()
+        qq = quad(q)
+        self._check(self.lib.bem2d_sweep_solve(
+            self.h, nk, garr, ctypes.byref(qq), kk.ctypes.data,
+            None if ee is None else ee.ctypes.data, float(direction[0]), float(direction[1]),
+            PREC[precision], float(tol), int(nworkers), xptr, infos))
+        self.sweep_infos = [(infos[i].info, infos[i].iterations, infos[i].residual)
+                            for i in range(nk)]
+        return outs
 
 
 def gauss(n):

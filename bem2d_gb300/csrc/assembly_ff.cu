@@ -10,6 +10,8 @@
 // where the small-argument Hankel pieces live; adjacent and identical pairs
 // belong to the FP64 near-field kernel as in the FP64 path.  Each entry is
 // stored twice: complex128 (refinement residual) and complex64 (the LU).
+#include <mutex>
+
 #include "common.cuh"
 #include "ff.cuh"
 #include "hankel_ff.cuh"
@@ -210,19 +212,29 @@ __global__ void deferred_fp64_kernel(NodeTable t, int ng, double k, double eta, 
   out32[(size_t)e.y * ld32 + e.x] = make_float2((float)re, (float)im);
 }
 
+// Device copy of the e^{i x} reduction table, made once per device (the
+// current one); thread-safe.
 static const float* expi_table_dev() {
-  static float* d = nullptr;  // per process; one device
-  if (!d) {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static float* tab[kMaxDev] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDev) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!tab[dev]) {
     float h[256];
     expi_table(h);
-    cudaMalloc(&d, sizeof h);
+    float* d = nullptr;
+    if (cudaMalloc(&d, sizeof h) != cudaSuccess) return nullptr;
     cudaMemcpy(d, h, sizeof h, cudaMemcpyHostToDevice);
+    tab[dev] = d;
   }
-  return d;
+  return tab[dev];
 }
 
 template <int KERNEL>
-static void launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+static int launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
                             double k, double eta, double alpha, double2* out, long long ld,
                             float2* out32, long long ld32, DeferList dl, cudaStream_t s) {
   KConstFF kc;
@@ -236,6 +248,7 @@ static void launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTabl
                       sizeof(long long) * 4 * kTileF;
   dim3 grid((g.n_unk + kTileF - 1) / kTileF, (g.n_unk + kTileF - 1) / kTileF);
   const float* tab = expi_table_dev();
+  if (!tab) return BEM2D_ERR_NOMEM;
   if (ng == 5) {
     far_ff_kernel<KERNEL, 5><<<grid, kFarFFThreads, smem, s>>>(g, t, tf, ng, kc, k, eta, alpha, out,
                                                                ld, out32, ld32, dl, tab);
@@ -246,25 +259,26 @@ static void launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTabl
     fn<<<grid, kFarFFThreads, smem, s>>>(g, t, tf, ng, kc, k, eta, alpha, out, ld, out32, ld32, dl,
                                          tab);
   }
+  return BEM2D_OK;
 }
 
-void launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
-                   int kernel, double k, double eta, double alpha, double2* out,
-                   long long ld, float2* out32, long long ld32, DeferList dl,
-                   cudaStream_t s) {
+int launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+                  int kernel, double k, double eta, double alpha, double2* out,
+                  long long ld, float2* out32, long long ld32, DeferList dl,
+                  cudaStream_t s) {
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      launch_far_ff_k<BEM2D_KERNEL_SINGLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
-      break;
+      return launch_far_ff_k<BEM2D_KERNEL_SINGLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32,
+                                                  ld32, dl, s);
     case BEM2D_KERNEL_DOUBLE:
-      launch_far_ff_k<BEM2D_KERNEL_DOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
-      break;
+      return launch_far_ff_k<BEM2D_KERNEL_DOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32,
+                                                  ld32, dl, s);
     case BEM2D_KERNEL_CONJDOUBLE:
-      launch_far_ff_k<BEM2D_KERNEL_CONJDOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl,
-                                               s);
-      break;
+      return launch_far_ff_k<BEM2D_KERNEL_CONJDOUBLE>(g, t, tf, ng, k, eta, alpha, out, ld, out32,
+                                                      ld32, dl, s);
     default:
-      launch_far_ff_k<BEM2D_KERNEL_COMBINED>(g, t, tf, ng, k, eta, alpha, out, ld, out32, ld32, dl, s);
+      return launch_far_ff_k<BEM2D_KERNEL_COMBINED>(g, t, tf, ng, k, eta, alpha, out, ld, out32,
+                                                    ld32, dl, s);
   }
 }
 

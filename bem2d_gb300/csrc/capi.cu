@@ -56,6 +56,7 @@ struct bem2d_ctx {
   long long launches = 0;
   std::unordered_map<std::string, bem2d_gpu::Buffer> bufs;
   std::map<bem2d_gpu::RuleKey, std::pair<void*, bem2d_gpu::DevRules>> rules;
+  std::vector<bem2d_ctx*> workers;  // per-thread contexts of batched sweeps
 };
 
 namespace bem2d_gpu {
@@ -387,11 +388,14 @@ static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, boo
     st->t = NodeTable{t, t + nn, t + 2 * nn, t + 3 * nn, t + 4 * nn};
     st->has_ff = ff_nodes;
     if (ff_nodes) {
-      const size_t bytes = sizeof(float2) * 5 * nn + sizeof(double2) * nu + sizeof(float) * nu;
+      // centres are double2: their offset is rounded up to 16 bytes (5 nn
+      // float2 entries end on an 8-byte boundary when nn is odd)
+      const size_t b_nodes = (sizeof(float2) * 5 * nn + 15) / 16 * 16;
+      const size_t bytes = b_nodes + sizeof(double2) * nu + sizeof(float) * nu;
       char* f = static_cast<char*>(ws(c, "nodes_ff", bytes, &rc));
       if (!f) return rc;
       float2* f2 = reinterpret_cast<float2*>(f);
-      double2* cen = reinterpret_cast<double2*>(f2 + 5 * nn);
+      double2* cen = reinterpret_cast<double2*>(f + b_nodes);
       st->tf = NodeTableFF{f2, f2 + nn, f2 + 2 * nn, f2 + 3 * nn, f2 + 4 * nn, cen,
                            reinterpret_cast<float*>(cen + nu)};
     }
@@ -445,8 +449,9 @@ static int assemble_mixed_dev(bem2d_ctx* c, const Staged& st, int kernel, double
   dl.capacity = cap;
   CUDA_TRY(c, cudaMemsetAsync(dl.count, 0, sizeof(unsigned), c->stream));
   int t = tic(c, BEM2D_PHASE_FAR);
-  launch_far_ff(st.g, st.t, st.tf, st.r.ng, kernel, k, eta, alpha, A, ld, A32, ld32, dl,
-                c->stream);
+  if (launch_far_ff(st.g, st.t, st.tf, st.r.ng, kernel, k, eta, alpha, A, ld, A32, ld32, dl,
+                    c->stream) != BEM2D_OK)
+    return fail(c, BEM2D_ERR_NOMEM, "device table for the far-field kernel");
   launch_deferred_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, dl, 0, A, ld, A32, ld32,
                        c->stream);
   toc(c, t);
@@ -511,6 +516,7 @@ int bem2d_ctx_create(int device, bem2d_ctx** out) {
 
 void bem2d_ctx_destroy(bem2d_ctx* c) {
   if (!c) return;
+  for (bem2d_ctx* w : c->workers) bem2d_ctx_destroy(w);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& kv : c->bufs)
@@ -1280,5 +1286,6 @@ namespace bem2d_gpu {
 int ctx_device(const bem2d_ctx* c) { return c->device; }
 cudaStream_t ctx_stream(const bem2d_ctx* c) { return c->stream; }
 long long* ctx_launches(bem2d_ctx* c) { return &c->launches; }
+std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c) { return c->workers; }
 int ctx_fail(bem2d_ctx* c, int code, const char* msg) { return fail(c, code, "%s", msg); }
 }  // namespace bem2d_gpu

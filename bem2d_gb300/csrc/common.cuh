@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/bem2d_gpu.h"
 #include "hankel.cuh"
@@ -241,11 +242,12 @@ struct DeferList {
 };
 
 // Mixed far field: float-float evaluation, writes complex128 (out) and
-// complex64 (out32) copies; deferred entries go to `dl`.
-void launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
-                   int kernel, double k, double eta, double alpha, double2* out,
-                   long long ld, float2* out32, long long ld32, DeferList dl,
-                   cudaStream_t s);
+// complex64 (out32) copies; deferred entries go to `dl`.  Returns
+// BEM2D_ERR_NOMEM if the device reduction table could not be made.
+int launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
+                  int kernel, double k, double eta, double alpha, double2* out,
+                  long long ld, float2* out32, long long ld32, DeferList dl,
+                  cudaStream_t s);
 // FP64 evaluation of the deferred entries (both outputs).
 void launch_deferred_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
                           double k, double eta, double alpha, const DeferList& dl,
@@ -272,6 +274,8 @@ void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, 
 int ctx_device(const bem2d_ctx* c);
 cudaStream_t ctx_stream(const bem2d_ctx* c);
 long long* ctx_launches(bem2d_ctx* c);
+// Worker contexts (own stream and workspace each) of the batched sweep.
+std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c);
 // Records msg as the context's last error and returns code.
 int ctx_fail(bem2d_ctx* c, int code, const char* msg);
 

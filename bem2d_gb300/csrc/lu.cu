@@ -23,7 +23,9 @@
 namespace cg = cooperative_groups;
 
 #include <algorithm>
+#include <atomic>
 #include <climits>
+#include <mutex>
 
 #include "common.cuh"
 #include "cplx.cuh"
@@ -354,12 +356,12 @@ gemm_sub_kernel(const T* __restrict__ Am, long long lda, const T* __restrict__ B
 
 template <typename T>
 static int panel_blocks(int H) {
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
+  static const int nsm = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(v, 1);
+  }();
   // at least 64 rows per block: fewer blocks make the per-column barrier
   // and the pivot agreement cheaper; one block per SM at most
   return std::max(1, std::min(nsm, (H + 63) / 64));
@@ -579,9 +581,11 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
   cudaMemsetAsync(w.info, 0, sizeof(int), s);
   cudaMemsetAsync(w.status, 0, sizeof(int), s);
   cudaMemsetAsync(sl.base, 0, slots_bytes(sizeof(T)), s);
-  static bool attr = false;
-  static bool cluster16 = true;
-  if (!attr) {
+  // one-time function attributes; thread-safe (workers of a sweep factor
+  // concurrently from several host threads)
+  static std::atomic<bool> cluster16{true};
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kClusterSmem);
@@ -597,8 +601,7 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     cudaFuncSetAttribute(dinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(T) * kNB * kNB));
     cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  });
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = std::min(kNB, n - k0);
     const int H = n - k0;
@@ -743,9 +746,9 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
 template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
              cudaStream_t s, long long* launches) {
-  static bool attr = false;
-  static int cmax = kMaxCluster;
-  if (!attr) {
+  static std::atomic<int> cmax{kMaxCluster};
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     cudaFuncSetAttribute(trisolve_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kClusterSmem);
     if (cudaFuncSetAttribute(trisolve_cluster_kernel<T>,
@@ -753,11 +756,10 @@ int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* 
       cudaGetLastError();
       cmax = 8;
     }
-    attr = true;
-  }
+  });
   for (;;) {
     const int nk = (n + kNB - 1) / kNB;
-    const int C = std::max(1, std::min(cmax, nk));
+    const int C = std::max(1, std::min(cmax.load(), nk));
     const int rpb = ((nk + C - 1) / C) * kNB;
     const size_t smem = sizeof(T) * ((size_t)rpb + kNB + 4 * (size_t)std::max(rpb, kNB));
     if (smem > kClusterSmem) return BEM2D_ERR_ARG;
@@ -853,9 +855,9 @@ trisolve_h_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
 template <typename T>
 int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
                cudaStream_t s, long long* launches) {
-  static bool attr = false;
-  static int cmax = kMaxCluster;
-  if (!attr) {
+  static std::atomic<int> cmax{kMaxCluster};
+  static std::once_flag attr;
+  std::call_once(attr, [] {
     cudaFuncSetAttribute(trisolve_h_cluster_kernel<T>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem);
     if (cudaFuncSetAttribute(trisolve_h_cluster_kernel<T>,
@@ -863,12 +865,11 @@ int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T
       cudaGetLastError();
       cmax = 8;
     }
-    attr = true;
-  }
+  });
   if (b == x) return BEM2D_ERR_ARG;  // the scatter at the end needs distinct buffers
   for (;;) {
     const int nk = (n + kNB - 1) / kNB;
-    const int C = std::max(1, std::min(cmax, nk));
+    const int C = std::max(1, std::min(cmax.load(), nk));
     const int rpb = ((nk + C - 1) / C) * kNB;
     const size_t smem = sizeof(T) * ((size_t)rpb + 3 * kNB);
     if (smem > kClusterSmem) return BEM2D_ERR_ARG;

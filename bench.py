@@ -1,17 +1,26 @@
 #!/usr/bin/env python
 """Benchmark: sound-soft scattering solves/s on one GB300 (replicas per GPU).
 
-Workload (default, `kite2048`): kite curve x(t) = (cos t + 0.65 cos 2t - 0.65,
-1.5 sin t), N = 2048 piecewise constants equispaced in t, k = 100, plane wave
-at the angle U[0, 2pi) drawn from numpy's default_rng(0), combined operator
-1/2 I + D' - i k S (eta = k), QuadOption {L=3, N=5, sigma=0.15}.
+Workloads (`--workload`):
+  ellipse_sweep256 (default)  ellipse with semi-axes (2,1) (EllipseArc(2,1,0,2pi)),
+      256 wavenumbers uniform in [20, 200], N_k = ceil(10 k P / 2pi)
+      (309 ... 3084 unknowns, sum N_k^2 = 9.03e8 entries), elements equispaced in
+      the parameter, plane wave d = (1, 0), eta = k.  One step = the whole sweep:
+      256 independent Discretize() + Solve() problems through bem2d_sweep_solve.
+  kite2048      kite curve, N = 2048 equispaced, k = 100, plane-wave angle from
+      numpy default_rng(0).uniform(0, 2pi); one step = one solve.
+  lshape16384   L-shaped domain (unit square minus [0.5,1]^2), corner grading
+      (8 levels, ratio 0.15), N = 16384, k = 500, d = (1, 0); one solve.
+  disk160       unit disk, 160 equal-arc elements, k = 10, d = (1, 0).
+All use the combined operator 1/2 I + D' - i eta S, QuadOption {L=3, N=5,
+sigma=0.15}.
 
-One step = one SoundSoftScattering::Discretize() + Solve() through the C ABI
-(bem2d_scattering_solve): FP64 assembly of A = Id + 2K and b, complex64 LU
-with partial pivoting, FP64 iterative refinement to backward error 1e-12
-(`mixed`).  The same step with a complex128 LU (`fp64`) is timed beside it
-(the plain FP64 GPU path).  Synthetic input: the geometry is generated, no
-dataset is read.
+A solve: FP64 near-field and small-argument assembly with a float-float
+far field, complex64 LU with partial pivoting, FP64 iterative refinement to
+backward error 1e-14 (`mixed`, the headline `value`).  Beside it the plain
+FP64 GPU path (FP64 assembly + complex128 LU, one problem after another) is
+timed (`plain_fp64`) and every mixed solution is compared with it.
+Synthetic input: geometries are generated, no dataset is read.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -35,24 +44,36 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 QUAD = (3, 5, 0.15)
+SWEEP_WORKERS = 8
 
 
 def workload(name):
+    """dict(problems=[(geometry, k, eta)], d, desc, cpu_sample=[indices])."""
     from bem2d_gb300 import geometry as G
-    if name == "kite2048":
+    if name == "ellipse_sweep256":
+        ks, ns = G.sweep_sizes(256, 20.0, 200.0)
+        probs = [(G.ellipse_arc_closed(n).add_poly_basis(0), float(k), float(k))
+                 for k, n in zip(ks, ns)]
+        return dict(problems=probs, d=(1.0, 0.0), cpu_sample=list(range(16, 256, 32)),
+                    ref_sample=[64, 192],
+                    desc="ellipse (2,1) sweep: 256 k uniform in [20,200], N_k = "
+                         "ceil(10 k P/2pi) = %d..%d, eta=k, d=(1,0), QuadOption{3,5,0.15}"
+                         % (min(ns), max(ns)))
+    if name in ("kite2048", "kite4096"):
+        n = int(name[4:])
         th = float(np.random.default_rng(0).uniform(0, 2 * math.pi))
-        g = G.kite(2048).add_poly_basis(0)
-        return dict(g=g, k=100.0, eta=100.0, d=(math.cos(th), math.sin(th)),
-                    desc="kite N=2048 equispaced, k=100, eta=k, plane wave angle "
-                         "%.15g (rng seed 0), QuadOption{3,5,0.15}" % th)
-    if name == "kite4096":
-        th = float(np.random.default_rng(0).uniform(0, 2 * math.pi))
-        g = G.kite(4096).add_poly_basis(0)
-        return dict(g=g, k=100.0, eta=100.0, d=(math.cos(th), math.sin(th)),
-                    desc="kite N=4096 equispaced, k=100, eta=k (profiling case)")
+        return dict(problems=[(G.kite(n).add_poly_basis(0), 100.0, 100.0)],
+                    d=(math.cos(th), math.sin(th)), cpu_sample=[0], ref_sample=[0],
+                    desc="kite N=%d equispaced, k=100, eta=k, plane wave angle %.15g "
+                         "(rng seed 0), QuadOption{3,5,0.15}" % (n, th))
+    if name == "lshape16384":
+        return dict(problems=[(G.lshape(4072, 8, 0.15).add_poly_basis(0), 500.0, 500.0)],
+                    d=(1.0, 0.0), cpu_sample=None, ref_sample=None,
+                    desc="L-shape, corner grading L=8 sigma=0.15, N=16384, k=500, eta=k, "
+                         "d=(1,0), QuadOption{3,5,0.15}")
     if name == "disk160":
         g = G.curve_equispaced(G.CIRCLE, 160).add_poly_basis(0)
-        return dict(g=g, k=10.0, eta=10.0, d=(1.0, 0.0),
+        return dict(problems=[(g, 10.0, 10.0)], d=(1.0, 0.0), cpu_sample=[0], ref_sample=[0],
                     desc="unit disk 160 equal-arc elements, k=10, d=(1,0)")
     raise SystemExit("unknown workload " + name)
 
@@ -113,30 +134,21 @@ def clocks_stop(p, f, path, gpu_index):
             "samples": len(sm)}
 
 
-def peaks():
-    try:
-        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        return {}
-
-
-def cpu_reference(w, steps, warmup, threads):
-    """The oracle (C restatement of the reference's assembly + LAPACK zgetrf /
-    zgetrs through scipy) on the host cores: returns (seconds per solve list,
-    x of the last solve)."""
+def cpu_solves(w, idx, threads):
+    """The oracle (C restatement of the reference's assembly, OpenMP, + scipy
+    LAPACK zgetrf/zgetrs) on the host cores for the problems `idx`: returns
+    (seconds, {index: x})."""
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
     from oracle import oracle as O
     from bem2d_gb300 import _build
     _build.build_oracle(with_reference=False)
-    times, x = [], None
-    for i in range(warmup + steps):
-        t0 = time.perf_counter()
-        A, b = O.system(w["g"], w["k"], w["d"], w["eta"], QUAD, threads=threads)
-        x = O.solve(A, b)
-        t1 = time.perf_counter()
-        if i >= warmup:
-            times.append(t1 - t0)
-    return times, x
+    xs = {}
+    t0 = time.perf_counter()
+    for i in idx:
+        g, k, eta = w["problems"][i]
+        A, b = O.system(g, k, w["d"], eta, QUAD, threads=threads)
+        xs[i] = O.solve(A, b)
+    return time.perf_counter() - t0, xs
 
 
 def run_reference(args):
@@ -144,9 +156,19 @@ def run_reference(args):
     if rank != 0:
         return
     w = workload(args.workload)
+    if not w["ref_sample"]:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the CPU restatement needs hours for this workload"}))
+        return
     threads = os.cpu_count() or 1
-    times, _ = cpu_reference(w, args.steps, args.warmup, threads)
-    v = len(times) / sum(times)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t, _ = cpu_solves(w, w["ref_sample"], threads)
+        if i >= args.warmup:
+            times.append(t)
+    v = len(w["ref_sample"]) * len(times) / sum(times)
+    sample = ("problems %s of %d per step (assemble + LU solve each)"
+              % (w["ref_sample"], len(w["problems"])))
     print(json.dumps({
         "impl": "reference", "metric": "solves/s", "value": v, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -154,31 +176,37 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w["desc"]},
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": "full assemble + LU solve per step (oracle restatement "
-                                   "of the reference + scipy LAPACK zgetrf/zgetrs)"},
+                         "sample": sample + "; oracle restatement of the reference "
+                                   "(OpenMP) + scipy LAPACK zgetrf/zgetrs"},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}))
 
 
 def run_only(args):
-    """Profiling driver: one phase only (assembly or solve), no JSON line."""
+    """Profiling driver: one phase only (assembly or solve) of the largest
+    problem of the workload, or the whole mixed sweep; no JSON line."""
     import torch
     from bem2d_gb300 import capi
     w = workload(args.workload)
-    n = w["g"].n_unknowns
-    arrays = w["g"].arrays()
+    probs = w["problems"]
+    g, k, eta = max(probs, key=lambda p: p[0].n_unknowns)
+    n = g.n_unknowns
+    arrays = g.arrays()
     ctx = capi.Context(0)
-    ctx.enable_timers(True)
-    A = torch.empty((n, n), dtype=torch.complex128, device="cuda")
+    ctx.enable_timers(args.only != "sweep")
+    A = torch.empty((n, n), dtype=torch.complex128, device="cuda") \
+        if args.only == "assembly" else None
     x = torch.zeros(n, dtype=torch.complex128, device="cuda")
     for _ in range(args.warmup + args.steps):
         if args.only == "assembly":
-            ctx.discrete_kernel(arrays, "combined", w["k"], w["eta"], QUAD, 2.0, 1.0, out=A)
+            ctx.discrete_kernel(arrays, "combined", k, eta, QUAD, 2.0, 1.0, out=A)
+        elif args.only == "sweep":
+            ctx.sweep_solve([p[0] for p in probs], [p[1] for p in probs], w["d"],
+                            [p[2] for p in probs], QUAD, "mixed", nworkers=SWEEP_WORKERS)
         else:
-            ctx.scattering_solve(arrays, w["k"], w["d"], w["eta"], QUAD,
-                                 precision=args.only, out=x)
+            ctx.scattering_solve(arrays, k, w["d"], eta, QUAD, precision=args.only, out=x)
     torch.cuda.synchronize()
-    print(json.dumps({"only": args.only, "workload": args.workload,
+    print(json.dumps({"only": args.only, "workload": args.workload, "n": n,
                       "timers_ms": {k: v[0] / max(v[1], 1) for k, v in ctx.timers().items()}}))
 
 
@@ -191,15 +219,21 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from bem2d_gb300 import capi
     w = workload(args.workload)
-    g = w["g"]
-    n = g.n_unknowns
+    probs = w["problems"]
+    P = len(probs)
     ctx = capi.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    x_dev = torch.zeros(n, dtype=torch.complex128, device="cuda")
-    x_host = torch.zeros(n, dtype=torch.complex128).pin_memory()
-    arrays = g.arrays()
-    h2d = sum(a.nbytes for a in arrays.values())
+    holds = [capi._GeomHold(g.arrays()) for g, _, _ in probs]
+    ks = [p[1] for p in probs]
+    etas = [p[2] for p in probs]
+    ns = [h.n for h in holds]
+    x_dev = [torch.zeros(n, dtype=torch.complex128, device="cuda") for n in ns]
+    x_pin = [torch.zeros(n, dtype=torch.complex128).pin_memory() for n in ns]
+    x_host = [t.numpy() for t in x_pin]
+    x_fp64 = [torch.zeros(n, dtype=torch.complex128, device="cuda") for n in ns]
+    h2d = sum(a.nbytes for h in holds for a in h.arrays.values()) + 16 * P
+    d2h = 16 * sum(ns)
 
     def barrier():
         torch.cuda.synchronize()
@@ -207,8 +241,11 @@ def run_ours(args):
             torch.distributed.barrier()
 
     def timed(fn, k, warm):
-        for _ in range(warm):
-            fn()
+        if callable(warm):
+            warm()
+        else:
+            for _ in range(warm):
+                fn()
         barrier()
         ms = []
         for _ in range(k):
@@ -218,7 +255,7 @@ def run_ours(args):
             e1 = torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 e0.record()
-            fn()
+            fn()  # host-synchronous: returns when every problem is solved
             with torch.cuda.stream(stream):
                 e1.record()
             e1.synchronize()
@@ -226,45 +263,67 @@ def run_ours(args):
         barrier()
         return ms
 
-    def step(prec, out):
-        return lambda: ctx.scattering_solve(arrays, w["k"], w["d"], w["eta"], QUAD,
-                                            precision=prec, out=out)
+    def mixed(outs):
+        if P == 1:
+            return lambda: ctx.scattering_solve(holds[0].arrays, ks[0], w["d"], etas[0], QUAD,
+                                                precision="mixed", out=outs[0])
+        return lambda: ctx.sweep_solve(holds, ks, w["d"], etas, QUAD, "mixed",
+                                       nworkers=SWEEP_WORKERS, outs=outs)
 
-    # -- headline: mixed path, device-resident result -------------------------
+    def fp64_all():
+        for i in range(P):
+            ctx.scattering_solve(holds[i].arrays, ks[i], w["d"], etas[i], QUAD,
+                                 precision="fp64", out=x_fp64[i])
+
+    big = int(np.argmax(ns))
+
+    def fp64_warm():  # workspace at its largest size; no full sweep
+        ctx.scattering_solve(holds[big].arrays, ks[big], w["d"], etas[big], QUAD,
+                             precision="fp64", out=x_fp64[big])
+
+    # -- headline: mixed path, device-resident results ------------------------
     clk_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
                             else "_build", "bench_clocks_%d.csv" % rank)
     os.makedirs(os.path.dirname(clk_path), exist_ok=True)
     cp, cf = clocks_start(clk_path)
     l0 = ctx.launches
-    ms_mixed = timed(step("mixed", x_dev), args.steps, args.warmup)
+    ms_mixed = timed(mixed(x_dev), args.steps, args.warmup)
     launches = (ctx.launches - l0) // (args.steps + args.warmup) * args.steps
     clocks = clocks_stop(cp, cf, clk_path, local)
-    info_mixed = ctx.last_info
-    # -- e2e: host result (device -> host copy inside the timed region) -------
-    ms_e2e = timed(step("mixed", x_host.numpy()), args.steps, 1)
-    # -- plain FP64 GPU path ---------------------------------------------------
-    ms_fp64 = timed(step("fp64", x_dev), max(2, args.steps // 2), 1)
-    # -- phase breakdown (events around each phase) ---------------------------
-    ctx.enable_timers(True)
-    step("mixed", x_dev)()
-    ph_mixed = ctx.timers()
-    ctx.enable_timers(True)
-    step("fp64", x_dev)()
-    ph_fp64 = ctx.timers()
-    ctx.enable_timers(False)
-    # -- roofline of the dominant kernel (FP64 far-field assembly) ------------
-    ctx.enable_timers(True)
-    A_dev = torch.empty((n, n), dtype=torch.complex128, device="cuda")
-    for _ in range(3):
-        ctx.discrete_kernel(arrays, "combined", w["k"], w["eta"], QUAD, 2.0, 1.0, out=A_dev)
-    far_ms, far_n = ctx.timers()["far"]
-    near_ms, near_n = ctx.timers()["near"]
-    ctx.enable_timers(False)
-    far_ms /= max(far_n, 1)
-    near_ms /= max(near_n, 1)
-    fp64_peak = capi.fma_peak("fp64")
-    flops_far = 100.0 * 25 * (n * n - 3 * n)
-    achieved = flops_far / (far_ms * 1e-3) / 1e12
+    infos = ctx.sweep_infos if P > 1 else [ctx.last_info]
+    # -- e2e: host results (device -> host copies inside the timed region) ----
+    ms_e2e = timed(mixed(x_host), args.steps, 1)
+    # -- plain FP64 GPU path, one problem after another -----------------------
+    fp64_steps = 1 if P > 1 or ns[0] > 8192 else max(2, args.steps // 2)
+    ms_fp64 = timed(fp64_all, fp64_steps, fp64_warm)
+    errs = [float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+            for a, b in zip(x_dev, x_fp64)]
+    # -- phases of the largest problem (events around each phase) -------------
+    def phases(prec):
+        ctx.enable_timers(True)
+        ctx.scattering_solve(holds[big].arrays, ks[big], w["d"], etas[big], QUAD,
+                             precision=prec, out=x_fp64[big] if prec == "fp64" else x_dev[big])
+        t = ctx.timers()
+        ctx.enable_timers(False)
+        return {k: v[0] for k, v in t.items()}
+
+    ph_mixed, ph_fp64 = phases("mixed"), phases("fp64")
+    nb = ns[big]
+    fp32_peak = capi.fma_peak("mixed")
+    lu_flops = 8.0 * nb ** 3 / 3.0
+    far_flops = 100.0 * 25 * (nb * nb - 3 * nb)
+    roof = {
+        "lu": {"bound": "fp32", "kernel": "complex64 LU (panel + trsm + gemm_sub_kernel<float2>)",
+               "achieved": lu_flops / (ph_mixed["lu"] * 1e-3) / 1e12,
+               "note": "8N^3/3 real flops (zgetrf count) per factorisation, N=%d" % nb},
+        "far": {"bound": "fp32", "kernel": "far_ff_kernel + deferred_fp64_kernel",
+                "achieved": far_flops / (ph_mixed["far"] * 1e-3) / 1e12,
+                "note": "100 flops per kernel evaluation (frozen convention), "
+                        "25 (N^2-3N) evaluations per launch, N=%d" % nb},
+    }
+    for r in roof.values():
+        r.update(peak=fp32_peak, unit="TFLOP/s", frac=r["achieved"] / fp32_peak, traffic=None)
+    dom = max(("lu", "far"), key=lambda p: ph_mixed[p])
 
     t_mixed = sum(ms_mixed) / len(ms_mixed)
     t_e2e = sum(ms_e2e) / len(ms_e2e)
@@ -274,57 +333,63 @@ def run_ours(args):
         t = torch.tensor(per_rank, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         per_rank = t.cpu().numpy()
-    t_mixed, t_e2e, t_fp64 = per_rank
+    t_mixed, t_e2e, t_fp64 = (float(v) for v in per_rank)
     if rank != 0:
         return
+    entries = float(sum(n * n for n in ns))
     res = {
-        "metric": "solves/s", "value": ws * 1e3 / t_mixed, "unit": "solves/s",
+        "metric": "solves/s", "value": ws * P * 1e3 / t_mixed, "unit": "solves/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 assembly + c64 LU + f64 refinement", "data": "synthetic",
-        "config": {"workload": w["desc"], "n_unknowns": n, "precision": "mixed",
+        "dtype": "c64 LU + f64 refinement; f64 near field, float-float far field",
+        "data": "synthetic",
+        "config": {"workload": w["desc"], "problems_per_step": P,
+                   "n_unknowns": ns[0] if P == 1 else [min(ns), max(ns)],
+                   "precision": "mixed", "sweep_workers": SWEEP_WORKERS if P > 1 else None,
                    "l2": "256 MB write between timed steps, outside the step events",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "e2e": {"value": ws * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": 16 * n},
+        "e2e": {"value": ws * P * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
-        "plain_fp64": {"value": ws * 1e3 / t_fp64, "unit": "solves/s", "ms_per_step": t_fp64},
+        "plain_fp64": {"value": ws * P * 1e3 / t_fp64, "unit": "solves/s", "ms_per_step": t_fp64,
+                       "steps": fp64_steps},
         "mixed_over_fp64": t_fp64 / t_mixed,
-        "galerkin_entries_per_s": n * n / ((far_ms + near_ms) * 1e-3),
-        "refinement": {"iterations": info_mixed[1], "backward_error": info_mixed[2]},
-        "phases_ms": {"mixed": {k: v[0] for k, v in ph_mixed.items()},
-                      "fp64": {k: v[0] for k, v in ph_fp64.items()}},
-        "roofline": {"bound": "fp64", "kernel": "far_fp64_kernel", "achieved": achieved,
-                     "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                     "traffic": None,
-                     "note": "100 flops per kernel evaluation (frozen convention), 25 (N^2-3N) "
-                             "evaluations per launch; peak = FP64 FMA chain measured in this run "
-                             "(MEASURED_PEAKS.json carries no FP64 figure)",
-                     "far_ms": far_ms, "near_ms": near_ms},
+        "galerkin_entries_per_s": ws * entries * 1e3 / t_mixed,
+        "mixed_vs_fp64_max_rel_err": max(errs),
+        "refinement": {"max_iterations": max(i[1] for i in infos),
+                       "max_backward_error": max(i[2] for i in infos)},
+        "phases_ms_largest": {"n": nb, "mixed": ph_mixed, "fp64": ph_fp64},
+        "roofline": dict(roof[dom], phase=dom),
+        "roofline_other": dict(roof["far" if dom == "lu" else "lu"]),
     }
+    res["roofline_other"]["phase"] = "far" if dom == "lu" else "lu"
     if clocks:
         res["clocks"] = clocks
-    if not args.no_cpu:
+    if not args.no_cpu and w["cpu_sample"]:
         threads = os.cpu_count() or 1
-        times, x_ref = cpu_reference(w, 1, 0, threads)
-        v = 1.0 / times[0]
+        secs, xr = cpu_solves(w, w["cpu_sample"], threads)
+        v = len(w["cpu_sample"]) / secs
         res["cpu_baseline"] = {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                               "sample": "one full assemble + LU solve (oracle restatement of "
-                                         "the reference, OpenMP, + scipy LAPACK)"}
-        x = x_dev.cpu().numpy()
-        res["rel_err_vs_oracle"] = float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))
+                               "sample": "problems %s of %d (assemble + LU solve each; oracle "
+                                         "restatement of the reference, OpenMP, + scipy LAPACK)"
+                                         % (w["cpu_sample"], P)}
+        rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        res["rel_err_vs_oracle"] = {
+            "mixed": max(rel(x_dev[i].cpu().numpy(), xr[i]) for i in xr),
+            "fp64": max(rel(x_fp64[i].cpu().numpy(), xr[i]) for i in xr),
+            "problems": sorted(xr)}
     print(json.dumps(res))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="kite2048")
+    ap.add_argument("--workload", default="ellipse_sweep256")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--only", choices=["assembly", "mixed", "fp64"],
+    ap.add_argument("--only", choices=["assembly", "mixed", "fp64", "sweep"],
                     help="profiling driver: run one phase, print its timers")
     args = ap.parse_args()
     if args.only:

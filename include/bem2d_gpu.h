@@ -239,6 +239,21 @@ int bem2d_scattering_solve(bem2d_ctx* ctx, const bem2d_geometry* geom,
                            int precision, double tol, void* x,
                            bem2d_solve_info* info);
 
+/* Batched sweep of nk independent bem2d_scattering_solve problems
+ * (geoms[i], k[i], eta[i] or k[i] if eta is NULL; one incident direction):
+ * replaces the serial per-wavenumber loop of the reference's sweeps
+ * (normcomps/ellipsenormcond.cpp:66-128, which rebuilds the geometry and
+ * the system for every k).  nworkers (<= 0: 8) host workers, each with its
+ * own stream and workspace, run the problems concurrently, largest first.
+ * x[i] (geoms[i].n_unk complex128, host or device) and infos[i] (may be
+ * NULL) receive each solution; results equal bem2d_scattering_solve's.
+ * Returns when every problem is done; on failure the first error (the
+ * message names the problem) and unfinished problems are skipped. */
+int bem2d_sweep_solve(bem2d_ctx* ctx, int nk, const bem2d_geometry* geoms,
+                      const bem2d_quad* quad, const double* k, const double* eta,
+                      double dir_x, double dir_y, int precision, double tol,
+                      int nworkers, void* const* x, bem2d_solve_info* infos);
+
 /* ---- measurement helpers (no counterpart in the reference) ------------ */
 /* Sustained FMA throughput of the FP64 (BEM2D_PREC_FP64) or FP32
  * (BEM2D_PREC_MIXED) pipe of the current device in TFLOP/s (2 flops per

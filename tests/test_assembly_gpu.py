@@ -157,3 +157,18 @@ def test_mixed_assembly_kite_config(ctx):
     assert rel(Am, A64) < 1e-12
     # entry-wise: no entry off by more than 1e-12 of the largest
     assert np.abs(Am - A64).max() < 1e-12 * np.abs(A64).max()
+
+
+@pytest.mark.parametrize("n", [3, 47, 309])
+def test_mixed_assembly_odd_sizes(ctx, n):
+    """Odd unknown counts (the float-float node table then ends off a 16-byte
+    boundary): mixed assembly and solve against the FP64 path."""
+    from bem2d_gb300 import geometry as G
+    g = G.ellipse_arc_closed(n).add_poly_basis(0)
+    k = 20.0
+    A64 = ctx.discrete_kernel(g, "combined", k, k, QUAD, alpha=2.0, beta=1.0)
+    Am, _ = ctx.discrete_kernel_mixed(g, "combined", k, k, QUAD, alpha=2.0, beta=1.0)
+    assert rel(Am, A64) < 1e-12
+    x64 = ctx.scattering_solve(g, k, (1.0, 0.0), k, QUAD, precision="fp64")
+    xm = ctx.scattering_solve(g, k, (1.0, 0.0), k, QUAD, precision="mixed")
+    assert rel(xm, x64) < 1e-10
