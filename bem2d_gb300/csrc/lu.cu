@@ -368,6 +368,39 @@ static int panel_blocks(int H) {
 }
 
 // ---- cluster panel ---------------------------------------------------------
+// The panel's H rows are split over the C CTAs of one cluster (rpb rows
+// each, at most kPanelRPT per thread) and held column-major in shared
+// memory; thread t owns rows t, t + 256, ... and is the only thread that
+// touches them, so the per-column update needs no intra-CTA barrier.
+// Candidates are pushed, not pulled: per column
+//   1. each thread: arg-max |re|+|im| over its rows >= kc, warp shuffles, one
+//      __syncthreads, warp 0 merges the warps and writes the CTA's candidate
+//      (value, row index, the whole row) into slot [parity][rank] of EVERY
+//      CTA's shared memory (DSMEM stores); warp 1 of the owner of row kc
+//      writes row kc into every CTA's krow[parity];
+//   2. one cluster barrier (release/acquire): all C candidates and row kc
+//      are now local to every CTA;
+//   3. every warp picks the pivot from the C local slots (ties to the smaller
+//      row, as izamax); the thread owning the pivot row takes row kc, the
+//      thread owning row kc takes the pivot row (the row swap), and every
+//      thread scales its rows below kc and applies the rank-1 update with the
+//      pivot row read from the local slot.
+// One __syncthreads and one cluster barrier per column, no DSMEM load on the
+// critical path.  Slots are double-buffered by column parity: a CTA can only
+// write the slots of column c + 1 after every CTA has left column c - 1.
+constexpr int kPanelRPT = 4;        // panel rows per thread at most
+constexpr int kMaxClusterPanel = 16;
+
+template <typename T>
+struct PanelSmem {
+  // offsets in units of T, after the [kNB][ldp] panel
+  static __host__ __device__ size_t slots(int ldp) { return (size_t)kNB * ldp; }
+  static __host__ __device__ size_t krow(int ldp) {
+    return slots(ldp) + (size_t)2 * kMaxClusterPanel * kNB;
+  }
+  static __host__ __device__ size_t total(int ldp) { return krow(ldp) + 2 * kNB; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads)
 panel_cluster_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
@@ -376,106 +409,562 @@ panel_cluster_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, in
   cg::cluster_group cl = cg::this_cluster();
   const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* P = reinterpret_cast<T*>(smem_raw);  // [rpb][kNB]
-  T* prow = P + (size_t)rpb * kNB;        // [kNB]
-  T* lcol = prow + kNB;                   // [rpb]
-  T* crow = lcol + rpb;                   // [2][kNB] candidate row per parity
-  T* krow = crow + 2 * kNB;               // [2][kNB] row kc per parity (owner)
-  __shared__ R cval[2];
-  __shared__ int cidx[2];
-  __shared__ int s_p, s_bw;
-  __shared__ R s_pv;
+  const int ldp = rpb | 1;  // odd column stride
+  T* P = reinterpret_cast<T*>(smem_raw);          // [kNB][ldp] panel rows, column-major
+  T* slot = P + PanelSmem<T>::slots(ldp);         // [2][kMaxClusterPanel][kNB] candidate rows
+  T* krow = P + PanelSmem<T>::krow(ldp);          // [2][kNB] row kc
+  __shared__ R sval[2][kMaxClusterPanel];
+  __shared__ int sidx[2][kMaxClusterPanel];
+  __shared__ R wv[kPanelThreads / 32];
+  __shared__ int wi[kPanelThreads / 32];
+  __shared__ int s_ipiv[kNB];  // pivots, written to global memory at the end
+  __shared__ int s_info;
   const int r0 = k0 + rank * rpb;
   const int r1 = min(r0 + rpb, n);
   const int nr = max(r1 - r0, 0);
-  for (int v = threadIdx.x; v < nr * nb; v += blockDim.x) {
-    const int c = v / nr, lr = v - c * nr;
-    P[lr * kNB + c] = A[(size_t)(k0 + c) * lda + r0 + lr];
-  }
+  const int lw = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int nw = (int)(blockDim.x >> 5);
+  for (int c = 0; c < nb; ++c)
+    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x)
+      P[c * ldp + lr] = A[(size_t)(k0 + c) * lda + r0 + lr];
+  if (threadIdx.x == 0) s_info = 0;
+  __syncthreads();
   cl.sync();  // every CTA of the cluster is running before any DSMEM access
   for (int c = 0; c < nb; ++c) {
     const int kc = k0 + c, par = c & 1;
+    // 1. local candidate, pushed to every CTA
+    T vc[kPanelRPT];
     R best = -1;
     int bidx = INT_MAX;
-    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-      const int gr = r0 + lr;
-      if (gr < kc) continue;
-      argmax_merge(best, bidx, cabs1(P[lr * kNB + c]), gr);
-    }
-    block_argmax(best, bidx);
-    if (threadIdx.x == 0) {
-      cval[par] = best;
-      cidx[par] = bidx;
-    }
-    if (bidx != INT_MAX)
-      for (int j = threadIdx.x; j < nb; j += blockDim.x) crow[par * kNB + j] = P[(bidx - r0) * kNB + j];
-    const bool own_k = kc >= r0 && kc < r1;
-    if (own_k)
-      for (int j = threadIdx.x; j < nb; j += blockDim.x) krow[par * kNB + j] = P[(kc - r0) * kNB + j];
-    cl.sync();
-    if (threadIdx.x < 32) {
-      R v = -1;
-      int i = INT_MAX;
-      for (int q = threadIdx.x; q < C; q += 32) {
-        argmax_merge(v, i, *cl.map_shared_rank(&cval[par], q), *cl.map_shared_rank(&cidx[par], q));
+#pragma unroll
+    for (int i = 0; i < kPanelRPT; ++i) {
+      const int lr = threadIdx.x + i * kPanelThreads;
+      if (lr < nr) {
+        vc[i] = P[c * ldp + lr];
+        if (r0 + lr >= kc) argmax_merge(best, bidx, cabs1(vc[i]), r0 + lr);
       }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R v2 = __shfl_xor_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bidx, o);
+      argmax_merge(best, bidx, v2, i2);
+    }
+    if (ln == 0) {
+      wv[lw] = best;
+      wi[lw] = bidx;
+    }
+    __syncthreads();
+    if (lw == 0) {
+      R v = ln < nw ? wv[ln] : R(-1);
+      int i = ln < nw ? wi[ln] : INT_MAX;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const R v2 = __shfl_xor_sync(0xffffffffu, v, o);
         const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
         argmax_merge(v, i, v2, i2);
       }
-      if (threadIdx.x == 0) {
-        if (i == INT_MAX || i < kc || i >= n) {
-          i = kc;
-          v = 0;
-        }
-        s_p = i;
-        s_bw = (i - k0) / rpb;
-        s_pv = v;
+      if (ln < C) {
+        *cl.map_shared_rank(&sval[par][rank], ln) = v;
+        *cl.map_shared_rank(&sidx[par][rank], ln) = i;
       }
-    }
-    __syncthreads();
-    const int p = s_p, bw = s_bw;
-    const bool zero = !(s_pv > 0);
-    const T* wrow = cl.map_shared_rank(crow, bw) + par * kNB;
-    for (int j = threadIdx.x; j < nb; j += blockDim.x) prow[j] = wrow[j];
-    if (rank == 0 && threadIdx.x == 0) {
-      ipiv[kc] = p;
-      if (zero && *info == 0) *info = kc + 1;
-    }
-    if (!zero && p != kc && p >= r0 && p < r1) {
-      const T* kr = cl.map_shared_rank(krow, (kc - k0) / rpb) + par * kNB;
-      for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(p - r0) * kNB + j] = kr[j];
-    }
-    __syncthreads();
-    if (!zero && p != kc && own_k)
-      for (int j = threadIdx.x; j < nb; j += blockDim.x) P[(kc - r0) * kNB + j] = prow[j];
-    __syncthreads();
-    if (!zero) {
-      const T inv = crcp(prow[c]);
-      for (int lr = threadIdx.x; lr < nr; lr += blockDim.x) {
-        if (r0 + lr > kc) {
-          const T l = cmul(P[lr * kNB + c], inv);
-          P[lr * kNB + c] = l;
-          lcol[lr] = l;
+      if (i != INT_MAX) {
+        const int lr = i - r0;
+        const T a0 = P[ln * ldp + lr], a1 = P[(ln + 32) * ldp + lr];
+        T* dst = slot + ((size_t)par * kMaxClusterPanel + rank) * kNB;
+        for (int q = 0; q < C; ++q) {
+          T* d = cl.map_shared_rank(dst, q);
+          d[ln] = a0;
+          d[ln + 32] = a1;
         }
       }
-      __syncthreads();
-      const int w = nb - c - 1;
-      if (w > 0) {
-        for (int u = threadIdx.x; u < nr * w; u += blockDim.x) {
-          const int lr = u / w, cc = c + 1 + (u - lr * w);
-          if (r0 + lr > kc) P[lr * kNB + cc] = cfms(P[lr * kNB + cc], lcol[lr], prow[cc]);
+    } else if (lw == 1 && kc >= r0 && kc < r1) {
+      const int lr = kc - r0;
+      const T a0 = P[ln * ldp + lr], a1 = P[(ln + 32) * ldp + lr];
+      T* dst = krow + (size_t)par * kNB;
+      for (int q = 0; q < C; ++q) {
+        T* d = cl.map_shared_rank(dst, q);
+        d[ln] = a0;
+        d[ln + 32] = a1;
+      }
+    }
+    // 2. every candidate and row kc local to every CTA
+    cl.sync();
+    // 3. pivot (every warp, from local slots), swap, scale, update
+    R v = -1;
+    int p = INT_MAX, from = 0;
+    if (ln < C) {
+      v = sval[par][ln];
+      p = sidx[par][ln];
+      from = ln;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, p, o);
+      const int f2 = __shfl_xor_sync(0xffffffffu, from, o);
+      if (v2 > v || (v2 == v && i2 < p)) {
+        v = v2;
+        p = i2;
+        from = f2;
+      }
+    }
+    const bool zero = !(v > 0) || p == INT_MAX || p < kc || p >= n;
+    if (threadIdx.x == 0) {
+      s_ipiv[c] = zero ? kc : p;
+      if (zero && s_info == 0) s_info = kc + 1;
+    }
+    if (zero) continue;  // LAPACK: no swap and no elimination for a zero pivot
+    const T* prow = slot + ((size_t)par * kMaxClusterPanel + from) * kNB;
+    const T* kr = krow + (size_t)par * kNB;
+    const T inv = crcp(prow[c]);
+#pragma unroll
+    for (int i = 0; i < kPanelRPT; ++i) {
+      const int lr = threadIdx.x + i * kPanelThreads;
+      if (lr >= nr) break;
+      const int gr = r0 + lr;
+      if (gr < kc) continue;
+      if (gr == kc) {
+        if (p != kc)  // row kc becomes the pivot row
+          for (int cc = 0; cc < nb; ++cc) P[cc * ldp + lr] = prow[cc];
+        continue;
+      }
+      T a = vc[i];
+      if (gr == p) {  // the pivot row takes row kc
+        for (int cc = 0; cc < nb; ++cc) P[cc * ldp + lr] = kr[cc];
+        a = kr[c];
+      }
+      const T l = cmul(a, inv);
+      P[c * ldp + lr] = l;
+      for (int cc0 = c + 1; cc0 < nb; cc0 += 8) {
+        T pv[8], pr[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (cc0 + u < nb) {
+            pv[u] = P[(cc0 + u) * ldp + lr];
+            pr[u] = prow[cc0 + u];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (cc0 + u < nb) P[(cc0 + u) * ldp + lr] = cfms(pv[u], l, pr[u]);
+      }
+    }
+  }
+  cl.sync();  // no CTA leaves while another may still write its shared memory
+  if (rank == 0) {
+    for (int c = threadIdx.x; c < nb; c += blockDim.x) ipiv[k0 + c] = s_ipiv[c];
+    if (threadIdx.x == 0 && s_info && *info == 0) *info = s_info;
+  }
+  for (int c = 0; c < nb; ++c)
+    for (int lr = threadIdx.x; lr < nr; lr += blockDim.x)
+      A[(size_t)(k0 + c) * lda + r0 + lr] = P[c * ldp + lr];
+}
+
+// ---- row-resident complex64 panel -------------------------------------------
+// Complex64 panels of up to 16 x 416 rows.  Thread t of CTA r owns rows t and
+// t + blockDim of its CTA's slice, stored row-major in shared memory (stride
+// 66 complex, 16-byte aligned rows) and is the only thread that ever changes
+// them.  Row exchanges are done by renaming: each row carries the index
+// (label) of the matrix row it currently represents; the pivot search runs
+// over (|re|+|im|, label) with ties to the smaller label (izamax order), and
+// at column c the pivot row takes label kc while the row labelled kc takes
+// the pivot's label - the permutation LAPACK applies with physical swaps, so
+// ipiv is the same.  At the end every row is written to the matrix row
+// named by its label.
+// A candidate is one 64-bit key: the bits of |re|+|im| (non-negative floats
+// order like their bit patterns) above (2^23 - 1 - label) and the local row,
+// so the arg-max is a plain maximum (one 64-bit shuffle per step).
+// Per column: warp maxima and one __syncthreads form the CTA key; warp 0
+// stages the candidate row (columns c..63) at a fixed place; one cluster
+// barrier; the warps read every CTA's key and staged row (one DSMEM round
+// trip) into local shared memory; a second __syncthreads; every warp picks
+// the pivot from the local keys, and each thread scales its rows and
+// applies the rank-1 update (16-byte shared-memory accesses, eight column
+// pairs per batch).  The update streams the CTA's rows through shared
+// memory, so the slices are kept short (64 rows per CTA while 16 CTAs
+// suffice) and the CTA has one thread per row.
+constexpr int kRowsMaxThreads = 256;
+constexpr int kRowsRPT = 2;     // rows per thread
+constexpr int kRowsLd = 66;     // complex64 per smem row (528 bytes)
+constexpr int kRowsMaxRpb = 416;
+constexpr int kRowsMinRpb = 64;
+constexpr int kLabelBits = 23;  // labels (matrix rows) below 2^23
+
+__host__ __device__ constexpr size_t panel_rows_smem(int rpb) {
+  return sizeof(float2) * ((size_t)rpb * kRowsLd + (size_t)(2 + kMaxClusterPanel) * kNB);
+}
+
+__device__ __forceinline__ unsigned long long pivot_key(float a, int label, int lr) {
+  return ((unsigned long long)__float_as_uint(a) << 32) |
+         ((unsigned long long)((1u << kLabelBits) - 1u - (unsigned)label) << 9) | (unsigned)lr;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, k, o);
+    k = k2 > k ? k2 : k;
+  }
+  return k;
+}
+
+__global__ void __launch_bounds__(kRowsMaxThreads, 1)
+panel_rows_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
+                  int* __restrict__ ipiv, int* info) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int T = (int)blockDim.x, nw = T >> 5;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* P = reinterpret_cast<float2*>(smem_raw);   // [rpb][kRowsLd]
+  float2* cand = P + (size_t)rpb * kRowsLd;           // [2][kNB] this CTA's candidate row
+  float2* stage = cand + 2 * kNB;                     // [kMaxClusterPanel][kNB] all candidates
+  __shared__ unsigned long long ckey[2];
+  __shared__ unsigned long long skey[kMaxClusterPanel];
+  __shared__ unsigned long long wkey[kRowsMaxThreads / 32];
+  __shared__ int s_ipiv[kNB];  // pivots, written to global memory at the end
+  __shared__ int s_info;
+  const int lw = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int r0 = k0 + rank * rpb;
+  const int nr = max(min(rpb, n - r0), 0);
+  int label[kRowsRPT];
+#pragma unroll
+  for (int i = 0; i < kRowsRPT; ++i) {
+    const int lr = threadIdx.x + i * T;
+    label[i] = lr < nr ? r0 + lr : INT_MAX;
+  }
+  // load: 16 columns of a row in flight per thread
+  for (int lr = threadIdx.x; lr < nr; lr += T) {
+    const float2* src = A + (size_t)k0 * lda + r0 + lr;
+    for (int c0 = 0; c0 < kNB; c0 += 16) {
+      float2 v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u)
+        v[u] = c0 + u < nb ? src[(size_t)(c0 + u) * lda] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) P[lr * kRowsLd + c0 + u] = v[u];
+    }
+  }
+  if (threadIdx.x == 0) s_info = 0;
+  __syncthreads();
+  cl.sync();  // every CTA of the cluster is running before any DSMEM access
+  for (int c = 0; c < nb; ++c) {
+    const int kc = k0 + c, par = c & 1;
+    // 1. CTA candidate key
+    unsigned long long key = 0;
+    float2 vc[kRowsRPT];
+#pragma unroll
+    for (int i = 0; i < kRowsRPT; ++i) {
+      const int lr = threadIdx.x + i * T;
+      vc[i] = make_float2(0.f, 0.f);
+      if (label[i] != INT_MAX) {
+        vc[i] = P[lr * kRowsLd + c];
+        const float a = cabs1(vc[i]);
+        if (label[i] >= kc && a >= 0.f) {  // NaN never wins, as in izamax
+          const unsigned long long k2 = pivot_key(a, label[i], lr);
+          key = k2 > key ? k2 : key;
         }
       }
     }
+    key = warp_max_key(key);
+    if (ln == 0) wkey[lw] = key;
     __syncthreads();
+    // 2. warp 0: the CTA key and its row, staged at a fixed place
+    if (lw == 0) {
+      key = warp_max_key(ln < nw ? wkey[ln] : 0ull);
+      if (key) {
+        const float2* src = P + (size_t)(key & 511ull) * kRowsLd;
+        if (c + ln < kNB) cand[par * kNB + c + ln] = src[c + ln];
+        if (c + 32 + ln < kNB) cand[par * kNB + c + 32 + ln] = src[c + 32 + ln];
+      }
+      if (ln == 0) ckey[par] = key;
+    }
+    cl.sync();
+    // 3. every CTA's key and staged row into local shared memory
+    for (int q = lw; q < C; q += nw) {
+      const float2* src = cl.map_shared_rank(cand, q) + par * kNB;
+      const unsigned long long kq = *cl.map_shared_rank(&ckey[par], q);
+      if (c + ln < kNB) stage[q * kNB + c + ln] = src[c + ln];
+      if (c + 32 + ln < kNB) stage[q * kNB + c + 32 + ln] = src[c + 32 + ln];
+      if (ln == 0) skey[q] = kq;
+    }
+    __syncthreads();
+    // 4. the pivot (every warp, from local keys)
+    const unsigned long long mine = ln < C ? skey[ln] : 0ull;
+    const unsigned long long best = warp_max_key(mine);
+    const float v = __uint_as_float((unsigned)(best >> 32));
+    const int p = (int)((1u << kLabelBits) - 1u - (unsigned)((best >> 9) & ((1u << kLabelBits) - 1u)));
+    const bool zero = best == 0ull || !(v > 0.f) || p < kc || p >= n;
+    if (threadIdx.x == 0) {
+      // no global store inside the loop: the release of the next cluster
+      // barrier would wait for it
+      s_ipiv[c] = zero ? kc : p;
+      if (zero && s_info == 0) s_info = kc + 1;
+    }
+    if (zero) continue;  // LAPACK neither swaps nor eliminates
+    const int q = __ffsll((long long)__ballot_sync(0xffffffffu, mine == best)) - 1;
+    const float2* prow = stage + q * kNB;
+    const float4* pr4 = reinterpret_cast<const float4*>(prow);
+    const float2 inv = crcp(prow[c]);
+    const int j0 = c >> 1;
+#pragma unroll
+    for (int i = 0; i < kRowsRPT; ++i) {
+      if (label[i] == p)
+        label[i] = kc;
+      else if (label[i] == kc)
+        label[i] = p;
+      if (label[i] <= kc || label[i] == INT_MAX) continue;
+      const int lr = threadIdx.x + i * T;
+      float4* row = reinterpret_cast<float4*>(P + (size_t)lr * kRowsLd);
+      const float2 l = cmul(vc[i], inv);
+      {  // the pair holding column c
+        const float4 w = row[j0];
+        float2 a = make_float2(w.x, w.y), b = make_float2(w.z, w.w);
+        if (c & 1) {
+          b = l;
+        } else {
+          a = l;
+          b = cfms(b, l, prow[c + 1]);
+        }
+        row[j0] = make_float4(a.x, a.y, b.x, b.y);
+      }
+      for (int jb = j0 + 1; jb < kNB / 2; jb += 8) {
+        float4 w[8], pq[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (jb + u < kNB / 2) {
+            w[u] = row[jb + u];
+            pq[u] = pr4[jb + u];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (jb + u < kNB / 2) {
+            const float2 a = cfms(make_float2(w[u].x, w[u].y), l, make_float2(pq[u].x, pq[u].y));
+            const float2 b = cfms(make_float2(w[u].z, w[u].w), l, make_float2(pq[u].z, pq[u].w));
+            row[jb + u] = make_float4(a.x, a.y, b.x, b.y);
+          }
+        }
+      }
+    }
   }
   cl.sync();  // no CTA leaves while another may still read its shared memory
-  for (int v = threadIdx.x; v < nr * nb; v += blockDim.x) {
-    const int c = v / nr, lr = v - c * nr;
-    A[(size_t)(k0 + c) * lda + r0 + lr] = P[lr * kNB + c];
+  if (rank == 0) {
+    for (int c = threadIdx.x; c < nb; c += T) ipiv[k0 + c] = s_ipiv[c];
+    if (threadIdx.x == 0 && s_info && *info == 0) *info = s_info;
+  }
+#pragma unroll
+  for (int i = 0; i < kRowsRPT; ++i) {
+    if (label[i] == INT_MAX) continue;
+    const int lr = threadIdx.x + i * T;
+    for (int cc = 0; cc < nb; ++cc) A[(size_t)(k0 + cc) * lda + label[i]] = P[lr * kRowsLd + cc];
+  }
+}
+
+// ---- register-window complex64 panel ----------------------------------------
+// Complex64 panels of up to 16 x 256 rows.  Two threads per row, each
+// holding every other column pair of it in registers (thread h of a row holds
+// pairs 2i + h, i = 0..15, as float4 r[16]).  Columns are processed in
+// blocks of four (two pairs, one per thread of the row): inside a block the
+// column index is a compile-time constant (the loop is unrolled), so every
+// register index is static; after a block its finished pairs go to shared
+// memory (Fin) and each thread's window shifts by one, so r[i] holds pair
+// 2(b + i) + h in block b.  Rows are exchanged by renaming, as in the
+// shared-memory panels (same ipiv).
+// Reductions use the warp reduce instructions: the maximum of (bits of
+// |re|+|im|) + 1 (0 = no candidate; non-negative floats order like their
+// bits), then the minimum label among the lanes holding that maximum.
+// Per column: one __syncthreads for the warp maxima, one for the CTA
+// candidate, whose two threads stage its row (columns c..63) in shared
+// memory; one cluster barrier; the threads pull every CTA's key and staged
+// row (one DSMEM round trip); a third __syncthreads; every warp picks the
+// pivot and each thread updates its registers.
+constexpr int kWinMaxRows = 256;
+constexpr int kWinMaxThreads = 2 * kWinMaxRows;
+
+__host__ __device__ constexpr size_t panel_win_smem(int rpb) {
+  return sizeof(float2) * ((size_t)rpb * kRowsLd + (size_t)(2 + kMaxClusterPanel) * kNB);
+}
+
+__device__ __forceinline__ float2 crcp_fast(float2 a) {
+  // 1/a = conj(a) / |a|^2 with the components scaled by 1/max(|re|,|im|)
+  const float sc = fmaxf(fabsf(a.x), fabsf(a.y));
+  const float rs = __frcp_rn(sc);
+  const float ar = a.x * rs, ai = a.y * rs;
+  const float rd = __frcp_rn(fmaf(ar, ar, ai * ai)) * rs;
+  return make_float2(ar * rd, -ai * rd);
+}
+
+__device__ __forceinline__ float4 cfms2(float4 w, float2 l, float4 q) {
+  const float2 a = cfms(make_float2(w.x, w.y), l, make_float2(q.x, q.y));
+  const float2 b = cfms(make_float2(w.z, w.w), l, make_float2(q.z, q.w));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+__global__ void __launch_bounds__(kWinMaxThreads, 1)
+panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
+                 int* __restrict__ ipiv, int* info) {
+  constexpr int kW = kNB / 4;  // pairs per thread
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int T = (int)blockDim.x, nw = T >> 5;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* Fin = reinterpret_cast<float2*>(smem_raw);    // [rpb][kRowsLd] finished pairs
+  float4* cand4 = reinterpret_cast<float4*>(Fin + (size_t)rpb * kRowsLd);  // [2][32]
+  float4* stage4 = cand4 + 2 * (kNB / 2);                // [kMaxClusterPanel][32]
+  __shared__ unsigned ckv[2], ckl[2];
+  __shared__ unsigned skv[kMaxClusterPanel], skl[kMaxClusterPanel];
+  __shared__ unsigned wkv[kWinMaxThreads / 32], wkl[kWinMaxThreads / 32];
+  __shared__ unsigned s_cl;
+  __shared__ int s_ipiv[kNB];
+  __shared__ int s_info;
+  const int lw = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int lr = threadIdx.x >> 1, h = threadIdx.x & 1;
+  const int r0 = k0 + rank * rpb;
+  const int nr = max(min(rpb, n - r0), 0);
+  const bool active = lr < nr;
+  unsigned label = active ? (unsigned)(r0 + lr) : 0xffffffffu;
+  float4 r[kW];
+#pragma unroll
+  for (int i = 0; i < kW; ++i) {
+    const int c0 = 4 * i + 2 * h;
+    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+    if (active && c0 < nb) a = A[(size_t)(k0 + c0) * lda + label];
+    if (active && c0 + 1 < nb) b = A[(size_t)(k0 + c0 + 1) * lda + label];
+    r[i] = make_float4(a.x, a.y, b.x, b.y);
+  }
+  if (threadIdx.x == 0) s_info = 0;
+  __syncthreads();
+  cl.sync();  // every CTA of the cluster is running before any DSMEM access
+  for (int b = 0; 4 * b < nb; ++b) {
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      const int c = 4 * b + cc;
+      if (c < nb) {
+        const int hc = cc >> 1;         // the thread of a row holding column c (static)
+        const bool hi = (cc & 1) != 0;  // static
+        const unsigned kc = (unsigned)(k0 + c);
+        const int par = c & 1;
+        // 1. warp and CTA candidates
+        const float2 vv = hi ? make_float2(r[0].z, r[0].w) : make_float2(r[0].x, r[0].y);
+        const float a = cabs1(vv);
+        const unsigned vb =
+            (active && h == hc && label >= kc && a >= 0.f) ? __float_as_uint(a) + 1u : 0u;
+        unsigned m = __reduce_max_sync(0xffffffffu, vb);
+        unsigned lab = __reduce_min_sync(0xffffffffu, (vb == m && m) ? label : 0xffffffffu);
+        if (ln == 0) {
+          wkv[lw] = m;
+          wkl[lw] = lab;
+        }
+        __syncthreads();
+        if (lw == 0) {
+          const unsigned wv = ln < nw ? wkv[ln] : 0u;
+          const unsigned wl = ln < nw ? wkl[ln] : 0xffffffffu;
+          m = __reduce_max_sync(0xffffffffu, wv);
+          lab = __reduce_min_sync(0xffffffffu, (wv == m && m) ? wl : 0xffffffffu);
+          if (ln == 0) {
+            s_cl = m ? lab : 0xfffffffeu;
+            ckv[par] = m;
+            ckl[par] = lab;
+          }
+        }
+        __syncthreads();
+        if (label == s_cl) {  // this row is the CTA candidate: stage pairs >= c/2
+          float4* dst = cand4 + par * (kNB / 2) + 2 * b + h;
+#pragma unroll
+          for (int i = 0; i < kW; ++i)
+            if (i < kW - b && (i > 0 || h >= hc)) dst[2 * i] = r[i];
+        }
+        // 2. every CTA's candidate visible
+        cl.sync();
+        // 3. pull all keys and staged rows: loads first, then stores, so
+        //    that a thread's DSMEM loads (up to four ranks) are in flight at once
+        for (int q0 = 0; q0 < C; q0 += 4 * nw) {
+          constexpr int kPer = 4;
+          const int j = ln;  // absolute pair index
+          float4 t4[kPer];
+          unsigned tv[kPer], tl[kPer];
+#pragma unroll
+          for (int u = 0; u < kPer; ++u) {
+            const int q = q0 + lw + u * nw;
+            if (q < C) {
+              if (j >= (c >> 1)) t4[u] = cl.map_shared_rank(cand4, q)[par * (kNB / 2) + j];
+              if (j == 0) {
+                tv[u] = *cl.map_shared_rank(&ckv[par], q);
+                tl[u] = *cl.map_shared_rank(&ckl[par], q);
+              }
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kPer; ++u) {
+            const int q = q0 + lw + u * nw;
+            if (q < C) {
+              if (j >= (c >> 1)) stage4[q * (kNB / 2) + j] = t4[u];
+              if (j == 0) {
+                skv[q] = tv[u];
+                skl[q] = tl[u];
+              }
+            }
+          }
+        }
+        __syncthreads();
+        // 4. the pivot, from the local keys (every warp)
+        const unsigned kv = ln < C ? skv[ln] : 0u;
+        const unsigned kl = ln < C ? skl[ln] : 0xffffffffu;
+        const unsigned bm = __reduce_max_sync(0xffffffffu, kv);
+        const unsigned p = __reduce_min_sync(0xffffffffu, (kv == bm && bm) ? kl : 0xffffffffu);
+        const bool zero = bm <= 1u || p < kc || p >= (unsigned)n;  // bm == 1: |pivot| = 0
+        if (threadIdx.x == 0) {
+          s_ipiv[c] = zero ? (int)kc : (int)p;
+          if (zero && s_info == 0) s_info = (int)kc + 1;
+        }
+        // the row's column-c value, from the thread holding it
+        const float2 v = make_float2(__shfl_sync(0xffffffffu, vv.x, (ln & ~1) | hc),
+                                     __shfl_sync(0xffffffffu, vv.y, (ln & ~1) | hc));
+        if (!zero) {
+          const int q = __ffs(__ballot_sync(0xffffffffu, kv == bm && kl == p)) - 1;
+          const float4* pr = stage4 + q * (kNB / 2) + 2 * b + h;  // pr[2i]: this thread's pair i
+          if (label == p)
+            label = kc;
+          else if (label == kc)
+            label = p;
+          if (active && label > kc) {
+            const float4 pc = stage4[q * (kNB / 2) + (c >> 1)];
+            const float2 piv = hi ? make_float2(pc.z, pc.w) : make_float2(pc.x, pc.y);
+            const float2 l = cmul(v, crcp_fast(piv));
+            if (h == hc) {  // the pair holding column c
+              if (hi) {
+                r[0].z = l.x;
+                r[0].w = l.y;
+              } else {
+                const float2 u = cfms(make_float2(r[0].z, r[0].w), l, make_float2(pc.z, pc.w));
+                r[0] = make_float4(l.x, l.y, u.x, u.y);
+              }
+            } else if (h > hc) {  // pair 2b + 1, right of column c
+              r[0] = cfms2(r[0], l, pr[0]);
+            }
+#pragma unroll
+            for (int i = 1; i < kW; ++i)
+              if (i < kW - b) r[i] = cfms2(r[i], l, pr[2 * i]);
+          }
+        }
+      }
+    }
+    // block b done: pair 2b + h is final; shift the window by one
+    if (active) reinterpret_cast<float4*>(Fin + (size_t)lr * kRowsLd)[2 * b + h] = r[0];
+#pragma unroll
+    for (int i = 0; i < kW - 1; ++i) r[i] = r[i + 1];
+    r[kW - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+  if (rank == 0) {
+    for (int c = threadIdx.x; c < nb; c += T) ipiv[k0 + c] = s_ipiv[c];
+    if (threadIdx.x == 0 && s_info && *info == 0) *info = s_info;
+  }
+  __syncthreads();  // Fin complete
+  if (active) {
+    const float2* fr = Fin + (size_t)lr * kRowsLd;
+    for (int c = h; c < nb; c += 2) A[(size_t)(k0 + c) * lda + label] = fr[c];
   }
 }
 
@@ -498,11 +987,11 @@ static cudaError_t launch_cluster(K kern, int C, int threads, size_t smem, cudaS
 }
 
 constexpr int kMaxCluster = 16;
-constexpr size_t kClusterSmem = 200 * 1024;
+constexpr size_t kClusterSmem = 220 * 1024;
 
 template <typename T>
 static size_t panel_cluster_smem(int rpb) {
-  return sizeof(T) * ((size_t)rpb * kNB + kNB + rpb + 4 * kNB);
+  return sizeof(T) * PanelSmem<T>::total(rpb | 1);
 }
 
 // Row permutation of the pivots: perm[i] = the original row that ends at i.
@@ -589,6 +1078,12 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kClusterSmem);
+    cudaFuncSetAttribute(panel_win_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(panel_win_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)panel_win_smem(kWinMaxRows));
+    cudaFuncSetAttribute(panel_rows_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(panel_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)panel_rows_smem(kRowsMaxRpb));
     if (cudaFuncSetAttribute(panel_cluster_kernel<T>,
                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
       cudaGetLastError();
@@ -605,13 +1100,57 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = std::min(kNB, n - k0);
     const int H = n - k0;
-    // cluster panel: 64 rows or more per CTA, at most 16 (8 portable) CTAs
+    // cluster panel.  complex64: about one row per thread (256 rows per
+    // CTA; the update is cheap on the FP32 pipe, fewer CTAs make the
+    // per-column barrier cheaper).  complex128: 64 rows per CTA, as many CTAs
+    // as allowed, since the rank-1 updates are bound by the FP64 pipe.  More
+    // CTAs when the rows do not fit in shared memory; at most 16 (8
+    // portable) CTAs and kPanelRPT rows per thread.
+    const int rows_target = sizeof(T) == sizeof(float2) ? kPanelThreads : 64;
     bool done = false;
-    for (int cmax : {cluster16 ? kMaxCluster : 8, 8}) {
-      const int C = std::max(1, std::min(cmax, (H + 63) / 64));
+    if (sizeof(T) == sizeof(float2)) {  // register-window panel
+      for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
+        int C = std::max(1, std::min(cmax, (H + kRowsMinRpb - 1) / kRowsMinRpb));
+        while ((H + C - 1) / C > kWinMaxRows) ++C;
+        if (C > cmax) continue;
+        const int rpb = (H + C - 1) / C;
+        const int threads = std::max(64, (2 * rpb + 31) / 32 * 32);
+        cudaError_t e = launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s,
+                                       reinterpret_cast<float2*>(A), lda, n, k0, nb, rpb,
+                                       w.ipiv, w.info);
+        if (e == cudaSuccess) {
+          done = true;
+          break;
+        }
+        cudaGetLastError();
+        if (cmax > 8) cluster16 = false;
+      }
+    }
+    if (!done && sizeof(T) == sizeof(float2)) {  // taller: shared-memory rows panel
+      for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
+        int C = std::max(1, std::min(cmax, (H + kRowsMinRpb - 1) / kRowsMinRpb));
+        while ((H + C - 1) / C > kRowsMaxRpb) ++C;
+        if (C > cmax) continue;
+        const int rpb = (H + C - 1) / C;
+        const int threads = rpb <= kRowsMaxThreads ? (rpb + 31) / 32 * 32 : kRowsMaxThreads;
+        cudaError_t e = launch_cluster(panel_rows_kernel, C, threads, panel_rows_smem(rpb), s,
+                                       reinterpret_cast<float2*>(A), lda, n, k0, nb, rpb,
+                                       w.ipiv, w.info);
+        if (e == cudaSuccess) {
+          done = true;
+          break;
+        }
+        cudaGetLastError();
+        if (cmax > 8) cluster16 = false;
+      }
+    }
+    for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
+      if (done) break;
+      int C = std::max(1, std::min(cmax, (H + rows_target - 1) / rows_target));
+      while (C < cmax && panel_cluster_smem<T>((H + C - 1) / C) > kClusterSmem) ++C;
       const int rpb = (H + C - 1) / C;
       const size_t smem = panel_cluster_smem<T>(rpb);
-      if (smem > kClusterSmem) continue;
+      if (smem > kClusterSmem || rpb > kPanelRPT * kPanelThreads) continue;
       cudaError_t e = launch_cluster(panel_cluster_kernel<T>, C, kPanelThreads, smem, s, A, lda,
                                      n, k0, nb, rpb, w.ipiv, w.info);
       if (e == cudaSuccess) {
