@@ -310,6 +310,13 @@ template <typename T>
 int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
                cudaStream_t s, long long* launches);
 
+// C -= A B for complex64 column-major operands on the tensor cores
+// (tcgen05 kind::tf32, 3xTF32 split; lu_tc.cu).  C is M x N, A M x K, B K x N.
+// Sets *status on a device-side wait timeout.
+int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
+                        const float2* B, long long ldb, int M, int N, int K, int* status,
+                        cudaStream_t s);
+
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);
 size_t residual_part_bytes(int n);

@@ -301,6 +301,7 @@ trsm_kernel(T* __restrict__ A, long long lda, int k0, int nb, int c0, int ncols)
 
 // C[M x N] -= A[M x K] B[K x N], K <= kNB, column-major operands.
 constexpr int kGB = 64;
+constexpr int kTensorMinN = 512;  // trailing size from which complex64 uses tcgen05
 template <typename T>
 __global__ void __launch_bounds__(256)
 gemm_sub_kernel(const T* __restrict__ Am, long long lda, const T* __restrict__ Bm,
@@ -1181,10 +1182,23 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     if (nc > 0) {
       trsm_kernel<T><<<(nc + 31) / 32, 256, sizeof(T) * (kNB * kNB + kNB * 32), s>>>(
           A, lda, k0, nb, c0, nc);
-      dim3 g((nc + kGB - 1) / kGB, (nc + kGB - 1) / kGB);
-      gemm_sub_kernel<T><<<g, 256, sizeof(T) * 2 * kNB * kGB, s>>>(
-          A + (size_t)k0 * lda + c0, lda, A + (size_t)c0 * lda + k0, lda,
-          A + (size_t)c0 * lda + c0, lda, nc, nc, nb);
+      bool tensor = false;
+      if constexpr (sizeof(T) == sizeof(float2)) {
+        // complex64: the tensor-core update once the trailing matrix is large
+        if (nc >= kTensorMinN) {
+          float2* Af = reinterpret_cast<float2*>(A);
+          if (launch_tc_cgemm_sub(Af + (size_t)c0 * lda + c0, lda, Af + (size_t)k0 * lda + c0, lda,
+                                  Af + (size_t)c0 * lda + k0, lda, nc, nc, nb, w.status, s))
+            return BEM2D_ERR_CUDA;
+          tensor = true;
+        }
+      }
+      if (!tensor) {
+        dim3 g((nc + kGB - 1) / kGB, (nc + kGB - 1) / kGB);
+        gemm_sub_kernel<T><<<g, 256, sizeof(T) * 2 * kNB * kGB, s>>>(
+            A + (size_t)k0 * lda + c0, lda, A + (size_t)c0 * lda + k0, lda,
+            A + (size_t)c0 * lda + c0, lda, nc, nc, nb);
+      }
       *launches += 2;
     }
   }
