@@ -301,7 +301,9 @@ trsm_kernel(T* __restrict__ A, long long lda, int k0, int nb, int c0, int ncols)
 
 // C[M x N] -= A[M x K] B[K x N], K <= kNB, column-major operands.
 constexpr int kGB = 64;
-constexpr int kTensorMinN = 512;  // trailing size from which complex64 uses tcgen05
+constexpr int kTensorMinN = 256;  // update size from which complex64 uses tcgen05
+constexpr int kOuterNB = 256;     // outer block width of the complex64 LU
+constexpr int kOuterMinN = 8192;  // smaller matrices: the extra launches cost more
 template <typename T>
 __global__ void __launch_bounds__(256)
 gemm_sub_kernel(const T* __restrict__ Am, long long lda, const T* __restrict__ Bm,
@@ -1063,6 +1065,42 @@ size_t lu_aux_bytes(int n, size_t elem) {
   return sizeof(int) * (size_t)n + 2 * nk * kNB * kNB * elem + 256;
 }
 
+// C -= Am Bm (M x N, inner dimension K; all three column-major with leading
+// dimension ld inside the matrix being factored).  complex64 updates of at
+// least kTensorMinN rows and columns run on the tensor cores, the rest on the
+// CUDA cores in slices of K = 64.
+template <typename T>
+static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N, int K,
+                      const LuWork& w, cudaStream_t s, long long* launches) {
+  if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
+  if constexpr (sizeof(T) == sizeof(float2)) {
+    if (M >= kTensorMinN && N >= kTensorMinN) {
+      ++*launches;
+      return launch_tc_cgemm_sub(reinterpret_cast<float2*>(C), ld,
+                                 reinterpret_cast<const float2*>(Am), ld,
+                                 reinterpret_cast<const float2*>(Bm), ld, M, N, K, w.status, s)
+                 ? BEM2D_ERR_CUDA
+                 : BEM2D_OK;
+    }
+  }
+  dim3 g((M + kGB - 1) / kGB, (N + kGB - 1) / kGB);
+  for (int k = 0; k < K; k += kNB) {
+    gemm_sub_kernel<T><<<g, 256, sizeof(T) * 2 * kNB * kGB, s>>>(
+        Am + (size_t)k * ld, ld, Bm + k, ld, C, ld, M, N, std::min(kNB, K - k));
+    ++*launches;
+  }
+  return BEM2D_OK;
+}
+
+template <typename T>
+static void trsm_rows(T* A, long long lda, int k0, int nb, int c0, int nc, cudaStream_t s,
+                      long long* launches) {
+  if (nc <= 0) return;
+  trsm_kernel<T><<<(nc + 31) / 32, 256, sizeof(T) * (kNB * kNB + kNB * 32), s>>>(A, lda, k0, nb,
+                                                                                c0, nc);
+  ++*launches;
+}
+
 template <typename T>
 int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
               long long* launches) {
@@ -1098,7 +1136,15 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
                          (int)(sizeof(T) * kNB * kNB));
     cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
   });
-  for (int k0 = 0; k0 < n; k0 += kNB) {
+  // complex64 matrices are factored in outer blocks of kOuterNB columns:
+  // inside a block each 64-column panel updates only the block's columns;
+  // the columns right of the block receive one rank-kOuterNB update (K =
+  // kOuterNB on the tensor cores), which reads and writes the trailing
+  // matrix once per block instead of once per panel.
+  const int outer = (sizeof(T) == sizeof(float2) && n >= kOuterMinN) ? kOuterNB : kNB;
+  for (int K0 = 0; K0 < n; K0 += outer) {
+  const int bend = std::min(n, K0 + outer);
+  for (int k0 = K0; k0 < bend; k0 += kNB) {
     const int nb = std::min(kNB, n - k0);
     const int H = n - k0;
     // cluster panel.  complex64: about one row per thread (256 rows per
@@ -1178,29 +1224,32 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
       laswp_kernel<T><<<(n - nb + 127) / 128, 128, 0, s>>>(A, lda, n, w.ipiv, k0, nb);
       ++*launches;
     }
-    const int c0 = k0 + nb, nc = n - c0;
-    if (nc > 0) {
-      trsm_kernel<T><<<(nc + 31) / 32, 256, sizeof(T) * (kNB * kNB + kNB * 32), s>>>(
-          A, lda, k0, nb, c0, nc);
-      bool tensor = false;
-      if constexpr (sizeof(T) == sizeof(float2)) {
-        // complex64: the tensor-core update once the trailing matrix is large
-        if (nc >= kTensorMinN) {
-          float2* Af = reinterpret_cast<float2*>(A);
-          if (launch_tc_cgemm_sub(Af + (size_t)c0 * lda + c0, lda, Af + (size_t)k0 * lda + c0, lda,
-                                  Af + (size_t)c0 * lda + k0, lda, nc, nc, nb, w.status, s))
-            return BEM2D_ERR_CUDA;
-          tensor = true;
-        }
-      }
-      if (!tensor) {
-        dim3 g((nc + kGB - 1) / kGB, (nc + kGB - 1) / kGB);
-        gemm_sub_kernel<T><<<g, 256, sizeof(T) * 2 * kNB * kGB, s>>>(
-            A + (size_t)k0 * lda + c0, lda, A + (size_t)c0 * lda + k0, lda,
-            A + (size_t)c0 * lda + c0, lda, nc, nc, nb);
-      }
-      *launches += 2;
+    // columns of the block right of this panel
+    const int c0 = k0 + nb, ncb = bend - c0;
+    if (ncb > 0) {
+      trsm_rows(A, lda, k0, nb, c0, ncb, s, launches);
+      int rc = update_sub(A + (size_t)c0 * lda + c0, A + (size_t)k0 * lda + c0,
+                          A + (size_t)c0 * lda + k0, lda, n - c0, ncb, nb, w, s, launches);
+      if (rc) return rc;
     }
+  }
+  // columns right of the block: U12 = L11^{-1} A12 block row by block row,
+  // then A22 -= L21 U12 with K = the block width
+  const int nc = n - bend;
+  if (nc > 0) {
+    for (int j0 = K0; j0 < bend; j0 += kNB) {
+      trsm_rows(A, lda, j0, kNB, bend, nc, s, launches);
+      const int r1 = j0 + kNB;
+      if (r1 < bend) {
+        int rc = update_sub(A + (size_t)bend * lda + r1, A + (size_t)j0 * lda + r1,
+                            A + (size_t)bend * lda + j0, lda, bend - r1, nc, kNB, w, s, launches);
+        if (rc) return rc;
+      }
+    }
+    int rc = update_sub(A + (size_t)bend * lda + bend, A + (size_t)K0 * lda + bend,
+                        A + (size_t)bend * lda + K0, lda, nc, nc, bend - K0, w, s, launches);
+    if (rc) return rc;
+  }
   }
   // solve aids: permutation and diagonal-block inverses
   const int nk = (n + kNB - 1) / kNB;
