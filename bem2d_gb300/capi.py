@@ -102,12 +102,20 @@ def load():
         lib.bem2d_change_basis.argtypes = [vp, i32, vp, i64, vp, i64, vp, i32, vp, i64]
         lib.bem2d_l2_norm_cond.argtypes = [vp, i32, vp, i64, d, ctypes.POINTER(d),
                                            ctypes.POINTER(d)]
-        lib.bem2d_num_range.argtypes = [vp, i32, vp, i64, i32, vp, d, vp]
+        lib.bem2d_num_range.argtypes = [vp, i32, vp, i64, i32, vp, d, i32, vp]
         lib.bem2d_eval_kernel.argtypes = [vp, vp, vp, i32, d, d, d, vp, i32, vp, vp]
         lib.bem2d_ctx_enable_timers.argtypes = [vp, i32]
         lib.bem2d_ctx_timer.argtypes = [vp, i32, ctypes.POINTER(d), ctypes.POINTER(i64)]
         _LIB = lib
     return _LIB
+
+
+def _ld(a, n):
+    """Leading dimension of a column-major matrix: numpy (Fortran order) or a
+    torch tensor (column-major view, or row-major storage of the transpose)."""
+    if hasattr(a, "stride"):
+        return a.stride(1) if a.stride(0) == 1 else a.stride(0)
+    return n
 
 
 def _ptr(a):
@@ -202,17 +210,21 @@ class Context:
         return out
 
     def discrete_kernel_mixed(self, g, kernel="combined", k=10.0, eta=None, q=(3, 5, 0.15),
-                              alpha=1.0, beta=0.0):
-        """Mixed-precision assembly: (complex128, complex64) host matrices."""
+                              alpha=1.0, beta=0.0, out=None, out32=None):
+        """Mixed-precision assembly: (complex128, complex64) matrices (host
+        numpy by default, or the given torch CUDA tensors)."""
         gh = _GeomHold(g)
         n = gh.n
-        out = np.zeros((n, n), dtype=np.complex128, order="F")
-        out32 = np.zeros((n, n), dtype=np.complex64, order="F")
+        if out is None:
+            out = np.zeros((n, n), dtype=np.complex128, order="F")
+        if out32 is None:
+            out32 = np.zeros((n, n), dtype=np.complex64, order="F")
         eta = float(k) if eta is None else float(eta)
         qq = quad(q)
         self._check(self.lib.bem2d_discrete_kernel_mixed(
             self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
-            eta, float(alpha), float(beta), _ptr(out), n, _ptr(out32), n))
+            eta, float(alpha), float(beta), _ptr(out), _ld(out, n), _ptr(out32),
+            _ld(out32, n)))
         return out, out32
 
     def eval_ident(self, g, q=(3, 5, 0.15), out=None):
@@ -222,7 +234,7 @@ class Context:
             out = np.zeros((n, n), dtype=np.complex128, order="F")
         qq = quad(q)
         self._check(self.lib.bem2d_eval_ident(self.h, ctypes.byref(gh.c), ctypes.byref(qq),
-                                              _ptr(out), n))
+                                              _ptr(out), _ld(out, n)))
         return out
 
     def rhs(self, g, k, direction, eta=None, q=(3, 5, 0.15), fun="combinedplanewave",
@@ -273,34 +285,40 @@ class Context:
         return out
 
     # -- dense operators ---------------------------------------------------
-    def change_basis(self, K, M, bstart):
+    def change_basis(self, K, M, bstart, out=None):
         """U^{-H} K U^{-1} with M = U^H U block diagonal (blocks at bstart)."""
         n = K.shape[0]
-        K = np.asfortranarray(K, dtype=np.complex128)
-        M = np.asfortranarray(M, dtype=np.complex128)
+        if isinstance(K, np.ndarray):
+            K = np.asfortranarray(K, dtype=np.complex128)
+        if isinstance(M, np.ndarray):
+            M = np.asfortranarray(M, dtype=np.complex128)
         bs = np.ascontiguousarray(bstart, dtype=np.int32)
-        out = np.zeros((n, n), dtype=np.complex128, order="F")
-        self._check(self.lib.bem2d_change_basis(self.h, n, _ptr(K), n, _ptr(M), n, _ptr(bs),
-                                                len(bs) - 1, _ptr(out), n))
+        if out is None:
+            out = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._check(self.lib.bem2d_change_basis(self.h, n, _ptr(K), _ld(K, n), _ptr(M),
+                                                _ld(M, n), _ptr(bs), len(bs) - 1, _ptr(out),
+                                                _ld(out, n)))
         return out
 
     def norm_cond(self, A, tol=0.0):
         """(sigma_max, sigma_max / sigma_min) of A."""
         n = A.shape[0]
-        A = np.asfortranarray(A, dtype=np.complex128)
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
         nrm, cond = ctypes.c_double(), ctypes.c_double()
-        self._check(self.lib.bem2d_l2_norm_cond(self.h, n, _ptr(A), n, float(tol),
+        self._check(self.lib.bem2d_l2_norm_cond(self.h, n, _ptr(A), _ld(A, n), float(tol),
                                                 ctypes.byref(nrm), ctypes.byref(cond)))
         return nrm.value, cond.value
 
-    def num_range_lmax(self, A, thetas, tol=0.0):
+    def num_range_lmax(self, A, thetas, tol=0.0, precision="fp64"):
         """lambda_max of (e^{i th} A + e^{-i th} A^H)/2 for each angle."""
         n = A.shape[0]
-        A = np.asfortranarray(A, dtype=np.complex128)
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
         th = np.ascontiguousarray(thetas, dtype=np.float64)
         out = np.zeros(len(th))
-        self._check(self.lib.bem2d_num_range(self.h, n, _ptr(A), n, len(th), _ptr(th),
-                                             float(tol), _ptr(out)))
+        self._check(self.lib.bem2d_num_range(self.h, n, _ptr(A), _ld(A, n), len(th), _ptr(th),
+                                             float(tol), PREC[precision], _ptr(out)))
         return out
 
     def potential(self, g, coeffs, points, kernel="single", k=10.0, eta=0.0, q=(3, 5, 0.15)):

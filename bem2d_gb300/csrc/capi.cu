@@ -926,6 +926,137 @@ static std::vector<std::complex<double>> start_vector(int n) {
   return v;
 }
 
+template <typename T>
+struct LzNames;
+template <>
+struct LzNames<double2> {
+  static constexpr const char* Q = "nr_Q";
+  static constexpr const char* Y1 = "nr_Y1";
+  static constexpr const char* Y2 = "nr_Y2";
+  static constexpr const char* W = "nr_W";
+  static constexpr const char* h = "nr_h";
+  static constexpr const char* sc = "nr_sc";
+};
+template <>
+struct LzNames<float2> {
+  static constexpr const char* Q = "nr32_Q";
+  static constexpr const char* Y1 = "nr32_Y1";
+  static constexpr const char* Y2 = "nr32_Y2";
+  static constexpr const char* W = "nr32_W";
+  static constexpr const char* h = "nr32_h";
+  static constexpr const char* sc = "nr32_sc";
+};
+
+// Batched Lanczos (full reorthogonalisation, two Gram-Schmidt passes) for
+// lambda_max of H_a = (e^{i th_a} A + e^{-i th_a} A^H) / 2, every angle at
+// once: one product with A and one with A^H per step for all angles.  An
+// angle has converged when its lambda_max moved by at most tol (relative)
+// in two consecutive steps.  start (complex128, n per angle): start vectors
+// (normalised here); else the deterministic start vector.  ritz (optional):
+// the Ritz vector of lambda_max per angle on return.
+template <typename T>
+static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int nang,
+                            const double* dth, double tol, int mmax, const double2* start,
+                            double* lam_out, T* ritz, bool full_reorth = true) {
+  int rc = 0;
+  const long long qs = (long long)n * (mmax + 1);  // per-angle basis stride
+  T* Q = static_cast<T*>(ws(c, LzNames<T>::Q, sizeof(T) * (size_t)qs * nang, &rc));
+  T* Y1 = static_cast<T*>(ws(c, LzNames<T>::Y1, sizeof(T) * (size_t)n * nang, &rc));
+  T* Y2 = static_cast<T*>(ws(c, LzNames<T>::Y2, sizeof(T) * (size_t)n * nang, &rc));
+  T* W = static_cast<T*>(ws(c, LzNames<T>::W, sizeof(T) * (size_t)n * nang, &rc));
+  T* h = static_cast<T*>(ws(c, LzNames<T>::h, sizeof(T) * (size_t)(mmax + 2) * nang, &rc));
+  double* sc = static_cast<double*>(ws(c, LzNames<T>::sc, sizeof(double) * 2 * nang + 64, &rc));
+  if (!Q || !Y1 || !Y2 || !W || !h || !sc) return rc;
+  std::vector<double> nn(nang), inv(nang);
+  if (start) {
+    if constexpr (sizeof(T) == sizeof(double2)) {
+      launch_batched_norm2(n, start, n, sc, nang, c->stream);
+      CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * nang, cudaMemcpyDeviceToHost, c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      for (int a = 0; a < nang; ++a) inv[a] = nn[a] > 0 ? 1.0 / std::sqrt(nn[a]) : 0.0;
+      CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
+      launch_batched_scale(n, start, n, sc, Q, qs, nang, c->stream);
+      c->launches += 2;
+    } else {
+      return fail(c, BEM2D_ERR_ARG, "start vectors are complex128");
+    }
+  } else {
+    const std::vector<std::complex<double>> v0 = start_vector(n);
+    std::vector<T> v0t(n);
+    for (int r = 0; r < n; ++r) v0t[r] = {(decltype(v0t[r].x))v0[r].real(), (decltype(v0t[r].x))v0[r].imag()};
+    for (int a = 0; a < nang; ++a)
+      CUDA_TRY(c, cudaMemcpyAsync(Q + (size_t)a * qs, v0t.data(), sizeof(T) * n,
+                                  cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // v0t is released below
+  }
+  std::vector<std::vector<double>> al(nang), be(nang);
+  std::vector<double> lam(nang, 0.0), prev(nang, NAN);
+  std::vector<int> stable(nang, 0);
+  std::vector<T> hh((size_t)(mmax + 2) * nang);
+  const int ldh = mmax + 2;
+  int steps = 0;
+  for (int j = 0; j < mmax; ++j) {
+    const T* Qj = Q + (size_t)j * n;
+    launch_zgemm(false, dA, la, n, Qj, qs, nang, Y1, n, c->stream);
+    launch_zgemm(true, dA, la, n, Qj, qs, nang, Y2, n, c->stream);
+    launch_herm_combine(n, Y1, Y2, n, dth, W, n, nang, c->stream);
+    // Gram-Schmidt (two passes) against q_0..q_j, or, without full
+    // reorthogonalisation, against q_{j-1}, q_j only (the three-term
+    // recurrence: the extreme Ritz value converges all the same)
+    const int w0 = full_reorth ? 0 : std::max(0, j - 1), nw = j + 1 - w0;
+    const T* Qw = Q + (size_t)w0 * n;
+    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(hh.data(), h, sizeof(T) * (size_t)ldh * nang, cudaMemcpyDeviceToHost, c->stream));
+    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
+    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
+    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
+    launch_batched_norm2(n, W, n, sc, nang, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * nang, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    c->launches += 8;
+    CHECK_LAUNCH(c);
+    steps = j + 1;
+    bool all = true;
+    for (int a = 0; a < nang; ++a) {
+      al[a].push_back(hh[(size_t)a * ldh + (j - w0)].x);
+      const double b = std::sqrt(nn[a]);
+      inv[a] = b > 1e-300 ? 1.0 / b : 0.0;
+      lam[a] = tridiag_lmax(al[a], be[a]);
+      const double scale = std::max(std::fabs(lam[a]), 1e-300);
+      if (std::fabs(lam[a] - prev[a]) <= tol * scale || b <= 1e-300) {
+        ++stable[a];
+      } else {
+        stable[a] = 0;
+      }
+      prev[a] = lam[a];
+      be[a].push_back(b);
+      if (stable[a] < 2 || j < 3) all = false;
+    }
+    if (all) break;
+    // q_{j+1} = w / beta
+    CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
+    launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, nang, c->stream);
+    ++c->launches;
+  }
+  for (int a = 0; a < nang; ++a) lam_out[a] = lam[a];
+  if (ritz) {
+    // u_a = Q_a s_a, s_a the eigenvector of T_a for lambda_max: W = 0,
+    // W -= Q (-s)
+    for (int a = 0; a < nang; ++a) {
+      std::vector<double> e(be[a].begin(), be[a].begin() + (steps - 1));
+      const std::vector<double> sv = tridiag_eigenvector(al[a], e, lam[a]);
+      for (int i = 0; i < steps; ++i)
+        hh[(size_t)a * ldh + i] = {(decltype(hh[0].x))(-sv[i]), (decltype(hh[0].x))0};
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(h, hh.data(), sizeof(T) * (size_t)ldh * nang, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemsetAsync(ritz, 0, sizeof(T) * (size_t)n * nang, c->stream));
+    launch_batched_sub(Q, qs, n, steps, ritz, n, h, ldh, nang, c->stream);
+    ++c->launches;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // hh is host memory
+  }
+  return BEM2D_OK;
+}
+
 // Largest singular value of an operator given y = op(x) and y = op^H(x), by
 // Golub-Kahan-Lanczos bidiagonalisation with two-pass Gram-Schmidt
 // reorthogonalisation of both bases.
@@ -1170,80 +1301,41 @@ int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double t
 }
 
 int bem2d_num_range(bem2d_ctx* c, int n, const void* A, int64_t lda, int nang,
-                    const double* theta, double tol, double* lmax) {
+                    const double* theta, double tol, int precision, double* lmax) {
   if (!c) return BEM2D_ERR_ARG;
   if (n < 1 || !A || nang < 1 || !theta || !lmax || lda < n)
     return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (precision != BEM2D_PREC_FP64 && precision != BEM2D_PREC_MIXED)
+    return fail(c, BEM2D_ERR_ARG, "unknown precision %d", precision);
   if (!(tol > 0)) tol = 1e-13;
   cudaSetDevice(c->device);
   int rc = 0;
   long long la = 0;
   const double2* dA = dev_in(c, A, n, n, lda, "nr_A", &la, &rc);
   if (!dA) return rc;
-  const int mmax = std::min(n, 160);
-  const long long qs = (long long)n * (mmax + 1);  // per-angle basis stride
-  double2* Q = static_cast<double2*>(ws(c, "nr_Q", sizeof(double2) * (size_t)qs * nang, &rc));
-  double2* Y1 = static_cast<double2*>(ws(c, "nr_Y1", sizeof(double2) * (size_t)n * nang, &rc));
-  double2* Y2 = static_cast<double2*>(ws(c, "nr_Y2", sizeof(double2) * (size_t)n * nang, &rc));
-  double2* W = static_cast<double2*>(ws(c, "nr_W", sizeof(double2) * (size_t)n * nang, &rc));
-  double2* h = static_cast<double2*>(ws(c, "nr_h", sizeof(double2) * (size_t)(mmax + 2) * nang, &rc));
-  double* sc = static_cast<double*>(ws(c, "nr_sc", sizeof(double) * 2 * nang + 64, &rc));
-  if (!Q || !Y1 || !Y2 || !W || !h || !sc) return rc;
-  double* dth = sc + nang;
+  double* dth = static_cast<double*>(ws(c, "nr_th", sizeof(double) * nang, &rc));
+  if (!dth) return rc;
   CUDA_TRY(c, cudaMemcpyAsync(dth, theta, sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
-  const std::vector<std::complex<double>> v0 = start_vector(n);
-  for (int a = 0; a < nang; ++a)
-    CUDA_TRY(c, cudaMemcpyAsync(Q + (size_t)a * qs, v0.data(), sizeof(double2) * n,
-                                cudaMemcpyHostToDevice, c->stream));
-  std::vector<std::vector<double>> al(nang), be(nang);
-  std::vector<double> lam(nang, 0.0), prev(nang, NAN);
-  std::vector<int> stable(nang, 0);
-  std::vector<std::complex<double>> hh((size_t)(mmax + 2) * nang);
-  std::vector<double> nn(nang), inv(nang);
-  const int ldh = mmax + 2;
-  for (int j = 0; j < mmax; ++j) {
-    const double2* Qj = Q + (size_t)j * n;
-    launch_zgemm(false, dA, la, n, Qj, qs, nang, Y1, n, c->stream);
-    launch_zgemm(true, dA, la, n, Qj, qs, nang, Y2, n, c->stream);
-    launch_herm_combine(n, Y1, Y2, n, dth, W, n, nang, c->stream);
-    // two Gram-Schmidt passes against q_0..q_j; alpha_j = Re(<q_j, H q_j>)
-    launch_batched_dots(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(hh.data(), h, sizeof(double2) * (size_t)ldh * nang, cudaMemcpyDeviceToHost, c->stream));
-    launch_batched_sub(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
-    launch_batched_dots(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
-    launch_batched_sub(Q, qs, n, j + 1, W, n, h, ldh, nang, c->stream);
-    launch_batched_norm2(n, W, n, sc, nang, c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * nang, cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    c->launches += 8;
-    CHECK_LAUNCH(c);
-    bool all = true;
-    for (int a = 0; a < nang; ++a) {
-      al[a].push_back(hh[(size_t)a * ldh + j].real());
-      const double b = std::sqrt(nn[a]);
-      inv[a] = b > 1e-300 ? 1.0 / b : 0.0;
-      std::vector<double> d(al[a]), e(be[a]), ev;
-      e.resize(d.size(), 0.0);
-      if (!tridiag_eigenvalues(d, e, &ev)) return fail(c, BEM2D_ERR_NOCONV, "tridiagonal QL failed");
-      lam[a] = *std::max_element(ev.begin(), ev.end());
-      const double scale = std::max(std::fabs(lam[a]), 1e-300);
-      if (std::fabs(lam[a] - prev[a]) <= tol * scale || b <= 1e-300) {
-        ++stable[a];
-      } else {
-        stable[a] = 0;
-      }
-      prev[a] = lam[a];
-      be[a].push_back(b);
-      if (stable[a] < 2 || j < 3) all = false;
-    }
-    if (all) break;
-    // q_{j+1} = w / beta
-    CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
-    launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, nang, c->stream);
-    ++c->launches;
-  }
-  for (int a = 0; a < nang; ++a) lmax[a] = lam[a];
-  return BEM2D_OK;
+  const int mmax = std::min(n, 160);
+  if (precision == BEM2D_PREC_FP64)
+    return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, nullptr, lmax, nullptr);
+  // mixed: complex64 Lanczos (three-term recurrence, cold start: every
+  // angle's largest eigenvalue is found from its own Krylov space) to
+  // ~1e-6, then complex128 Lanczos (full reorthogonalisation) started from
+  // the complex64 Ritz vectors, all angles in one batch
+  float2* A32 = static_cast<float2*>(ws(c, "nr_A32", sizeof(float2) * (size_t)n * n, &rc));
+  float2* R32 = static_cast<float2*>(ws(c, "nr_R32", sizeof(float2) * (size_t)n * nang, &rc));
+  double2* S64 = static_cast<double2*>(ws(c, "nr_S64", sizeof(double2) * (size_t)n * nang, &rc));
+  if (!A32 || !R32 || !S64) return rc;
+  launch_to_c64(dA, la, A32, n, n, n, c->stream);
+  ++c->launches;
+  std::vector<double> l32(nang);
+  if ((rc = numrange_lanczos<float2>(c, n, A32, n, nang, dth, 1e-6, mmax, nullptr, l32.data(), R32,
+                                     false)))
+    return rc;
+  launch_widen(n, R32, n, S64, n, nang, c->stream);
+  ++c->launches;
+  return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, S64, lmax, nullptr);
 }
 
 int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,

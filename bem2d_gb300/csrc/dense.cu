@@ -141,28 +141,30 @@ void launch_mvh(const double2* A, long long lda, int n, const double2* x, double
 
 // ---- matrix-matrix products: C (n x m) = op(A) (n x n) B (n x m) -------------
 // op = A or A^H; 64 x 64 output tiles, K in chunks of 16, 4 x 4 per thread.
-template <bool HERM>
+// T = double2 (complex128) or float2 (complex64).
+template <typename T, bool HERM>
 __global__ void __launch_bounds__(256)
-zgemm_kernel(const double2* __restrict__ A, long long lda, int n, const double2* __restrict__ B,
-             long long ldb, int m, double2* __restrict__ C, long long ldc) {
-  __shared__ double2 As[16][64 + 1];
-  __shared__ double2 Bs[16][64 + 1];
+zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict__ B,
+             long long ldb, int m, T* __restrict__ C, long long ldc) {
+  __shared__ T As[16][64 + 1];
+  __shared__ T Bs[16][64 + 1];
+  const T zero = CTraits<T>::make(0, 0);
   const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double2 acc[4][4];
+  T acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = make_double2(0, 0);
+    for (int b = 0; b < 4; ++b) acc[a][b] = zero;
   for (int k0 = 0; k0 < n; k0 += 16) {
     for (int v = threadIdx.x; v < 16 * 64; v += 256) {
       const int kk = v / 64, ii = v - kk * 64;
       const int i = i0 + ii, k = k0 + kk;
-      double2 a = make_double2(0, 0);
+      T a = zero;
       if (i < n && k < n) {
         if (HERM) {
-          const double2 t = A[(size_t)i * lda + k];  // (A^H)_{ik} = conj(A_{ki})
-          a = make_double2(t.x, -t.y);
+          const T t = A[(size_t)i * lda + k];  // (A^H)_{ik} = conj(A_{ki})
+          a = CTraits<T>::make(t.x, -t.y);
         } else {
           a = A[(size_t)k * lda + i];
         }
@@ -172,12 +174,12 @@ zgemm_kernel(const double2* __restrict__ A, long long lda, int n, const double2*
     for (int v = threadIdx.x; v < 16 * 64; v += 256) {
       const int jj = v / 16, kk = v - jj * 16;
       const int j = j0 + jj, k = k0 + kk;
-      Bs[kk][jj] = (j < m && k < n) ? B[(size_t)j * ldb + k] : make_double2(0, 0);
+      Bs[kk][jj] = (j < m && k < n) ? B[(size_t)j * ldb + k] : zero;
     }
     __syncthreads();
 #pragma unroll 4
     for (int kk = 0; kk < 16; ++kk) {
-      double2 av[4], bv[4];
+      T av[4], bv[4];
 #pragma unroll
       for (int a = 0; a < 4; ++a) av[a] = As[kk][tx + 16 * a];
 #pragma unroll
@@ -201,29 +203,40 @@ zgemm_kernel(const double2* __restrict__ A, long long lda, int n, const double2*
   }
 }
 
-void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
-                  long long ldb, int m, double2* C, long long ldc, cudaStream_t s) {
+template <typename T>
+static void zgemm_t(bool herm, const T* A, long long lda, int n, const T* B, long long ldb, int m,
+                    T* C, long long ldc, cudaStream_t s) {
   dim3 g((n + 63) / 64, (m + 63) / 64);
   if (herm)
-    zgemm_kernel<true><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
+    zgemm_kernel<T, true><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
   else
-    zgemm_kernel<false><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
+    zgemm_kernel<T, false><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
+}
+void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
+                  long long ldb, int m, double2* C, long long ldc, cudaStream_t s) {
+  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, s);
+}
+void launch_zgemm(bool herm, const float2* A, long long lda, int n, const float2* B,
+                  long long ldb, int m, float2* C, long long ldc, cudaStream_t s) {
+  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, s);
 }
 
 // ---- batched vector kernels (columns of n x m blocks) ----------------------
-// h[c * ldh + i] = sum_r conj(Q[c][r, i]) w[c][r] for i < j (Q[c] = Q + c*qstride)
-__global__ void batched_dots_kernel(const double2* __restrict__ Q, long long qstride, int n,
-                                    int j, const double2* __restrict__ W, long long wstride,
-                                    double2* __restrict__ h, int ldh) {
+// h[c * ldh + i] = sum_r conj(Q[c][r, i]) w[c][r] for i < j (Q[c] = Q + c*qstride);
+// sums in double for both element types
+template <typename T>
+__global__ void batched_dots_kernel(const T* __restrict__ Q, long long qstride, int n, int j,
+                                    const T* __restrict__ W, long long wstride,
+                                    T* __restrict__ h, int ldh) {
   const int c = blockIdx.y, i = blockIdx.x;
   if (i >= j) return;
-  const double2* q = Q + (size_t)c * qstride + (size_t)i * n;
-  const double2* w = W + (size_t)c * wstride;
+  const T* q = Q + (size_t)c * qstride + (size_t)i * n;
+  const T* w = W + (size_t)c * wstride;
   double sr = 0, si = 0;
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    const double2 a = q[r], b = w[r];
-    sr += a.x * b.x + a.y * b.y;
-    si += a.x * b.y - a.y * b.x;
+    const T a = q[r], b = w[r];
+    sr += (double)a.x * b.x + (double)a.y * b.y;
+    si += (double)a.x * b.y - (double)a.y * b.x;
   }
   __shared__ double red[2][256];
   red[0][threadIdx.x] = sr;
@@ -236,29 +249,32 @@ __global__ void batched_dots_kernel(const double2* __restrict__ Q, long long qst
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) h[(size_t)c * ldh + i] = make_double2(red[0][0], red[1][0]);
+  if (threadIdx.x == 0) h[(size_t)c * ldh + i] = CTraits<T>::make(red[0][0], red[1][0]);
 }
 
 // w[c] -= Q[c][:, :j] h[c]
-__global__ void batched_sub_kernel(const double2* __restrict__ Q, long long qstride, int n, int j,
-                                   double2* __restrict__ W, long long wstride,
-                                   const double2* __restrict__ h, int ldh) {
+template <typename T>
+__global__ void batched_sub_kernel(const T* __restrict__ Q, long long qstride, int n, int j,
+                                   T* __restrict__ W, long long wstride, const T* __restrict__ h,
+                                   int ldh) {
   const int c = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  const double2* q = Q + (size_t)c * qstride + r;
-  double2 acc = W[(size_t)c * wstride + r];
+  const T* q = Q + (size_t)c * qstride + r;
+  T acc = W[(size_t)c * wstride + r];
   for (int i = 0; i < j; ++i) acc = cfms(acc, q[(size_t)i * n], h[(size_t)c * ldh + i]);
   W[(size_t)c * wstride + r] = acc;
 }
 
 // norms[c] = ||w[c]||_2^2
-__global__ void batched_norm2_kernel(int n, const double2* __restrict__ W, long long wstride,
+template <typename T>
+__global__ void batched_norm2_kernel(int n, const T* __restrict__ W, long long wstride,
                                      double* __restrict__ out) {
   const int c = blockIdx.x;
-  const double2* w = W + (size_t)c * wstride;
+  const T* w = W + (size_t)c * wstride;
   double s = 0;
-  for (int r = threadIdx.x; r < n; r += blockDim.x) s += w[r].x * w[r].x + w[r].y * w[r].y;
+  for (int r = threadIdx.x; r < n; r += blockDim.x)
+    s += (double)w[r].x * w[r].x + (double)w[r].y * w[r].y;
   __shared__ double red[256];
   red[threadIdx.x] = s;
   __syncthreads();
@@ -270,59 +286,79 @@ __global__ void batched_norm2_kernel(int n, const double2* __restrict__ W, long 
 }
 
 // dst[c] = src[c] * scale[c]
-__global__ void batched_scale_kernel(int n, const double2* __restrict__ src, long long sstride,
-                                     const double* __restrict__ scale, double2* __restrict__ dst,
+template <typename T>
+__global__ void batched_scale_kernel(int n, const T* __restrict__ src, long long sstride,
+                                     const double* __restrict__ scale, T* __restrict__ dst,
                                      long long dstride) {
   const int c = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const double f = scale[c];
-  const double2 v = src[(size_t)c * sstride + r];
-  dst[(size_t)c * dstride + r] = make_double2(v.x * f, v.y * f);
+  const T v = src[(size_t)c * sstride + r];
+  dst[(size_t)c * dstride + r] = CTraits<T>::make(v.x * f, v.y * f);
 }
 
 // numerical range: w[c] = (e^{i th_c} Y1[c] + e^{-i th_c} Y2[c]) / 2
-__global__ void herm_combine_kernel(int n, const double2* __restrict__ Y1,
-                                    const double2* __restrict__ Y2, long long stride,
-                                    const double* __restrict__ theta, double2* __restrict__ W,
-                                    long long wstride) {
+template <typename T>
+__global__ void herm_combine_kernel(int n, const T* __restrict__ Y1, const T* __restrict__ Y2,
+                                    long long stride, const double* __restrict__ theta,
+                                    T* __restrict__ W, long long wstride) {
   const int c = blockIdx.y;
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   double s, co;
   sincos(theta[c], &s, &co);
-  const double2 a = Y1[(size_t)c * stride + r], b = Y2[(size_t)c * stride + r];
+  const T a = Y1[(size_t)c * stride + r], b = Y2[(size_t)c * stride + r];
   // (co + i s) a + (co - i s) b
-  const double re = co * (a.x + b.x) - s * (a.y - b.y);
-  const double im = co * (a.y + b.y) + s * (a.x - b.x);
-  W[(size_t)c * wstride + r] = make_double2(0.5 * re, 0.5 * im);
+  const double re = co * ((double)a.x + b.x) - s * ((double)a.y - b.y);
+  const double im = co * ((double)a.y + b.y) + s * ((double)a.x - b.x);
+  W[(size_t)c * wstride + r] = CTraits<T>::make(0.5 * re, 0.5 * im);
 }
 
-void launch_batched_dots(const double2* Q, long long qstride, int n, int j, const double2* W,
-                         long long wstride, double2* h, int ldh, int nb, cudaStream_t s) {
-  if (j <= 0) return;
-  batched_dots_kernel<<<dim3(j, nb), 256, 0, s>>>(Q, qstride, n, j, W, wstride, h, ldh);
+// dst (complex128) = src (complex64), columns of n x nb blocks
+__global__ void widen_kernel(int n, const float2* __restrict__ src, long long sstride,
+                             double2* __restrict__ dst, long long dstride) {
+  const int c = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const float2 v = src[(size_t)c * sstride + r];
+  dst[(size_t)c * dstride + r] = make_double2(v.x, v.y);
 }
-void launch_batched_sub(const double2* Q, long long qstride, int n, int j, double2* W,
-                        long long wstride, const double2* h, int ldh, int nb, cudaStream_t s) {
-  if (j <= 0) return;
-  batched_sub_kernel<<<dim3((n + 127) / 128, nb), 128, 0, s>>>(Q, qstride, n, j, W, wstride, h,
-                                                              ldh);
-}
-void launch_batched_norm2(int n, const double2* W, long long wstride, double* out, int nb,
-                          cudaStream_t s) {
-  batched_norm2_kernel<<<nb, 256, 0, s>>>(n, W, wstride, out);
-}
-void launch_batched_scale(int n, const double2* src, long long sstride, const double* scale,
-                          double2* dst, long long dstride, int nb, cudaStream_t s) {
-  batched_scale_kernel<<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, src, sstride, scale, dst,
-                                                                dstride);
-}
-void launch_herm_combine(int n, const double2* Y1, const double2* Y2, long long stride,
-                         const double* theta, double2* W, long long wstride, int nb,
-                         cudaStream_t s) {
-  herm_combine_kernel<<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, Y1, Y2, stride, theta, W,
-                                                               wstride);
+
+#define BEM2D_BATCHED_LAUNCHERS(T)                                                            \
+  void launch_batched_dots(const T* Q, long long qstride, int n, int j, const T* W,           \
+                           long long wstride, T* h, int ldh, int nb, cudaStream_t s) {        \
+    if (j <= 0) return;                                                                       \
+    batched_dots_kernel<T><<<dim3(j, nb), 256, 0, s>>>(Q, qstride, n, j, W, wstride, h, ldh); \
+  }                                                                                           \
+  void launch_batched_sub(const T* Q, long long qstride, int n, int j, T* W, long long wstride, \
+                          const T* h, int ldh, int nb, cudaStream_t s) {                      \
+    if (j <= 0) return;                                                                       \
+    batched_sub_kernel<T><<<dim3((n + 127) / 128, nb), 128, 0, s>>>(Q, qstride, n, j, W,      \
+                                                                   wstride, h, ldh);          \
+  }                                                                                           \
+  void launch_batched_norm2(int n, const T* W, long long wstride, double* out, int nb,        \
+                            cudaStream_t s) {                                                 \
+    batched_norm2_kernel<T><<<nb, 256, 0, s>>>(n, W, wstride, out);                           \
+  }                                                                                           \
+  void launch_batched_scale(int n, const T* src, long long sstride, const double* scale,      \
+                            T* dst, long long dstride, int nb, cudaStream_t s) {              \
+    batched_scale_kernel<T><<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, src, sstride, scale, \
+                                                                     dst, dstride);           \
+  }                                                                                           \
+  void launch_herm_combine(int n, const T* Y1, const T* Y2, long long stride,                 \
+                           const double* theta, T* W, long long wstride, int nb,              \
+                           cudaStream_t s) {                                                  \
+    herm_combine_kernel<T><<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, Y1, Y2, stride, theta, \
+                                                                    W, wstride);              \
+  }
+BEM2D_BATCHED_LAUNCHERS(double2)
+BEM2D_BATCHED_LAUNCHERS(float2)
+#undef BEM2D_BATCHED_LAUNCHERS
+
+void launch_widen(int n, const float2* src, long long sstride, double2* dst, long long dstride,
+                  int nb, cudaStream_t s) {
+  widen_kernel<<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, src, sstride, dst, dstride);
 }
 
 // y -= a x (real a)
@@ -384,6 +420,103 @@ bool tridiag_eigenvalues(std::vector<double> d, std::vector<double> e, std::vect
   }
   *ev = d;
   return true;
+}
+
+
+// Largest eigenvalue of the symmetric tridiagonal (d, e) by bisection on
+// Sturm counts (the number of negative pivots of T - x I = L D L^T is the
+// number of eigenvalues below x): O(n) per step, about 60 steps to full
+// precision, against O(n^2) for a complete QL sweep.
+double tridiag_lmax(const std::vector<double>& d, const std::vector<double>& e) {
+  const int n = (int)d.size();
+  double lo = INFINITY, hi = -INFINITY;
+  for (int i = 0; i < n; ++i) {  // Gershgorin bounds
+    const double r = (i > 0 ? std::fabs(e[i - 1]) : 0.0) + (i + 1 < n ? std::fabs(e[i]) : 0.0);
+    lo = std::min(lo, d[i] - r);
+    hi = std::max(hi, d[i] + r);
+  }
+  const double scale = std::max(std::fabs(lo), std::fabs(hi));
+  auto below = [&](double x) {  // eigenvalues < x
+    int cnt = 0;
+    double q = 1.0;
+    for (int i = 0; i < n; ++i) {
+      q = d[i] - x - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+      if (q == 0.0) q = -1e-300 * std::max(scale, 1.0);
+      if (q < 0) ++cnt;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200 && hi - lo > 2.2e-16 * std::max(scale, 1e-300); ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (below(mid) == n)
+      hi = mid;  // every eigenvalue below mid
+    else
+      lo = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+// Inverse iteration: solve (T - sigma I) x = b twice with sigma just above
+// lambda, by Gaussian elimination with partial pivoting on the tridiagonal
+// (as LAPACK's dgtsv), and normalise.
+std::vector<double> tridiag_eigenvector(const std::vector<double>& d, const std::vector<double>& e,
+                                        double lambda) {
+  const int n = (int)d.size();
+  std::vector<double> x(n, 1.0);
+  if (n == 1) return x;
+  double anorm = 0;
+  for (int i = 0; i < n; ++i)
+    anorm = std::max(anorm, std::fabs(d[i]) + (i > 0 ? std::fabs(e[i - 1]) : 0.0) +
+                                (i + 1 < n ? std::fabs(e[i]) : 0.0));
+  const double sigma = lambda + 1e-13 * std::max(anorm, 1e-300);
+  for (int it = 0; it < 3; ++it) {
+    // rows: sub l[i] (i >= 1), diag m[i], super u[i], second super u2[i]
+    std::vector<double> dl(n, 0.0), dm(n), du(n, 0.0), du2(n, 0.0), b(x);
+    for (int i = 0; i < n; ++i) {
+      dm[i] = d[i] - sigma;
+      if (i + 1 < n) {
+        du[i] = e[i];
+        dl[i + 1] = e[i];
+      }
+    }
+    for (int i = 0; i + 1 < n; ++i) {
+      if (std::fabs(dm[i]) >= std::fabs(dl[i + 1])) {
+        double f = dm[i] != 0.0 ? dl[i + 1] / dm[i] : 0.0;
+        dm[i + 1] -= f * du[i];
+        if (i + 2 < n) du[i + 1] -= f * du2[i];  // du2[i] is 0 here
+        b[i + 1] -= f * b[i];
+      } else {  // swap rows i and i+1
+        const double f = dm[i] / dl[i + 1];
+        const double t_m = dl[i + 1], t_u = dm[i + 1], t_u2 = (i + 2 < n) ? du[i + 1] : 0.0;
+        dm[i + 1] = du[i] - f * t_u;
+        if (i + 2 < n) du[i + 1] = -f * t_u2;
+        dm[i] = t_m;
+        du[i] = t_u;
+        du2[i] = t_u2;
+        const double tb = b[i];
+        b[i] = b[i + 1];
+        b[i + 1] = tb - f * b[i];
+      }
+    }
+    const double tiny = 1e-300;
+    for (int i = n - 1; i >= 0; --i) {
+      double v = b[i];
+      if (i + 1 < n) v -= du[i] * x[i + 1];
+      if (i + 2 < n) v -= du2[i] * x[i + 2];
+      const double piv = std::fabs(dm[i]) > tiny ? dm[i] : tiny;
+      x[i] = v / piv;
+    }
+    double nrm = 0;
+    for (double v : x) nrm += v * v;
+    nrm = std::sqrt(nrm);
+    if (!(nrm > 0) || !std::isfinite(nrm)) {
+      std::fill(x.begin(), x.end(), 1.0 / std::sqrt((double)n));
+      return x;
+    }
+    for (double& v : x) v /= nrm;
+  }
+  return x;
 }
 
 }  // namespace bem2d_gpu

@@ -18,18 +18,32 @@ void launch_mvh(const double2* A, long long lda, int n, const double2* x, double
                 cudaStream_t s);
 void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
                   long long ldb, int m, double2* C, long long ldc, cudaStream_t s);
-void launch_batched_dots(const double2* Q, long long qstride, int n, int j, const double2* W,
-                         long long wstride, double2* h, int ldh, int nb, cudaStream_t s);
-void launch_batched_sub(const double2* Q, long long qstride, int n, int j, double2* W,
-                        long long wstride, const double2* h, int ldh, int nb, cudaStream_t s);
-void launch_batched_norm2(int n, const double2* W, long long wstride, double* out, int nb,
-                          cudaStream_t s);
-void launch_batched_scale(int n, const double2* src, long long sstride, const double* scale,
-                          double2* dst, long long dstride, int nb, cudaStream_t s);
-void launch_herm_combine(int n, const double2* Y1, const double2* Y2, long long stride,
-                         const double* theta, double2* W, long long wstride, int nb,
-                         cudaStream_t s);
+void launch_zgemm(bool herm, const float2* A, long long lda, int n, const float2* B,
+                  long long ldb, int m, float2* C, long long ldc, cudaStream_t s);
+#define BEM2D_BATCHED_DECLS(T)                                                                \
+  void launch_batched_dots(const T* Q, long long qstride, int n, int j, const T* W,           \
+                           long long wstride, T* h, int ldh, int nb, cudaStream_t s);         \
+  void launch_batched_sub(const T* Q, long long qstride, int n, int j, T* W, long long wstride, \
+                          const T* h, int ldh, int nb, cudaStream_t s);                       \
+  void launch_batched_norm2(int n, const T* W, long long wstride, double* out, int nb,        \
+                            cudaStream_t s);                                                  \
+  void launch_batched_scale(int n, const T* src, long long sstride, const double* scale,      \
+                            T* dst, long long dstride, int nb, cudaStream_t s);               \
+  void launch_herm_combine(int n, const T* Y1, const T* Y2, long long stride,                 \
+                           const double* theta, T* W, long long wstride, int nb, cudaStream_t s);
+BEM2D_BATCHED_DECLS(double2)
+BEM2D_BATCHED_DECLS(float2)
+#undef BEM2D_BATCHED_DECLS
+// dst (complex128) = src (complex64), nb columns of n
+void launch_widen(int n, const float2* src, long long sstride, double2* dst, long long dstride,
+                  int nb, cudaStream_t s);
 void launch_axpy_real(int n, double a, const double2* x, double2* y, cudaStream_t s);
 bool tridiag_eigenvalues(std::vector<double> d, std::vector<double> e, std::vector<double>* ev);
+// Largest eigenvalue of the symmetric tridiagonal (d, e) (e: n-1 entries).
+double tridiag_lmax(const std::vector<double>& d, const std::vector<double>& e);
+// Unit eigenvector of the symmetric tridiagonal (d, e) for its eigenvalue
+// lambda (inverse iteration).
+std::vector<double> tridiag_eigenvector(const std::vector<double>& d, const std::vector<double>& e,
+                                        double lambda);
 
 }  // namespace bem2d_gpu

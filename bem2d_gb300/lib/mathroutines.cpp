@@ -141,7 +141,8 @@ void NumRange(const Matrix& m, int n, std::string filename) {
     th[i] = i * step;
     th[n + i] = i * step + PI;
   }
-  detail::check(bem2d_num_range(detail::ctx(), N, &(*m.data)[0], N, 2 * n, th.data(), 0.0, lmax.data()),
+  detail::check(bem2d_num_range(detail::ctx(), N, &(*m.data)[0], N, 2 * n, th.data(), 0.0,
+                                GetSolverPrecision(), lmax.data()),
                 "NumRange");
   dvector eigs(2 * n), steps(2 * n);
   for (int i = 0; i < n; ++i) {

@@ -182,6 +182,111 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
+AUX = {
+    "square8192_normcond": "unit square, corner grading L=8 sigma=0.15, N=8192, k=200, eta=k: "
+                           "||A||_2, ||A^-1||_2, cond(A) of ChangeBasis(A, Id)",
+    "numrange2048": "unit square Polygon(pts, 512), N=2048, k=50, eta=k: numerical range of "
+                    "ChangeBasis(A, Id), lambda_max of the Hermitian part at 360 angles",
+}
+
+
+def run_aux(args):
+    """Norm / condition (BASELINE config 3) and numerical range (config 5b):
+    one step = mixed assembly + ChangeBasis(A, Id) + the study, through the C
+    ABI.  The results are checked once, untimed, against dense cuSOLVER
+    spectra (torch.linalg)."""
+    import torch
+    from bem2d_gb300 import capi
+    from bem2d_gb300 import geometry as G
+    ctx = capi.Context(0)
+    if args.workload == "square8192_normcond":
+        g = G.graded_square(2032, 8, 0.15).add_poly_basis(0)
+        k = 200.0
+    else:
+        g = G.polygon_uniform([(0, 0), (1, 0), (1, 1), (0, 1)], 512).add_poly_basis(0)
+        k = 50.0
+    arrays = g.arrays()
+    n = g.n_unknowns
+    dev = "cuda"
+    A = torch.empty((n, n), dtype=torch.complex128, device=dev)   # column-major A = A.T view
+    A32 = torch.empty((n, n), dtype=torch.complex64, device=dev)
+    M = torch.zeros((n, n), dtype=torch.complex128, device=dev)
+    B = torch.empty((n, n), dtype=torch.complex128, device=dev)
+    bstart = np.arange(n + 1, dtype=np.int32)  # P0: 1 x 1 mass blocks
+    thetas = 2 * np.pi * np.arange(360) / 360.0
+    ph = {}
+
+    def step():
+        t = []
+        for name, fn in (
+                ("assembly", lambda: ctx.discrete_kernel_mixed(arrays, "combined", k, k, QUAD,
+                                                               2.0, 1.0, out=A, out32=A32)),
+                ("change_basis", lambda: (ctx.eval_ident(arrays, QUAD, out=M),
+                                          ctx.change_basis(A, M, bstart, out=B))),
+                ("study", lambda: ph.__setitem__(
+                    "out", ctx.norm_cond(B) if args.workload == "square8192_normcond"
+                    else ctx.num_range_lmax(B, thetas, precision="mixed")))):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            t.append((name, e0.elapsed_time(e1)))
+        return t
+
+    for _ in range(args.warmup):
+        step()
+    runs = [step() for _ in range(args.steps)]
+    ms = [sum(v for _, v in r) for r in runs]
+    phases = {name: sum(r[i][1] for r in runs) / len(runs) for i, (name, _) in enumerate(runs[0])}
+    Bt = B.T  # the column-major matrix as a torch view
+    res = {"metric": "norm-cond evaluations/s" if args.workload == "square8192_normcond"
+           else "numerical-range scans/s",
+           "value": 1e3 * len(ms) / sum(ms), "unit": "1/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True,
+           "dtype": "mixed assembly; f64 Lanczos on the complex128 operator"
+           if args.workload == "square8192_normcond" else
+           "mixed assembly; c64 Lanczos, then f64 Lanczos from its Ritz vectors",
+           "data": "synthetic", "config": {"workload": AUX[args.workload], "n_unknowns": n},
+           "phases_ms": phases}
+    if args.workload == "square8192_normcond":
+        nrm, cond = ph["out"]
+        sv = torch.linalg.svdvals(Bt)
+        smax, smin = float(sv[0]), float(sv[-1])
+        res["result"] = {"norm": nrm, "norm_inv": cond / nrm, "cond": cond}
+        res["rel_err_vs_dense_svd"] = {"norm": abs(nrm - smax) / smax,
+                                      "norm_inv": abs(cond / nrm - 1 / smin) * smin,
+                                      "cond": abs(cond - smax / smin) / (smax / smin)}
+    else:
+        lm = ph["out"]
+        # the plain FP64 path (complex128 Lanczos from the start), timed once
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        lm64 = ctx.num_range_lmax(B, thetas, precision="fp64")
+        e1.record()
+        e1.synchronize()
+        t64 = e0.elapsed_time(e1)
+        res["plain_fp64"] = {"study_ms": t64, "value": 1e3 / (t64 + phases["assembly"] +
+                                                              phases["change_basis"]),
+                             "unit": "1/s"}
+        res["mixed_over_fp64_study"] = t64 / phases["study"]
+        res["mixed_vs_fp64_max_rel_err"] = float(np.max(np.abs(lm - lm64)) / np.max(np.abs(lm64)))
+        errs = []
+        for j in range(0, 360, 45):
+            z = complex(np.cos(thetas[j]), np.sin(thetas[j]))
+            H = 0.5 * (z * Bt + np.conj(z) * Bt.conj().T)
+            ev = float(torch.linalg.eigvalsh(H)[-1])
+            errs.append(abs(lm[j] - ev) / max(abs(ev), 1e-300))
+        res["result"] = {"lambda_max_min": float(np.min(lm)), "lambda_max_max": float(np.max(lm))}
+        res["max_rel_err_vs_dense_eigvalsh"] = max(errs)
+        res["checked_angles"] = 8
+    print(json.dumps(res))
+
+
 def run_only(args):
     """Profiling driver: one phase only (assembly or solve) of the largest
     problem of the workload, or the whole mixed sweep; no JSON line."""
@@ -197,16 +302,26 @@ def run_only(args):
     A = torch.empty((n, n), dtype=torch.complex128, device="cuda") \
         if args.only == "assembly" else None
     x = torch.zeros(n, dtype=torch.complex128, device="cuda")
-    for _ in range(args.warmup + args.steps):
+    step_ms = []
+    for it in range(args.warmup + args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
         if args.only == "assembly":
             ctx.discrete_kernel(arrays, "combined", k, eta, QUAD, 2.0, 1.0, out=A)
         elif args.only == "sweep":
             ctx.sweep_solve([p[0] for p in probs], [p[1] for p in probs], w["d"],
-                            [p[2] for p in probs], QUAD, "mixed", nworkers=SWEEP_WORKERS)
+                            [p[2] for p in probs], QUAD, "mixed", nworkers=args.workers)
         else:
             ctx.scattering_solve(arrays, k, w["d"], eta, QUAD, precision=args.only, out=x)
+        e1.record()
+        e1.synchronize()
+        if it >= args.warmup:
+            step_ms.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
     print(json.dumps({"only": args.only, "workload": args.workload, "n": n,
+                      "step_ms": step_ms, "workers": args.workers if args.only == "sweep" else None,
                       "timers_ms": {k: v[0] / max(v[1], 1) for k, v in ctx.timers().items()}}))
 
 
@@ -268,7 +383,7 @@ def run_ours(args):
             return lambda: ctx.scattering_solve(holds[0].arrays, ks[0], w["d"], etas[0], QUAD,
                                                 precision="mixed", out=outs[0])
         return lambda: ctx.sweep_solve(holds, ks, w["d"], etas, QUAD, "mixed",
-                                       nworkers=SWEEP_WORKERS, outs=outs)
+                                       nworkers=args.workers, outs=outs)
 
     def fp64_all():
         for i in range(P):
@@ -345,7 +460,7 @@ def run_ours(args):
         "data": "synthetic",
         "config": {"workload": w["desc"], "problems_per_step": P,
                    "n_unknowns": ns[0] if P == 1 else [min(ns), max(ns)],
-                   "precision": "mixed", "sweep_workers": SWEEP_WORKERS if P > 1 else None,
+                   "precision": "mixed", "sweep_workers": args.workers if P > 1 else None,
                    "l2": "256 MB write between timed steps, outside the step events",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": ws * P * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -389,10 +504,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ellipse_sweep256")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--workers", type=int, default=SWEEP_WORKERS,
+                    help="concurrent problems (host workers, one stream each) of a sweep")
     ap.add_argument("--only", choices=["assembly", "mixed", "fp64", "sweep"],
                     help="profiling driver: run one phase, print its timers")
     args = ap.parse_args()
-    if args.only:
+    if args.workload in AUX:
+        run_aux(args)
+    elif args.only:
         run_only(args)
     elif args.impl == "reference":
         run_reference(args)

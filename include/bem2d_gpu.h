@@ -215,9 +215,14 @@ int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double
  * nang angles th_j: the eigenvalue step of NumRange
  * (lib/bem2d_mathroutines.cpp:590-653, zheev per angle; the smallest
  * eigenvalue at th is -lmax at th + pi).  Lanczos with full
- * reorthogonalisation, all angles in one block of matrix products. */
+ * reorthogonalisation, all angles in one block of matrix products, until
+ * lmax moves by less than tol (relative; tol <= 0 selects 1e-13).
+ * BEM2D_PREC_FP64: complex128 throughout.  BEM2D_PREC_MIXED: complex64
+ * Lanczos (three-term recurrence, cold start) to 1e-6, then complex128 Lanczos
+ * (full reorthogonalisation) started from its Ritz
+ * vectors (same tolerance). */
 int bem2d_num_range(bem2d_ctx* ctx, int n, const void* A, int64_t lda, int nang,
-                    const double* theta, double tol, double* lmax);
+                    const double* theta, double tol, int precision, double* lmax);
 
 /* out[j] = sum_u c_u sum_q K(p_j, y_uq) |J(y_uq)| phi_u(y_uq) w_q: the
  * potential of the density c at npts points p (x0 y0 x1 y1 ...): replaces

@@ -88,6 +88,9 @@ def test_num_range_matches_reference(ctx):
     lm = ctx.num_range_lmax(B, th)
     ref = O.numrange_lmax(B, th)
     assert np.abs(lm - ref).max() < 1e-12 * np.abs(ref).max()
+    # complex64 Lanczos + complex128 Lanczos from its Ritz vectors: same bar
+    lm_mixed = ctx.num_range_lmax(B, th, precision="mixed")
+    assert np.abs(lm_mixed - ref).max() < 1e-12 * np.abs(ref).max()
     steps = np.arange(n) * np.pi / n
     eigs = np.concatenate([-lm[n:], lm[:n], [-lm[n]]])
     st = np.concatenate([steps, steps, [0.0]])
