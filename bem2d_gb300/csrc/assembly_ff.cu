@@ -22,42 +22,53 @@ struct KConstFF {
   ff k, invk, kq, eq, amp0;
 };
 
-template <int KERNEL>
-__device__ __forceinline__ ffc kernel_ff(ff dx, ff dy, ff n1x, ff n1y, ff n2x, ff n2y,
-                                         const KConstFF& kc, const float* tab) {
+// The distance-dependent part of the kernel at one node pair: 1/d, the
+// asymptotic P/Q factors of H0 and H1, the amplitude sqrt(2/(pi x)) and
+// e^{i(x - pi/4)}.  Shared by entry (i, j) and entry (j, i).
+struct HankelTermsFF {
+  ff y, p0, q0, p1, q1, amp;
+  ffc e;
+};
+
+__device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KConstFF& kc,
+                                                        const float* tab) {
+  HankelTermsFF h;
   const ff d2 = ff_add_fast(ff_sqr(dx), ff_sqr(dy));
-  const ff y = ff_rsqrt(d2);  // 1/d
-  const ff d = ff_mul(d2, y);
+  h.y = ff_rsqrt(d2);  // 1/d
+  const ff d = ff_mul(d2, h.y);
   const ff x = ff_mul(d, kc.k);
-  const ff ix = ff_mul(y, kc.invk);
-  ff p0, q0, p1, q1;
-  pq_ff(x.hi, ix, &p0, &q0, &p1, &q1);
-  const ff amp = ff_mul(kc.amp0, ff_sqrt(ix));
-  const ffc e = expi_ff(x, tab);
+  const ff ix = ff_mul(h.y, kc.invk);
+  pq_ff(x.hi, ix, &h.p0, &h.q0, &h.p1, &h.q1);
+  h.amp = ff_mul(kc.amp0, ff_sqrt(ix));
+  h.e = expi_ff(x, tab);
+  return h;
+}
+
+// Kernel value from the shared terms.  dot: the normal factor of the
+// double-layer kernels (n_x . (x - y) for the adjoint double layer at
+// (x, y), n_y . (y - x) for the double layer); unused by SINGLE.
+template <int KERNEL>
+__device__ __forceinline__ ffc kernel_from_terms(const HankelTermsFF& h, ff dot,
+                                                 const KConstFF& kc) {
   ffc F;
   if (KERNEL == BEM2D_KERNEL_SINGLE) {
     // (i/4) H0:  F = (i/4)(P0 + i Q0)
-    F.re = ff_scale2(ff_neg(q0), 0.25f);
-    F.im = ff_scale2(p0, 0.25f);
+    F.re = ff_scale2(ff_neg(h.q0), 0.25f);
+    F.im = ff_scale2(h.p0, 0.25f);
   } else {
-    ff dot;
-    if (KERNEL == BEM2D_KERNEL_DOUBLE)
-      dot = ff_neg(ff_add_fast(ff_mul(n2x, dx), ff_mul(n2y, dy)));
-    else
-      dot = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));
-    const ff cc = ff_mul(ff_mul(dot, y), kc.kq);  // (k/4) n.w/d
+    const ff cc = ff_mul(ff_mul(dot, h.y), kc.kq);  // (k/4) n.w/d
     // -i (k/4) c H1 with H1 = -i amp (P1 + i Q1) E  ->  -(k/4) c (P1 + i Q1)
-    F.re = ff_neg(ff_mul(cc, p1));
-    F.im = ff_neg(ff_mul(cc, q1));
+    F.re = ff_neg(ff_mul(cc, h.p1));
+    F.im = ff_neg(ff_mul(cc, h.q1));
     if (KERNEL == BEM2D_KERNEL_COMBINED) {
-      F.re = ff_add_fast(F.re, ff_mul(kc.eq, p0));
-      F.im = ff_add_fast(F.im, ff_mul(kc.eq, q0));
+      F.re = ff_add_fast(F.re, ff_mul(kc.eq, h.p0));
+      F.im = ff_add_fast(F.im, ff_mul(kc.eq, h.q0));
     }
   }
   // K = amp E F
   ffc K;
-  K.re = ff_mul(amp, ff_add_fast(ff_mul(e.re, F.re), ff_neg(ff_mul(e.im, F.im))));
-  K.im = ff_mul(amp, ff_add_fast(ff_mul(e.re, F.im), ff_mul(e.im, F.re)));
+  K.re = ff_mul(h.amp, ff_add_fast(ff_mul(h.e.re, F.re), ff_neg(ff_mul(h.e.im, F.im))));
+  K.im = ff_mul(h.amp, ff_add_fast(ff_mul(h.e.re, F.im), ff_mul(h.e.im, F.re)));
   return K;
 }
 
@@ -87,23 +98,47 @@ constexpr int kTileF = 32;
 constexpr int kFarFFThreads = 256;
 constexpr float kDeferX = 8.001f;
 
+// Tiles are processed in symmetric pairs: CTA b owns tile (I, J), I <= J,
+// and computes both (I, J) and (J, I).  The distance-dependent work at a node
+// pair (the Hankel terms, most of the cost) is the same for entry (r, c) and
+// entry (c, r); only the normal factor of the double-layer kernels differs.
+// Entry (r, c) is stored directly (a warp writes 32 consecutive rows of a
+// column); entry (c, r) goes to a shared-memory copy of tile (J, I) that is
+// written out, column by column, at the end.  A pair that is near in either
+// direction is left, in that direction, to the near-field kernel; the
+// small-argument test depends on the distance only, so a deferred pair is
+// deferred in both directions.  On a diagonal tile only r < c is computed.
+__device__ __forceinline__ void tile_of(unsigned b, int* I, int* J) {
+  int j = (int)((sqrt(8.0 * (double)b + 1.0) - 1.0) * 0.5);
+  while ((long long)(j + 1) * (j + 2) / 2 <= (long long)b) ++j;
+  while ((long long)j * (j + 1) / 2 > (long long)b) --j;
+  *J = j;
+  *I = (int)((long long)b - (long long)j * (j + 1) / 2);
+}
+
 template <int KERNEL, int NG>
-__global__ void __launch_bounds__(kFarFFThreads)
+__global__ void __launch_bounds__(kFarFFThreads, 2)
 far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, double k,
               double eta, double alpha, double2* __restrict__ out, long long ld,
               float2* __restrict__ out32, long long ld32, DeferList dl, const float* gtab) {
   const int ng = NG > 0 ? NG : ng_rt;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* tab = reinterpret_cast<float*>(smem_raw);             // 256
+  double2* tT = reinterpret_cast<double2*>(smem_raw);          // [32][33] tile (J, I)
+  unsigned* vT = reinterpret_cast<unsigned*>(tT + kTileF * (kTileF + 1));  // [32] masks
+  float* tab = reinterpret_cast<float*>(vT + kTileF);          // 256
   double2* cen = reinterpret_cast<double2*>(tab + 256);        // rows 32, cols 32
   float2* rs = reinterpret_cast<float2*>(cen + 2 * kTileF);    // [5][ng][32]
   float2* cs = rs + 5 * ng * kTileF;                           // [5][ng][32]
   float* rad = reinterpret_cast<float*>(cs + 5 * ng * kTileF); // rows 32, cols 32
-  long long* links = reinterpret_cast<long long*>(rad + 2 * kTileF);  // 4 x 32
+  long long* links = reinterpret_cast<long long*>(rad + 2 * kTileF);  // 6 x 32
 
-  const int row0 = blockIdx.x * kTileF, col0 = blockIdx.y * kTileF;
+  int I, J;
+  tile_of(blockIdx.x, &I, &J);
+  const int row0 = I * kTileF, col0 = J * kTileF;
+  const bool diag = I == J;
   const int n = g.n_unk;
   for (int v = threadIdx.x; v < 256; v += blockDim.x) tab[v] = gtab[v];
+  if (threadIdx.x < kTileF) vT[threadIdx.x] = 0u;
   const int SZ = ng * kTileF;
   for (int v = threadIdx.x; v < SZ; v += blockDim.x) {
     const int q = v / kTileF, l = v - q * kTileF;
@@ -133,6 +168,8 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
     links[kTileF + l] = g.next[er];
     links[2 * kTileF + l] = g.prev[er];
     links[3 * kTileF + l] = g.index[ec];
+    links[4 * kTileF + l] = g.next[ec];
+    links[5 * kTileF + l] = g.prev[ec];
   }
   __syncthreads();
 
@@ -146,29 +183,36 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
 #pragma unroll 1
   for (int cc = warp; cc < kTileF; cc += kFarFFThreads / 32) {
     const int col = col0 + cc;
-    const long long ci = links[3 * kTileF + cc];
-    const bool near = (ri == ci) || (rn == ci) || (rp == ci);
-    if (row >= n || col >= n || near) continue;
+    const long long ci = links[3 * kTileF + cc], cn = links[4 * kTileF + cc],
+                    cp = links[5 * kTileF + cc];
+    // rc: entry (row, col); cr: entry (col, row)
+    bool rc = row < n && col < n && !((ri == ci) || (rn == ci) || (rp == ci));
+    bool cr = row < n && col < n && !((ci == ri) || (cn == ri) || (cp == ri));
+    if (diag && lane >= cc) rc = cr = false;
+    if (!rc && !cr) continue;
     const double dxc = crow.x - cen[kTileF + cc].x, dyc = crow.y - cen[kTileF + cc].y;
     const float dist = sqrtf((float)(dxc * dxc + dyc * dyc));
     if (kf * (dist * (1.0f - 1e-6f) - rrow - rad[kTileF + cc]) <= kDeferX) {
       // small arguments somewhere on this pair: FP64 pass (or here, if the
       // list is full)
-      const unsigned slot = atomicAdd(dl.count, 1u);
-      if (slot < dl.capacity) {
-        dl.ij[slot] = make_int2(row, col);
-      } else {
-        double re, im;
-        entry_fp64<KERNEL>(t, ng, row, col, k, 0.25 * k, 0.25 * eta, &re, &im);
-        out[(size_t)col * ld + row] = make_double2(alpha * re, alpha * im);
-        out32[(size_t)col * ld32 + row] = make_float2((float)(alpha * re), (float)(alpha * im));
+      for (int dir = 0; dir < 2; ++dir) {
+        if (!(dir == 0 ? rc : cr)) continue;
+        const int a = dir == 0 ? row : col, b = dir == 0 ? col : row;
+        const unsigned slot = atomicAdd(dl.count, 1u);
+        if (slot < dl.capacity) {
+          dl.ij[slot] = make_int2(a, b);
+        } else {
+          double re, im;
+          entry_fp64<KERNEL>(t, ng, a, b, k, 0.25 * k, 0.25 * eta, &re, &im);
+          out[(size_t)b * ld + a] = make_double2(alpha * re, alpha * im);
+          out32[(size_t)b * ld32 + a] = make_float2((float)(alpha * re), (float)(alpha * im));
+        }
       }
       continue;
     }
     const ff Dx = ff_from_double(dxc), Dy = ff_from_double(dyc);
-    ffc acc;
-    acc.re = ff_make(0.0f, 0.0f);
-    acc.im = ff_make(0.0f, 0.0f);
+    ffc arc, acr;
+    arc.re = arc.im = acr.re = acr.im = ff_make(0.0f, 0.0f);
 #pragma unroll 1
     for (int q1 = 0; q1 < ng; ++q1) {
       const int o1 = q1 * kTileF + lane;
@@ -181,18 +225,57 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
         const int o2 = q2 * kTileF + cc;
         const float2 b0 = cs[o2], b1 = cs[SZ + o2], b2 = cs[2 * SZ + o2], b3 = cs[3 * SZ + o2],
                      b4 = cs[4 * SZ + o2];
+        // w = x - y, x a node of the row element, y of the column element
         const ff dx = ff_add_fast(Dx, ff_add_fast(ox1, ff_make(-b0.x, -b0.y)));
         const ff dy = ff_add_fast(Dy, ff_add_fast(oy1, ff_make(-b1.x, -b1.y)));
-        const ffc K = kernel_ff<KERNEL>(dx, dy, n1x, n1y, ff_make(b2.x, b2.y),
-                                        ff_make(b3.x, b3.y), kc, tab);
+        const HankelTermsFF h = hankel_terms_ff(dx, dy, kc, tab);
         const ff ww = ff_mul(w1, ff_make(b4.x, b4.y));
-        acc.re = ff_add_fast(acc.re, ff_mul(K.re, ww));
-        acc.im = ff_add_fast(acc.im, ff_mul(K.im, ww));
+        ff dot_rc = ff_make(0.0f, 0.0f), dot_cr = ff_make(0.0f, 0.0f);
+        if (KERNEL != BEM2D_KERNEL_SINGLE) {
+          const ff n1w = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));  // n_x . (x - y)
+          const ff n2w = ff_add_fast(ff_mul(ff_make(b2.x, b2.y), dx),
+                                     ff_mul(ff_make(b3.x, b3.y), dy));  // n_y . (x - y)
+          if (KERNEL == BEM2D_KERNEL_DOUBLE) {
+            dot_rc = ff_neg(n2w);  // (row, col): n_y . (y - x)
+            dot_cr = n1w;          // (col, row): n_x . (x - y)
+          } else {
+            dot_rc = n1w;          // (row, col): n_x . (x - y)
+            dot_cr = ff_neg(n2w);  // (col, row): n_y . (y - x)
+          }
+        }
+        if (rc) {
+          const ffc K = kernel_from_terms<KERNEL>(h, dot_rc, kc);
+          arc.re = ff_add_fast(arc.re, ff_mul(K.re, ww));
+          arc.im = ff_add_fast(arc.im, ff_mul(K.im, ww));
+        }
+        if (cr) {
+          const ffc K = KERNEL == BEM2D_KERNEL_SINGLE ? kernel_from_terms<KERNEL>(h, dot_rc, kc)
+                                                      : kernel_from_terms<KERNEL>(h, dot_cr, kc);
+          acr.re = ff_add_fast(acr.re, ff_mul(K.re, ww));
+          acr.im = ff_add_fast(acr.im, ff_mul(K.im, ww));
+        }
       }
     }
-    const double re = alpha * ff_to_double(acc.re), im = alpha * ff_to_double(acc.im);
-    out[(size_t)col * ld + row] = make_double2(re, im);
-    out32[(size_t)col * ld32 + row] = make_float2((float)re, (float)im);
+    if (rc) {
+      const double re = alpha * ff_to_double(arc.re), im = alpha * ff_to_double(arc.im);
+      out[(size_t)col * ld + row] = make_double2(re, im);
+      out32[(size_t)col * ld32 + row] = make_float2((float)re, (float)im);
+    }
+    if (cr) {
+      tT[cc * (kTileF + 1) + lane] =
+          make_double2(alpha * ff_to_double(acr.re), alpha * ff_to_double(acr.im));
+      atomicOr(&vT[cc], 1u << lane);
+    }
+  }
+  __syncthreads();
+  // tile (J, I): entry (col0 + cc, row0 + l) = tT[cc][l]; a warp writes 32
+  // consecutive rows (cc) of one column (row0 + l)
+  for (int l = warp; l < kTileF; l += kFarFFThreads / 32) {
+    const int cc = lane;
+    if (!((vT[cc] >> l) & 1u)) continue;
+    const double2 v = tT[cc * (kTileF + 1) + l];
+    out[(size_t)(row0 + l) * ld + col0 + cc] = v;
+    out32[(size_t)(row0 + l) * ld32 + col0 + cc] = make_float2((float)v.x, (float)v.y);
   }
 }
 
@@ -243,10 +326,12 @@ static int launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTable
   kc.kq = ff_from_double(0.25 * k);
   kc.eq = ff_from_double(0.25 * eta);
   kc.amp0 = ff_from_double(0.79788456080286535588);  // sqrt(2/pi)
-  const size_t smem = sizeof(float) * 256 + sizeof(double2) * 2 * kTileF +
+  const size_t smem = sizeof(double2) * kTileF * (kTileF + 1) + sizeof(unsigned) * kTileF +
+                      sizeof(float) * 256 + sizeof(double2) * 2 * kTileF +
                       sizeof(float2) * 10 * ng * kTileF + sizeof(float) * 2 * kTileF +
-                      sizeof(long long) * 4 * kTileF;
-  dim3 grid((g.n_unk + kTileF - 1) / kTileF, (g.n_unk + kTileF - 1) / kTileF);
+                      sizeof(long long) * 6 * kTileF;
+  const unsigned nt = (unsigned)((g.n_unk + kTileF - 1) / kTileF);
+  dim3 grid(nt * (nt + 1) / 2);  // tile pairs (I, J), I <= J
   const float* tab = expi_table_dev();
   if (!tab) return BEM2D_ERR_NOMEM;
   if (ng == 5) {
