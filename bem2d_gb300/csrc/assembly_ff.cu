@@ -5,7 +5,7 @@
 // unknown, node data staged in shared memory).  Pair geometry: the centre
 // difference of the two elements in FP64, node offsets from the centres in
 // float-float, so |x - y| keeps ~48 bits relative to itself even for
-// neighbouring elements.  Entries whose element pair admits k|x - y| <= 8
+// neighbouring elements.  Entries whose element pair admits k|x - y| <= 4
 // anywhere (bounded with the element radii) are deferred to an FP64 pass,
 // where the small-argument Hankel pieces live; adjacent and identical pairs
 // belong to the FP64 near-field kernel as in the FP64 path.  Each entry is
@@ -96,7 +96,7 @@ __device__ __forceinline__ void entry_fp64(const NodeTable& t, int ng, int row, 
 
 constexpr int kTileF = 32;
 constexpr int kFarFFThreads = 256;
-constexpr float kDeferX = 8.001f;
+constexpr float kDeferX = 4.001f;
 
 // Tiles are processed in symmetric pairs: CTA b owns tile (I, J), I <= J,
 // and computes both (I, J) and (J, I).  The distance-dependent work at a node

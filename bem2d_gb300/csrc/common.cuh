@@ -233,7 +233,7 @@ struct NodeTableFF {
 void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
                        const NodeTableFF* tf, cudaStream_t s);
 
-// Entries the float-float far kernel leaves to FP64 (an argument k|x-y| <= 8
+// Entries the float-float far kernel leaves to FP64 (an argument k|x-y| <= 4
 // somewhere on the element pair): (row, column) list with a counter.
 struct DeferList {
   int2* ij;

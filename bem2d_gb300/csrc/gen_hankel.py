@@ -135,7 +135,9 @@ def f32(v):
     return float(np.float32(float(v)))
 
 
-FF_INTERVALS = ((8, 16), (16, 64), (64, None))
+# index 3 (4 <= x < 8) was added after the first three; the order keeps the
+# generated names of the others
+FF_INTERVALS = ((8, 16), (16, 64), (64, None), (4, 8))
 FF_TAIL_BOUND = 1.5e-8
 
 
@@ -189,9 +191,9 @@ def main():
                    % (suffix, max(map(len, small)), max(map(len, mid)), max(map(len, far))))
     with open(os.path.join(HERE, "hankel_coeffs.h"), "w") as f:
         f.write("\n".join(out) + "\n")
-    # float-float tables for x > 8 (three intervals)
+    # float-float tables for x >= 4 (four intervals)
     out = ["// Generated by gen_hankel.py: float-float pieces of the Hankel evaluator",
-           "// for x > 8 (see hankel_ff.cuh).  Do not edit by hand.",
+           "// for x >= 4 (see hankel_ff.cuh).  Do not edit by hand.",
            "#pragma once", '#include "ff.cuh"', "", "namespace bem2d_gpu {", ""]
     for idx, (X, xhi) in enumerate(FF_INTERVALS):
         funcs, slo = pq_funcs(X, mp.mpf(xhi) if xhi else None)

@@ -1,7 +1,7 @@
 // Far-field kernel evaluation in float-float arithmetic (FP32 pipe) for
-// arguments x = k d > 8: H0 and H1 in modulus-phase form
+// arguments x = k d >= 4: H0 and H1 in modulus-phase form
 //   H_nu(x) = sqrt(2/(pi x)) (P_nu + i Q_nu) e^{i(x - (2 nu + 1) pi/4)}
-// with P, Q from hankel_ff_coeffs.h (three intervals of x), and e^{i(x-pi/4)}
+// with P, Q from hankel_ff_coeffs.h (four intervals of x), and e^{i(x-pi/4)}
 // from a Cody-Waite reduction modulo 2 pi/64 plus short Taylor polynomials
 // around a 64-entry table of e^{i(2 pi j/64 - pi/4)}.  Accuracy ~1e-14
 // relative to |H|; the same source builds on the host for accuracy tests.
@@ -51,11 +51,20 @@ __host__ __device__ __forceinline__ ffc expi_ff(ff x, const float* tab) {
   return e;
 }
 
-// P0, Q0, P1, Q1 at x > 8 given ix = 1/x.
+// P0, Q0, P1, Q1 at x >= 4 given ix = 1/x.
 __host__ __device__ __forceinline__ void pq_ff(float xhi, ff ix, ff* p0, ff* q0, ff* p1,
                                                ff* q1) {
   const ff ix2 = ff_sqr(ix);
-  if (xhi < 16.0f) {
+  if (xhi < 8.0f) {
+    const ff s = ff_scale2(ix2, 16.0f);  // (4/x)^2 in (1/4, 1]
+    const ff tt = ff_add_fast(ff_mul(s, ff_make(2.6666667461395264f, -7.947286206899662e-08f)),
+                              ff_make(-1.6666666269302368f, -3.973643103449831e-08f));
+    const ff q = ff_scale2(ix, 4.0f);
+    *p0 = hkff_3_0(tt);
+    *q0 = ff_mul(hkff_3_1(tt), q);
+    *p1 = hkff_3_2(tt);
+    *q1 = ff_mul(hkff_3_3(tt), q);
+  } else if (xhi < 16.0f) {
     const ff s = ff_scale2(ix2, 64.0f);  // (8/x)^2 in [1/4, 1]
     // t = 2 (s - 1/4) / (3/4) - 1 = (8/3) s - 5/3
     const ff tt = ff_add_fast(ff_mul(s, ff_make(2.6666667461395264f, -7.947286206899662e-08f)),

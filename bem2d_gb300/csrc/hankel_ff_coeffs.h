@@ -1,5 +1,5 @@
 // Generated by gen_hankel.py: float-float pieces of the Hankel evaluator
-// for x > 8 (see hankel_ff.cuh).  Do not edit by hand.
+// for x >= 4 (see hankel_ff.cuh).  Do not edit by hand.
 #pragma once
 #include "ff.cuh"
 
@@ -95,6 +95,49 @@ __host__ __device__ __forceinline__ ff hkff_2_3(ff t) {
   const float tail = fmaf(fmaf(fmaf(-2.497464547e-19f, t.hi, 9.327624092e-17f), t.hi, -5.628396376e-14f), t.hi, 6.445888961e-11f);
   ff y = ff_add_f(ff_make(-1.954486493e-07f, -4.400672010e-15f), t.hi * tail);
   y = ff_add_fast(ff_make(5.859179422e-03f, 6.457173685e-11f), ff_mul(t, y));
+  return y;
+}
+
+// x in [4, 8): P0, (x/4) Q0, P1, (x/4) Q1 in t = 2 (s - 0.25)/(1 - 0.25) - 1,
+// s = (4/x)^2
+__host__ __device__ __forceinline__ ff hkff_3_0(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-9.966476971e-14f, t.hi, 2.834943380e-13f), t.hi, -4.609592330e-13f), t.hi, 1.563911869e-12f), t.hi, -6.037730212e-12f), t.hi, 2.135572448e-11f), t.hi, -7.985621886e-11f), t.hi, 3.236383106e-10f), t.hi, -1.432233110e-09f), t.hi, 7.083329034e-09f);
+  ff y = ff_add_f(ff_make(-4.054247782e-08f, -4.227331005e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(2.835932378e-07f, -1.179624246e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-2.660637392e-06f, -4.541433215e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(4.005517985e-05f, 1.619732235e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.484501641e-03f, 3.700010090e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.973993301e-01f, -2.831054680e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_3_1(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-8.603064618e-15f, t.hi, 2.193270861e-14f), t.hi, -1.847712081e-14f), t.hi, 5.969276316e-14f), t.hi, -2.642188497e-13f), t.hi, 7.824213282e-13f), t.hi, -2.333518795e-12f), t.hi, 7.571226632e-12f), t.hi, -2.571285199e-11f), t.hi, 9.176995969e-11f), t.hi, -3.488292433e-10f), t.hi, 1.432085894e-09f), t.hi, -6.473263259e-09f);
+  ff y = ff_add_f(ff_make(3.313157393e-08f, -1.652424908e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(-2.004139503e-07f, 6.548905959e-15f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.537146659e-06f, 9.179610299e-15f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.698078631e-05f, -4.527189713e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(3.538296151e-04f, 1.055392058e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-3.060379811e-02f, 4.511467311e-10f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_3_2(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(1.077778478e-13f, t.hi, -3.073842721e-13f), t.hi, 5.035856714e-13f), t.hi, -1.713513012e-12f), t.hi, 6.628552308e-12f), t.hi, -2.355503119e-11f), t.hi, 8.858114936e-11f), t.hi, -3.614105126e-10f), t.hi, 1.612949552e-09f), t.hi, -8.065939916e-09f);
+  ff y = ff_add_f(ff_make(4.687875688e-08f, 5.662665657e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(-3.354862770e-07f, -1.096394484e-16f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(3.270190973e-06f, 6.238468130e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-5.324109952e-05f, -1.221442001e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.532773418e-03f, 7.705639946e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.004387736e+00f, 4.432021328e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_3_3(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(fmaf(-2.355683330e-14f, t.hi, 6.154680308e-14f), t.hi, -6.479468654e-14f), t.hi, 2.083127507e-13f), t.hi, -8.497687146e-13f), t.hi, 2.622495103e-12f), t.hi, -8.282361776e-12f), t.hi, 2.819539567e-11f), t.hi, -1.012866249e-10f), t.hi, 3.872884236e-10f), t.hi, -1.601550559e-09f), t.hi, 7.307455530e-09f);
+  ff y = ff_add_f(ff_make(-3.787590330e-08f, -4.528970290e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(2.332946707e-07f, -4.871077686e-15f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.841078415e-06f, 9.906881257e-15f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.142969970e-05f, -9.038700235e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-5.072252243e-04f, -1.697871357e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.283403307e-02f, -2.668786969e-09f), ff_mul(t, y));
   return y;
 }
 

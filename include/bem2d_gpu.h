@@ -136,7 +136,7 @@ int bem2d_discrete_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom,
 /* Mixed-precision variant of bem2d_discrete_kernel: same matrix, with the
  * far-field bulk evaluated in compensated single-single (float-float)
  * arithmetic on the FP32 pipe (~1e-14 relative per kernel evaluation) and
- * the near-field, self and small-argument (k|x-y| <= 8) entries in FP64.
+ * the near-field, self and small-argument (k|x-y| <= 4) entries in FP64.
  * Writes complex128 (out, ld) and its complex64 rounding (out32, ld32):
  * the residual and LU inputs of the mixed solver.  Requires k > 0. */
 int bem2d_discrete_kernel_mixed(bem2d_ctx* ctx, const bem2d_geometry* geom,

@@ -61,3 +61,42 @@ def test_against_libm(hk):
     r0 = np.abs(h0 - (f["j0"](x) + 1j * f["y0"](x))) / np.abs(h0)
     r1 = np.abs(h1 - (f["j1"](x) + 1j * f["y1"](x))) / np.abs(h1)
     assert r0.max() < 4e-15 and r1.max() < 4e-15, (r0.max(), r1.max())
+
+
+@pytest.fixture(scope="module")
+def hkff(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("hkff") / "libhkff.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=on",
+                    "-I" + os.path.join(ROOT, "bem2d_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "native", "hankel_ff_host.cpp"), "-o", out],
+                   check=True)
+    lib = ctypes.CDLL(out)
+
+    def f(x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        o = np.zeros((len(x), 4))
+        lib.hankel01_ff_host(ctypes.c_int(len(x)), x.ctypes.data_as(ctypes.c_void_p),
+                             o.ctypes.data_as(ctypes.c_void_p))
+        return o[:, 0] + 1j * o[:, 1], o[:, 2] + 1j * o[:, 3]
+    return f
+
+
+def test_float_float_against_mpmath(hkff):
+    """The float-float far-field evaluator (used from k|x - y| = 4 on) against
+    mpmath at 50 digits, on every interval of the piecewise fit and across
+    its joins (4, 8, 16, 64): relative error of H0 and H1 within 3e-14 plus
+    x * 2^-48 (x itself is held as a float-float, ~48 bits, so the phase
+    x - pi/4 carries an absolute error of that size)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    rng = np.random.default_rng(3)
+    x = np.concatenate([np.linspace(4.0, 8.0, 201), 10 ** rng.uniform(np.log10(4), 4, 600),
+                        np.linspace(7.99, 8.01, 11), np.linspace(15.99, 16.01, 11),
+                        np.linspace(63.99, 64.01, 11)])
+    h0, h1 = hkff(x)
+    r0 = np.array([complex(mp.hankel1(0, mp.mpf(float(v)))) for v in x])
+    r1 = np.array([complex(mp.hankel1(1, mp.mpf(float(v)))) for v in x])
+    bound = 3e-14 + x * 2.0 ** -48
+    e0 = np.abs(h0 - r0) / np.abs(r0) / bound
+    e1 = np.abs(h1 - r1) / np.abs(r1) / bound
+    assert e0.max() < 1 and e1.max() < 1, (e0.max(), e1.max())
