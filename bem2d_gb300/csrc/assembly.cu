@@ -253,6 +253,35 @@ near_fp64_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs,
       acc_re = fma(re, x * w, acc_re);
       acc_im = fma(im, x * w, acc_im);
     }
+  } else if (pr.rule == RULE_G3_PAIR) {
+    // (i, j) with AdaptedGauss3 at (x, y), (j, i) with its mirror
+    // AdaptedGauss2 at (y, x): the same point pairs, one evaluation each
+    double acc2_re = 0.0, acc2_im = 0.0;
+    for (int p = lane; p < r.n3; p += 32) {
+      const double x = r.r3[3 * p], y = r.r3[3 * p + 1], w = r.r3[3 * p + 2];
+      const ElemPt a = elem_eval(g.kind[e1], g.param + 8 * (size_t)e1, x);
+      const ElemPt b = elem_eval(g.kind[e2], g.param + 8 * (size_t)e2, y);
+      double n1x, n1y, n2x, n2y;
+      elem_normal(a, &n1x, &n1y);
+      elem_normal(b, &n2x, &n2y);
+      double r1, i1, r2, i2;
+      kernel_d_pair<KERNEL>(k, kq, eq, a.mx, a.my, b.mx, b.my, n1x, n1y, n2x, n2y, &r1, &i1,
+                            &r2, &i2);
+      const double f = basis_eval(g.unk_kind[pr.i], g.unk_param[pr.i], x) *
+                       basis_eval(g.unk_kind[pr.j], g.unk_param[pr.j], y) * elem_jac(a) *
+                       elem_jac(b) * w;
+      acc_re = fma(r1, f, acc_re);
+      acc_im = fma(i1, f, acc_im);
+      acc2_re = fma(r2, f, acc2_re);
+      acc2_im = fma(i2, f, acc2_im);
+    }
+    acc2_re = warp_sum(acc2_re);
+    acc2_im = warp_sum(acc2_im);
+    if (lane == 0) {
+      const double re = alpha * acc2_re, im = alpha * acc2_im;
+      out[(size_t)pr.i * ld + pr.j] = make_double2(re, im);
+      if (out32) out32[(size_t)pr.i * ld32 + pr.j] = make_float2((float)re, (float)im);
+    }
   } else {
     const double* rule = pr.rule == RULE_G2 ? r.r2 : r.r3;
     const int np = pr.rule == RULE_G2 ? r.n2 : r.n3;

@@ -326,7 +326,26 @@ static std::vector<NearPair> near_pairs(const bem2d_geometry* g) {
       for (int j : it->second) out.push_back(NearPair{i, j, rules[k], k == 0 ? 1 : 0});
     }
   }
-  return out;
+  // Pair each (i, j, G3) with its reverse (j, i, G2) when that exists: one
+  // warp then integrates both (the rules are mirror images), and the G2
+  // entry leaves the list.
+  std::unordered_map<long long, size_t> g2;
+  auto key = [](int a, int b) { return ((long long)a << 32) | (unsigned)b; };
+  for (size_t p = 0; p < out.size(); ++p)
+    if (out[p].rule == RULE_G2) g2[key(out[p].i, out[p].j)] = p;
+  std::vector<char> drop(out.size(), 0);
+  for (auto& pr : out) {
+    if (pr.rule != RULE_G3) continue;
+    auto it = g2.find(key(pr.j, pr.i));
+    if (it == g2.end() || drop[it->second]) continue;
+    pr.rule = RULE_G3_PAIR;
+    drop[it->second] = 1;
+  }
+  std::vector<NearPair> kept;
+  kept.reserve(out.size());
+  for (size_t p = 0; p < out.size(); ++p)
+    if (!drop[p]) kept.push_back(out[p]);
+  return kept;
 }
 
 static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, bool nodes,

@@ -184,8 +184,45 @@ __device__ __forceinline__ void kernel_d(double kk, double kq, double eq,
   }
 }
 
+// Both orientations of a pair at once: K(x, y) with the normal n1 at x and
+// n2 at y (re1, im1), and K(y, x) with the roles swapped (re2, im2).  One
+// distance and one Hankel evaluation serve both.
+template <int KERNEL>
+__device__ __forceinline__ void kernel_d_pair(double kk, double kq, double eq, double xx,
+                                              double xy, double yx, double yy, double n1x,
+                                              double n1y, double n2x, double n2y, double* re1,
+                                              double* im1, double* re2, double* im2) {
+  const double wx = xx - yx, wy = xy - yy;
+  const double d = sqrt(wx * wx + wy * wy);
+  double j0, y0, j1, y1;
+  hankel01_d(kk * d, &j0, &y0, &j1, &y1);
+  if (KERNEL == BEM2D_KERNEL_SINGLE) {
+    *re1 = *re2 = -0.25 * y0;
+    *im1 = *im2 = 0.25 * j0;
+  } else {
+    const double n1w = n1x * wx + n1y * wy, n2w = n2x * wx + n2y * wy;
+    // DoubleLayer: n_y . (y - x); the others: n_x . (x - y)
+    const double dot1 = (KERNEL == BEM2D_KERNEL_DOUBLE) ? -n2w : n1w;
+    const double dot2 = (KERNEL == BEM2D_KERNEL_DOUBLE) ? n1w : -n2w;
+    const double c1 = dot1 / d, c2 = dot2 / d;
+    *re1 = kq * c1 * y1;
+    *im1 = -kq * c1 * j1;
+    *re2 = kq * c2 * y1;
+    *im2 = -kq * c2 * j1;
+    if (KERNEL == BEM2D_KERNEL_COMBINED) {
+      *re1 = fma(eq, j0, *re1);
+      *im1 = fma(eq, y0, *im1);
+      *re2 = fma(eq, j0, *re2);
+      *im2 = fma(eq, y0, *im2);
+    }
+  }
+}
+
 // ---- near-pair rules -------------------------------------------------------
-enum NearRule : int { RULE_SELF = 0, RULE_G2 = 1, RULE_G3 = 2 };
+// RULE_G3_PAIR: the pair (i, j), j the next element of i, integrated with
+// AdaptedGauss3 together with its reverse (j, i), whose rule AdaptedGauss2
+// is the mirror image of AdaptedGauss3 ((x, y) -> (y, x), same weights).
+enum NearRule : int { RULE_SELF = 0, RULE_G2 = 1, RULE_G3 = 2, RULE_G3_PAIR = 3 };
 
 struct NearPair {
   int i;     // test unknown (row)
