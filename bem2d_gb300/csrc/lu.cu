@@ -273,24 +273,49 @@ __global__ void laswp_kernel(T* __restrict__ A, long long lda, int n,
 template <typename T>
 __global__ void __launch_bounds__(256)
 trsm_kernel(T* __restrict__ A, long long lda, int k0, int nb, int c0, int ncols) {
+  // U12 = L11^{-1} A12 for 32 columns per CTA, by blocks of 8 rows: warp w
+  // holds rows 8w..8w+7 of its lane's column in registers; block b is
+  // solved by warp b alone (8 steps in registers), then one __syncthreads
+  // and every warp below subtracts L[w-block, b-block] x_b: 8 barriers
+  // instead of one per row.
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* L = reinterpret_cast<T*>(smem_raw);  // [kNB][kNB] column-major
   T* X = L + kNB * kNB;                   // [kNB][32]: X[r*32 + c]
+  const T zero = CTraits<T>::make(0, 0);
   const int cb = c0 + blockIdx.x * 32;
   const int nc = min(32, c0 + ncols - cb);
-  for (int v = threadIdx.x; v < nb * nb; v += blockDim.x) {
-    const int s = v / nb, r = v - s * nb;
-    L[s * kNB + r] = A[(size_t)(k0 + s) * lda + k0 + r];
+  for (int v = threadIdx.x; v < kNB * kNB; v += blockDim.x) {
+    const int s = v >> 6, r = v & 63;
+    L[s * kNB + r] = (s < nb && r < nb) ? A[(size_t)(k0 + s) * lda + k0 + r] : zero;
   }
-  for (int v = threadIdx.x; v < nb * nc; v += blockDim.x) {
-    const int c = v / nb, r = v - c * nb;
-    X[r * 32 + c] = A[(size_t)(cb + c) * lda + k0 + r];
+  for (int v = threadIdx.x; v < kNB * 32; v += blockDim.x) {
+    const int c = v >> 6, r = v & 63;
+    X[r * 32 + c] = (c < nc && r < nb) ? A[(size_t)(cb + c) * lda + k0 + r] : zero;
   }
-  const int c = threadIdx.x & 31, rg = threadIdx.x >> 5;
-  for (int s = 0; s < nb; ++s) {
+  __syncthreads();
+  const int c = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T x[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = X[(8 * w + i) * 32 + c];
+  const int nbk = (nb + 7) >> 3;
+  for (int b = 0; b < nbk; ++b) {
+    if (w == b) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = i + 1; j < 8; ++j) x[j] = cfms(x[j], L[(8 * b + i) * kNB + 8 * b + j], x[i]);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) X[(8 * b + i) * 32 + c] = x[i];
+    }
     __syncthreads();
-    const T xs = X[s * 32 + c];
-    for (int r = s + 1 + rg; r < nb; r += 8) X[r * 32 + c] = cfms(X[r * 32 + c], L[s * kNB + r], xs);
+    if (w > b) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const T xb = X[(8 * b + j) * 32 + c];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = cfms(x[i], L[(8 * b + j) * kNB + 8 * w + i], xb);
+      }
+    }
   }
   __syncthreads();
   for (int v = threadIdx.x; v < nb * nc; v += blockDim.x) {
