@@ -95,6 +95,9 @@ __device__ __forceinline__ void entry_fp64(const NodeTable& t, int ng, int row, 
 }
 
 constexpr int kTileF = 32;
+constexpr int kDeferRC = 1 << 30;  // deferred item: entry (row, col) wanted
+constexpr int kDeferCR = 1 << 29;  // deferred item: entry (col, row) wanted
+constexpr int kDeferIdx = kDeferCR - 1;
 constexpr int kFarFFThreads = 256;
 constexpr float kDeferX = 4.001f;
 
@@ -194,14 +197,15 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
     const float dist = sqrtf((float)(dxc * dxc + dyc * dyc));
     if (kf * (dist * (1.0f - 1e-6f) - rrow - rad[kTileF + cc]) <= kDeferX) {
       // small arguments somewhere on this pair: FP64 pass (or here, if the
-      // list is full)
-      for (int dir = 0; dir < 2; ++dir) {
-        if (!(dir == 0 ? rc : cr)) continue;
-        const int a = dir == 0 ? row : col, b = dir == 0 ? col : row;
-        const unsigned slot = atomicAdd(dl.count, 1u);
-        if (slot < dl.capacity) {
-          dl.ij[slot] = make_int2(a, b);
-        } else {
+      // list is full).  One list item per pair: (row, col) with the flags
+      // kDeferRC / kDeferCR in the top bits of .x for the directions needed.
+      const unsigned slot = atomicAdd(dl.count, 1u);
+      if (slot < dl.capacity) {
+        dl.ij[slot] = make_int2(row | (rc ? kDeferRC : 0) | (cr ? kDeferCR : 0), col);
+      } else {
+        for (int dir = 0; dir < 2; ++dir) {
+          if (!(dir == 0 ? rc : cr)) continue;
+          const int a = dir == 0 ? row : col, b = dir == 0 ? col : row;
           double re, im;
           entry_fp64<KERNEL>(t, ng, a, b, k, 0.25 * k, 0.25 * eta, &re, &im);
           out[(size_t)b * ld + a] = make_double2(alpha * re, alpha * im);
@@ -284,15 +288,38 @@ __global__ void deferred_fp64_kernel(NodeTable t, int ng, double k, double eta, 
                                      const int2* __restrict__ ij, const unsigned* count,
                                      unsigned cap, double2* __restrict__ out, long long ld,
                                      float2* __restrict__ out32, long long ld32) {
+  // one item = one element pair; both orientations share every distance
+  // and Hankel evaluation
   const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= min(*count, cap)) return;
   const int2 e = ij[p];
-  double re, im;
-  entry_fp64<KERNEL>(t, ng, e.x, e.y, k, 0.25 * k, 0.25 * eta, &re, &im);
-  re *= alpha;
-  im *= alpha;
-  out[(size_t)e.y * ld + e.x] = make_double2(re, im);
-  out32[(size_t)e.y * ld32 + e.x] = make_float2((float)re, (float)im);
+  const int row = e.x & kDeferIdx, col = e.y;
+  const bool want_rc = (e.x & kDeferRC) != 0, want_cr = (e.x & kDeferCR) != 0;
+  const double kq = 0.25 * k, eq = 0.25 * eta;
+  double r1 = 0.0, i1 = 0.0, r2 = 0.0, i2 = 0.0;
+  for (int q1 = 0; q1 < ng; ++q1) {
+    const size_t a = (size_t)row * ng + q1;
+    const double x1 = t.x[a], y1 = t.y[a], n1x = t.nx[a], n1y = t.ny[a], w1 = t.w[a];
+    for (int q2 = 0; q2 < ng; ++q2) {
+      const size_t b = (size_t)col * ng + q2;
+      double vr1, vi1, vr2, vi2;
+      kernel_d_pair<KERNEL>(k, kq, eq, x1, y1, t.x[b], t.y[b], n1x, n1y, t.nx[b], t.ny[b], &vr1,
+                            &vi1, &vr2, &vi2);
+      const double ww = w1 * t.w[b];
+      r1 = fma(vr1, ww, r1);
+      i1 = fma(vi1, ww, i1);
+      r2 = fma(vr2, ww, r2);
+      i2 = fma(vi2, ww, i2);
+    }
+  }
+  if (want_rc) {
+    out[(size_t)col * ld + row] = make_double2(alpha * r1, alpha * i1);
+    out32[(size_t)col * ld32 + row] = make_float2((float)(alpha * r1), (float)(alpha * i1));
+  }
+  if (want_cr) {
+    out[(size_t)row * ld + col] = make_double2(alpha * r2, alpha * i2);
+    out32[(size_t)row * ld32 + col] = make_float2((float)(alpha * r2), (float)(alpha * i2));
+  }
 }
 
 // Device copy of the e^{i x} reduction table, made once per device (the
