@@ -746,6 +746,9 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
   const double accept = std::max(tol, 1e-12);
   float2* LU = static_cast<float2*>(ws(c, "lu32", sizeof(float2) * (size_t)n * n, &rc));
   if (!LU) return rc;
+  w.pack_bytes = lu_pack_bytes(n);
+  w.pack = ws(c, "lu_pack", w.pack_bytes, &rc);
+  if (!w.pack) return rc;
   double2* r = static_cast<double2*>(ws(c, "ir_r", sizeof(double2) * n, &rc));
   float2* d = static_cast<float2*>(ws(c, "ir_d", sizeof(float2) * n, &rc));
   double2* part = static_cast<double2*>(ws(c, "ir_part", residual_part_bytes(n), &rc));

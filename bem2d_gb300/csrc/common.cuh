@@ -324,6 +324,10 @@ struct LuWork {
   void* scratch;         // panel exchange slots (lu_scratch_bytes)
   size_t scratch_bytes;
   int* perm;             // [n] row permutation of the pivots (filled by lu_factor)
+  // workspace of the complex64 tensor-core update (lu_pack_bytes(n)); null:
+  // the update runs on the CUDA cores
+  void* pack = nullptr;
+  size_t pack_bytes = 0;
   void* dinv;            // inverses of the 64 x 64 diagonal blocks of L and U
 };
 
@@ -331,6 +335,8 @@ struct LuWork {
 size_t lu_scratch_bytes(int n);
 // Bytes of perm + dinv for n unknowns of `elem` bytes each.
 size_t lu_aux_bytes(int n, size_t elem);
+// Bytes of LuWork::pack for a complex64 factorisation of order n.
+size_t lu_pack_bytes(int n);
 
 // LU with partial pivoting in place; T = double2 (complex128) or float2.
 // Also fills w.perm and w.dinv for lu_solve.
@@ -350,9 +356,11 @@ int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T
 // C -= A B for complex64 column-major operands on the tensor cores
 // (tcgen05 kind::tf32, 3xTF32 split; lu_tc.cu).  C is M x N, A M x K, B K x N.
 // Sets *status on a device-side wait timeout.
+// `pack` (tc_pack_bytes(M, N, K) bytes) holds the split, re-laid-out operands.
+size_t tc_pack_bytes(int M, int N, int K);
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
-                        const float2* B, long long ldb, int M, int N, int K, int* status,
-                        cudaStream_t s);
+                        const float2* B, long long ldb, int M, int N, int K, void* pack,
+                        size_t pack_bytes, int* status, cudaStream_t s);
 
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);

@@ -1085,6 +1085,10 @@ __global__ void __launch_bounds__(128) dinv_kernel(const T* __restrict__ LU, lon
   }
 }
 
+size_t lu_pack_bytes(int n) {
+  return tc_pack_bytes(n, n, n >= kOuterMinN ? kOuterNB : kNB);
+}
+
 size_t lu_aux_bytes(int n, size_t elem) {
   const size_t nk = (n + kNB - 1) / kNB;
   return sizeof(int) * (size_t)n + 2 * nk * kNB * kNB * elem + 256;
@@ -1101,11 +1105,16 @@ static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N
   if constexpr (sizeof(T) == sizeof(float2)) {
     if (M >= kTensorMinN && N >= kTensorMinN) {
       ++*launches;
-      return launch_tc_cgemm_sub(reinterpret_cast<float2*>(C), ld,
-                                 reinterpret_cast<const float2*>(Am), ld,
-                                 reinterpret_cast<const float2*>(Bm), ld, M, N, K, w.status, s)
-                 ? BEM2D_ERR_CUDA
-                 : BEM2D_OK;
+      if (w.pack && tc_pack_bytes(M, N, K) <= w.pack_bytes) {
+        *launches += 2;  // + the two packing kernels
+        return launch_tc_cgemm_sub(reinterpret_cast<float2*>(C), ld,
+                                   reinterpret_cast<const float2*>(Am), ld,
+                                   reinterpret_cast<const float2*>(Bm), ld, M, N, K, w.pack,
+                                   w.pack_bytes, w.status, s)
+                   ? BEM2D_ERR_CUDA
+                   : BEM2D_OK;
+      }
+      --*launches;
     }
   }
   dim3 g((M + kGB - 1) / kGB, (N + kGB - 1) / kGB);

@@ -10,8 +10,7 @@
 //   re C_i = D1[2i] - D2[2i+1],   im C_i = D2[2i] + D1[2i+1].
 // One CTA owns a tile of 64 complex rows (128 real rows = the MMA's M) and
 // 64 complex columns (the MMA's N); D1 and D2 take 64 tensor-memory columns
-// each.  K is staged 32 at a time (64 KB of shared memory), so three CTAs
-// share an SM and one CTA's epilogue overlaps another's staging and MMAs.
+// each.
 //
 // Accuracy (3xTF32): every FP32 operand x is split into hi = x with its low
 // 13 mantissa bits cleared (exactly a TF32 value) and lo = x - hi; each
@@ -19,15 +18,21 @@
 // per product - the accuracy of the FP32 update it replaces, so the LU keeps
 // the quality the FP64 refinement expects.
 //
-// Operands are staged by the CTA's threads (global -> split -> shared memory)
-// in the K-major, non-swizzled canonical layout: core matrices of 8 rows x
-// 16 bytes; 128 bytes from one core matrix to the next along K (leading
-// byte offset), 1024 bytes from one group of 8 rows to the next (stride
-// byte offset).  One thread issues the MMAs; tcgen05.commit signals an
-// mbarrier that the others wait on (bounded: on timeout the status flag is
-// set and the tile is left unchanged).  The epilogue reads D1/D2 with
-// tcgen05.ld (warp w reads lanes 32w..32w+31 = real rows), combines rows
-// 2i/2i+1 with one shuffle and updates C in place.
+// Operands are packed once per update (pack_a_kernel, pack_b_kernel): split
+// into hi/lo and laid out, per tile and per chunk of 16 along K, exactly as
+// the MMA reads them from shared memory - the K-major, non-swizzled
+// canonical layout (core matrices of 8 rows x 16 bytes, 128 bytes from one
+// core matrix to the next along K, 512 bytes from one group of 8 rows to the
+// next).  The update kernel then stages each chunk with two bulk copies
+// (cp.async.bulk, completion counted in bytes on an mbarrier) into one of two
+// shared-memory stages, so the copy of chunk c + 1 overlaps the MMAs of
+// chunk c.  One thread issues the copies and the MMAs; tcgen05.commit
+// signals an mbarrier when a stage's MMAs are done (the stage may then be
+// refilled) and, at the end, that the accumulators are complete.  Every wait
+// is bounded: on timeout the status flag is set and the tile is left
+// unchanged.  The epilogue reads D1/D2 with tcgen05.ld (warp w reads lanes
+// 32w..32w+31 = real rows), combines rows 2i/2i+1 with one shuffle and
+// updates C in place.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -37,13 +42,16 @@ namespace {
 
 constexpr int kTcBM = 64;   // complex rows per tile (128 real rows = MMA M)
 constexpr int kTcBN = 64;   // complex columns per tile (MMA N)
-constexpr int kTcBK = 32;   // K per staged chunk
+constexpr int kTcBK = 16;   // K per chunk (two MMAs of K = 8)
 constexpr int kTcThreads = 128;
-constexpr int kCoreBytes = 128;                      // 8 rows x 16 bytes
-constexpr int kTcSBO = (kTcBK / 4) * kCoreBytes;     // 1024
-constexpr int kTcAbytes = 2 * kTcBM * kTcBK * 4;     // 16 KB per split part
-constexpr int kTcBbytes = kTcBN * kTcBK * 4;         // 8 KB per part
-constexpr int kTcSmem = 2 * kTcAbytes + 4 * kTcBbytes + 64;
+constexpr int kCoreBytes = 128;                   // 8 rows x 16 bytes
+constexpr int kTcSBO = (kTcBK / 4) * kCoreBytes;  // 512
+constexpr int kTcApart = 2 * kTcBM * kTcBK * 4;   // 8 KB: 128 real rows x 16
+constexpr int kTcBpart = kTcBN * kTcBK * 4;       // 4 KB: 64 rows x 16
+constexpr int kTcChunkA = 2 * kTcApart;           // hi, lo
+constexpr int kTcChunkB = 4 * kTcBpart;           // re hi, re lo, im hi, im lo
+constexpr int kTcStage = kTcChunkA + kTcChunkB;   // 32 KB
+constexpr int kTcSmem = 2 * kTcStage + 64;
 constexpr unsigned kTcSpin = 1u << 24;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -55,8 +63,8 @@ __device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
          ((unsigned long long)(kCoreBytes >> 4) << 16) |
          ((unsigned long long)(kTcSBO >> 4) << 32) | (1ull << 46);
 }
-// byte offset of (row r, k) in the canonical layout
-__device__ __forceinline__ int kmajor_off(int r, int k) {
+// byte offset of (row r, k) inside one packed chunk
+__host__ __device__ __forceinline__ int kmajor_off(int r, int k) {
   return (r >> 3) * kTcSBO + (k >> 2) * kCoreBytes + (r & 7) * 16 + (k & 3) * 4;
 }
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
@@ -72,6 +80,33 @@ __device__ __forceinline__ void mma_tf32(unsigned d, unsigned a, unsigned b, uns
       "l"(smem_desc(a)), "l"(smem_desc(b)), "r"(idesc), "r"(acc));
 }
 
+__device__ __forceinline__ void mbar_init(unsigned long long* m) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(m)));
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* m, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)),
+               "r"(bytes));
+}
+// bounded wait for phase `parity` of the mbarrier; false on timeout
+__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity) {
+  unsigned done = 0;
+  for (unsigned it = 0; it < kTcSpin && !done; ++it)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(m)), "r"(parity));
+  return done != 0;
+}
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes,
+                                          unsigned long long* m) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(m))
+      : "memory");
+}
+
 #define TC_LD16(dst, addr)                                                                  \
   asm volatile(                                                                             \
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
@@ -81,29 +116,75 @@ __device__ __forceinline__ void mma_tf32(unsigned d, unsigned a, unsigned b, uns
         "=r"(dst[12]), "=r"(dst[13]), "=r"(dst[14]), "=r"(dst[15])                          \
       : "r"(addr))
 
+// ---- packing ---------------------------------------------------------------
+// A (M x K complex) -> Apk[mt][kc] = {hi, lo} chunks of kTcApart bytes each.
+// grid: (ceil(M / 64) * 64 / 128 x nkc * 16), 128 threads
+__global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int nkc,
+                              unsigned char* __restrict__ Apk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;  // complex row
+  const int k = blockIdx.y;                             // 0 .. nkc * 16 - 1
+  const int mt = i / kTcBM, il = i - mt * kTcBM;
+  const int kc = k / kTcBK, kl = k - kc * kTcBK;
+  if (i >= ((M + kTcBM - 1) / kTcBM) * kTcBM) return;
+  const float2 v = (i < M && k < K) ? A[(size_t)k * lda + i] : make_float2(0.f, 0.f);
+  unsigned char* chunk = Apk + ((size_t)mt * nkc + kc) * kTcChunkA;
+  float h, l;
+  tf32_split(v.x, h, l);
+  *reinterpret_cast<float*>(chunk + kmajor_off(2 * il, kl)) = h;
+  *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il, kl)) = l;
+  tf32_split(v.y, h, l);
+  *reinterpret_cast<float*>(chunk + kmajor_off(2 * il + 1, kl)) = h;
+  *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il + 1, kl)) = l;
+}
+
+// B (K x N complex) -> Bpk[nt][kc] = {re hi, re lo, im hi, im lo} chunks.
+// grid: (ceil(N / 64) * 64 x ceil(nkc * 16 / 64)), 64 threads
+__global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int nkc,
+                              unsigned char* __restrict__ Bpk) {
+  const int n = blockIdx.x;                             // complex column
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;  // 0 .. nkc * 16 - 1
+  if (k >= nkc * kTcBK) return;
+  const int nt = n / kTcBN, nl = n - nt * kTcBN;
+  const int kc = k / kTcBK, kl = k - kc * kTcBK;
+  const float2 v = (k < K && n < N) ? B[(size_t)n * ldb + k] : make_float2(0.f, 0.f);
+  unsigned char* chunk = Bpk + ((size_t)nt * nkc + kc) * kTcChunkB;
+  const int off = kmajor_off(nl, kl);
+  float h, l;
+  tf32_split(v.x, h, l);
+  *reinterpret_cast<float*>(chunk + off) = h;
+  *reinterpret_cast<float*>(chunk + kTcBpart + off) = l;
+  tf32_split(v.y, h, l);
+  *reinterpret_cast<float*>(chunk + 2 * kTcBpart + off) = h;
+  *reinterpret_cast<float*>(chunk + 3 * kTcBpart + off) = l;
+}
+
+// ---- the update --------------------------------------------------------------
+// grid (ceil(M / 64), ceil(N / 64)), 128 threads, kTcSmem bytes of shared memory
 __global__ void __launch_bounds__(kTcThreads, 3)
-tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const float2* __restrict__ A,
-                    long long lda, const float2* __restrict__ B, long long ldb, int M, int N,
-                    int K, int* status) {
+tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* __restrict__ Apk,
+                    const unsigned char* __restrict__ Bpk, int M, int N, int nkc, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char* Ahi = sm;
-  unsigned char* Alo = sm + kTcAbytes;
-  unsigned char* Brh = sm + 2 * kTcAbytes;
-  unsigned char* Brl = Brh + kTcBbytes;
-  unsigned char* Bih = Brl + kTcBbytes;
-  unsigned char* Bil = Bih + kTcBbytes;
-  unsigned long long* mbar = reinterpret_cast<unsigned long long*>(Bil + kTcBbytes);
-  unsigned* tslot = reinterpret_cast<unsigned*>(mbar + 1);
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(sm + 2 * kTcStage);
+  unsigned long long* done = full + 2;
+  unsigned* tslot = reinterpret_cast<unsigned*>(done + 2);
+  int* s_ok = reinterpret_cast<int*>(tslot + 1);
   const int t = threadIdx.x, w = t >> 5;
-  const int i0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
+  const int mt = blockIdx.x, nt = blockIdx.y;
+  const int i0 = mt * kTcBM, n0 = nt * kTcBN;
+  const unsigned char* asrc = Apk + (size_t)mt * nkc * kTcChunkA;
+  const unsigned char* bsrc = Bpk + (size_t)nt * nkc * kTcChunkB;
   if (w == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
         smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+    mbar_init(&full[0]);
+    mbar_init(&full[1]);
+    mbar_init(&done[0]);
+    mbar_init(&done[1]);
     asm volatile("fence.mbarrier_init.release.cluster;");
+    *s_ok = 1;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -113,101 +194,59 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const float2* __restr
   // K-major, N >> 3 at bit 17, M >> 4 at bit 24
   const unsigned idesc =
       (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kTcBN >> 3) << 17) | ((128u >> 4) << 24);
-  unsigned phase = 0;
-  bool timeout = false;
-  for (int kb = 0; kb < K; kb += kTcBK) {
-    // Stage A: a warp covers 4 complex rows x 4 k, both components, so its
-    // 32 stores fill one 128-byte line of core matrices (no bank conflict);
-    // loads are batched 16 deep.
-    {
-      const int l = t & 31;
-      const int ci = (l >> 2) & 1, kl = l & 3, il = l >> 3;
-      const float* Af = reinterpret_cast<const float*>(A);
-      for (int j0 = 0; j0 < kTcBM * kTcBK * 2 / kTcThreads; j0 += 16) {
-        float v[16];
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int b = w + 4 * (j0 + u);
-          const int i = (b & 15) * 4 + il, k = (b >> 4) * 4 + kl;
-          v[u] = (i0 + i < M && kb + k < K) ? Af[2 * ((size_t)(kb + k) * lda + i0 + i) + ci] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int b = w + 4 * (j0 + u);
-          const int i = (b & 15) * 4 + il, k = (b >> 4) * 4 + kl;
-          const int off = kmajor_off(2 * i + ci, k);
-          float h, lo;
-          tf32_split(v[u], h, lo);
-          *reinterpret_cast<float*>(Ahi + off) = h;
-          *reinterpret_cast<float*>(Alo + off) = lo;
-        }
+  if (t == 0) {
+    // chunk c goes to stage c & 1: A (hi, lo) and B (four parts) are each
+    // one contiguous block in the packed operands
+    auto issue = [&](int c) {
+      unsigned char* st = sm + (c & 1) * kTcStage;
+      mbar_expect_tx(&full[c & 1], kTcStage);
+      bulk_copy(st, asrc + (size_t)c * kTcChunkA, kTcChunkA, &full[c & 1]);
+      bulk_copy(st + kTcChunkA, bsrc + (size_t)c * kTcChunkB, kTcChunkB, &full[c & 1]);
+    };
+    issue(0);
+    if (nkc > 1) issue(1);
+    const unsigned d1 = tmem, d2 = tmem + kTcBN;
+    for (int c = 0; c < nkc; ++c) {
+      const int s = c & 1;
+      const unsigned ph = (c >> 1) & 1;
+      if (!mbar_wait(&full[s], ph)) {
+        *s_ok = 0;
+        break;
       }
-    }
-    // Stage B: a warp covers 8 columns n x 4 k (one line per part)
-    {
-      const int l = t & 31;
-      const int kl = l & 3, nl = l >> 2;
-      for (int j0 = 0; j0 < kTcBN * kTcBK / kTcThreads; j0 += 16) {
-        float2 v[16];
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int b = w + 4 * (j0 + u);
-          const int n = (b & 7) * 8 + nl, k = (b >> 3) * 4 + kl;
-          v[u] = (n0 + n < N && kb + k < K) ? B[(size_t)(n0 + n) * ldb + kb + k]
-                                             : make_float2(0.f, 0.f);
-        }
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int b = w + 4 * (j0 + u);
-          const int n = (b & 7) * 8 + nl, k = (b >> 3) * 4 + kl;
-          const int off = kmajor_off(n, k);
-          float h, lo;
-          tf32_split(v[u].x, h, lo);
-          *reinterpret_cast<float*>(Brh + off) = h;
-          *reinterpret_cast<float*>(Brl + off) = lo;
-          tf32_split(v[u].y, h, lo);
-          *reinterpret_cast<float*>(Bih + off) = h;
-          *reinterpret_cast<float*>(Bil + off) = lo;
-        }
-      }
-    }
-    asm volatile("fence.proxy.async.shared::cta;");
-    __syncthreads();
-    if (t == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const unsigned d1 = tmem, d2 = tmem + kTcBN;
-      for (int s = 0; s < kTcBK / 8; ++s) {
-        const unsigned o = 256u * s;  // K = 8 tf32 = two core matrices
-        const unsigned ah = smem_u32(Ahi) + o, al = smem_u32(Alo) + o;
-        const unsigned acc = (kb == 0 && s == 0) ? 0u : 1u;
-        mma_tf32(d1, ah, smem_u32(Brh) + o, idesc, acc);
-        mma_tf32(d1, ah, smem_u32(Brl) + o, idesc, 1u);
-        mma_tf32(d1, al, smem_u32(Brh) + o, idesc, 1u);
-        mma_tf32(d2, ah, smem_u32(Bih) + o, idesc, acc);
-        mma_tf32(d2, ah, smem_u32(Bil) + o, idesc, 1u);
-        mma_tf32(d2, al, smem_u32(Bih) + o, idesc, 1u);
+      const unsigned base = smem_u32(sm + s * kTcStage);
+      const unsigned ah = base, al = base + kTcApart;
+      const unsigned brh = base + kTcChunkA, brl = brh + kTcBpart;
+      const unsigned bih = brh + 2 * kTcBpart, bil = brh + 3 * kTcBpart;
+#pragma unroll
+      for (int ks = 0; ks < kTcBK / 8; ++ks) {
+        const unsigned o = 256u * ks;  // K = 8 tf32 = two core matrices
+        const unsigned acc = (c == 0 && ks == 0) ? 0u : 1u;
+        mma_tf32(d1, ah + o, brh + o, idesc, acc);
+        mma_tf32(d1, ah + o, brl + o, idesc, 1u);
+        mma_tf32(d1, al + o, brh + o, idesc, 1u);
+        mma_tf32(d2, ah + o, bih + o, idesc, acc);
+        mma_tf32(d2, ah + o, bil + o, idesc, 1u);
+        mma_tf32(d2, al + o, bih + o, idesc, 1u);
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(mbar)));
-    }
-    unsigned done = 0;
-    for (unsigned it = 0; it < kTcSpin && !done; ++it)
-      asm volatile(
-          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-          " selp.u32 %0, 1, 0, p;\n}\n"
-          : "=r"(done)
-          : "r"(smem_u32(mbar)), "r"(phase));
-    if (!done) timeout = true;
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    __syncthreads();  // the operands may be restaged
-    if (__syncthreads_or(timeout)) {
-      timeout = true;
-      break;
+              smem_u32(&done[s])));
+      if (c + 2 < nkc) {  // refill this stage once its MMAs have read it
+        if (!mbar_wait(&done[s], ph)) {
+          *s_ok = 0;
+          break;
+        }
+        issue(c + 2);
+      }
     }
   }
-  if (timeout) {
+  __syncthreads();
+  // the last commit covers every MMA of the tile
+  bool ok = *s_ok != 0;
+  if (ok) ok = mbar_wait(&done[(nkc - 1) & 1], ((nkc - 1) >> 1) & 1);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (__syncthreads_or(!ok)) {
     if (t == 0) atomicExch(status, 1);
   } else {
     const int i = t >> 1, c = t & 1;  // real row t = 2i + c
@@ -221,14 +260,14 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const float2* __restr
         const int n = n0 + j0 + u;
         cv[u] = (row_ok && n < N) ? Cf[2 * ((size_t)n * ldc + i0 + i) + c] : 0.f;
       }
-      unsigned d1[16], d2[16];
-      TC_LD16(d1, lanes + j0);
-      TC_LD16(d2, lanes + kTcBN + j0);
+      unsigned dv1[16], dv2[16];
+      TC_LD16(dv1, lanes + j0);
+      TC_LD16(dv2, lanes + kTcBN + j0);
       asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
       for (int u = 0; u < 16; ++u) {
-        const float p2 = __shfl_xor_sync(0xffffffffu, __uint_as_float(d2[u]), 1);
-        const float o = __uint_as_float(d1[u]) + (c ? p2 : -p2);
+        const float p2 = __shfl_xor_sync(0xffffffffu, __uint_as_float(dv2[u]), 1);
+        const float o = __uint_as_float(dv1[u]) + (c ? p2 : -p2);
         const int n = n0 + j0 + u;
         if (row_ok && n < N) Cf[2 * ((size_t)n * ldc + i0 + i) + c] = cv[u] - o;
       }
@@ -241,17 +280,33 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const float2* __restr
 
 #undef TC_LD16
 
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
 }  // namespace
 
+size_t tc_pack_bytes(int M, int N, int K) {
+  const size_t nkc = (size_t)(K + kTcBK - 1) / kTcBK;
+  const size_t mt = (size_t)(M + kTcBM - 1) / kTcBM, nt = (size_t)(N + kTcBN - 1) / kTcBN;
+  return align256(mt * nkc * kTcChunkA) + align256(nt * nkc * kTcChunkB);
+}
+
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
-                        const float2* B, long long ldb, int M, int N, int K, int* status,
-                        cudaStream_t s) {
+                        const float2* B, long long ldb, int M, int N, int K, void* pack,
+                        size_t pack_bytes, int* status, cudaStream_t s) {
   static const cudaError_t attr = cudaFuncSetAttribute(
       tc_cgemm_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (attr != cudaSuccess) return BEM2D_ERR_CUDA;
   if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
-  dim3 grid((M + kTcBM - 1) / kTcBM, (N + kTcBN - 1) / kTcBN);
-  tc_cgemm_sub_kernel<<<grid, kTcThreads, kTcSmem, s>>>(C, ldc, A, lda, B, ldb, M, N, K, status);
+  if (!pack || tc_pack_bytes(M, N, K) > pack_bytes) return BEM2D_ERR_ARG;
+  const int nkc = (K + kTcBK - 1) / kTcBK;
+  const int mt = (M + kTcBM - 1) / kTcBM, nt = (N + kTcBN - 1) / kTcBN;
+  unsigned char* Apk = static_cast<unsigned char*>(pack);
+  unsigned char* Bpk = Apk + align256((size_t)mt * nkc * kTcChunkA);
+  pack_a_kernel<<<dim3((mt * kTcBM + 127) / 128, nkc * kTcBK), 128, 0, s>>>(A, lda, M, K, nkc,
+                                                                            Apk);
+  pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc, Bpk);
+  tc_cgemm_sub_kernel<<<dim3(mt, nt), kTcThreads, kTcSmem, s>>>(C, ldc, Apk, Bpk, M, N, nkc,
+                                                                status);
   return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
 }
 
