@@ -1103,7 +1103,8 @@ static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N
                       const LuWork& w, cudaStream_t s, long long* launches) {
   if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
   if constexpr (sizeof(T) == sizeof(float2)) {
-    if (M >= kTensorMinN && N >= kTensorMinN) {
+    // tall and narrow updates (the columns inside an outer block) too
+    if ((M >= kTensorMinN && N >= kTensorMinN) || (M >= 4 * kTensorMinN && N >= kNB)) {
       ++*launches;
       if (w.pack && tc_pack_bytes(M, N, K) <= w.pack_bytes) {
         *launches += 2;  // + the two packing kernels
@@ -1379,9 +1380,83 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
   for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[r0 + i] = bc[i];
 }
 
+// ---- grid-wide triangular solves (large n) -----------------------------------
+// One launch per 64-row block step.  Every CTA forms y = D^{-1} x_k from the
+// stored inverse of the diagonal block (64 x 64, redundantly: 4096 complex
+// multiply-adds) and subtracts L[rows, k] y (U[rows, k] y going back) from
+// its own 256 rows; CTA 0 also writes y to the output.  The trailing rows
+// are spread over all SMs, so the factor streams at full memory bandwidth;
+// the kernel boundary orders the steps.
+constexpr int kGridSolveThreads = 256;
+constexpr int kGridSolveMinN = 8192;  // below: the single-cluster solve (fewer launches)
+
+template <typename T>
+__global__ void perm_gather_kernel(int n, const int* __restrict__ perm, const T* __restrict__ b,
+                                   T* __restrict__ u) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) u[r] = b[perm[r]];
+}
+
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(kGridSolveThreads)
+trisolve_step_kernel(const T* __restrict__ LU, long long lda, int n, const T* __restrict__ dinv,
+                     int kb, T* __restrict__ work, T* __restrict__ out) {
+  __shared__ T y[kNB];
+  __shared__ T xk[kNB];
+  const int k0 = kb * kNB, nb = min(kNB, n - k0);
+  const T zero = CTraits<T>::make(0, 0);
+  if ((int)threadIdx.x < nb) xk[threadIdx.x] = work[k0 + threadIdx.x];
+  __syncthreads();
+  if ((int)threadIdx.x < nb) {
+    const T* Di = dinv + (size_t)(2 * kb + (FWD ? 0 : 1)) * kNB * kNB;
+    const int i = threadIdx.x;
+    T acc = zero;
+    for (int j = 0; j < nb; ++j) acc = cfma(Di[j * kNB + i], xk[j], acc);
+    y[i] = acc;
+    if (blockIdx.x == 0) out[k0 + i] = acc;
+  }
+  __syncthreads();
+  // rows below the block (forward) or above it (backward)
+  const int lo = FWD ? k0 + nb : 0, hi = FWD ? n : k0;
+  const int r = lo + blockIdx.x * kGridSolveThreads + threadIdx.x;
+  if (r >= hi) return;
+  const T* col = LU + (size_t)k0 * lda + r;
+  T acc = zero;
+#pragma unroll 16
+  for (int j = 0; j < nb; ++j) acc = cfma(col[(size_t)j * lda], y[j], acc);
+  T v = work[r];
+  v.x -= acc.x;
+  v.y -= acc.y;
+  work[r] = v;
+}
+
+template <typename T>
+static int lu_solve_grid(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+                         cudaStream_t s, long long* launches) {
+  if (w.scratch_bytes < sizeof(T) * 2 * (size_t)n) return BEM2D_ERR_ARG;
+  T* u = static_cast<T*>(w.scratch);  // permuted right-hand side, updated in place
+  T* v = u + n;                       // forward result, updated in place going back
+  const int nk = (n + kNB - 1) / kNB;
+  perm_gather_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(n, w.perm, b, u);
+  const T* dinv = reinterpret_cast<const T*>(w.dinv);
+  for (int kb = 0; kb < nk; ++kb) {
+    const int rows = n - std::min(n, (kb + 1) * kNB);
+    const int g = std::max(1, (rows + kGridSolveThreads - 1) / kGridSolveThreads);
+    trisolve_step_kernel<T, true><<<g, kGridSolveThreads, 0, s>>>(LU, lda, n, dinv, kb, u, v);
+  }
+  for (int kb = nk - 1; kb >= 0; --kb) {
+    const int rows = kb * kNB;
+    const int g = std::max(1, (rows + kGridSolveThreads - 1) / kGridSolveThreads);
+    trisolve_step_kernel<T, false><<<g, kGridSolveThreads, 0, s>>>(LU, lda, n, dinv, kb, v, x);
+  }
+  *launches += 1 + 2 * nk;
+  return BEM2D_OK;
+}
+
 template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
              cudaStream_t s, long long* launches) {
+  if (n >= kGridSolveMinN) return lu_solve_grid(LU, lda, n, w, b, x, s, launches);
   static std::atomic<int> cmax{kMaxCluster};
   static std::once_flag attr;
   std::call_once(attr, [] {

@@ -72,3 +72,28 @@ def test_repeat_calls_reuse_workspace(ctx):
     for n in (400, 100, 400):
         A, b = rand_system(n, 100 + n)
         assert rel(ctx.solve(A, b, "fp64"), np.linalg.solve(A, b)) < 1e-12
+
+
+def test_large_order_grid_solve():
+    """n = 8200 uses the grid-wide triangular solves (n >= 8192): residual
+    ||b - A x|| / (||A||_F ||x|| + ||b||) at FP64 roundoff for both
+    precisions, inputs and outputs on the device."""
+    torch = pytest.importorskip("torch")
+    from bem2d_gb300 import capi
+    n = 8200
+    g = torch.Generator(device="cuda").manual_seed(8200)
+    A = torch.randn((n, n), dtype=torch.complex128, device="cuda", generator=g)
+    A += 2 * n ** 0.5 * torch.eye(n, dtype=torch.complex128, device="cuda")
+    b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    At = A.T.contiguous().T  # column-major view of A
+    ctx = capi.Context(0)
+    try:
+        for prec, bound in (("fp64", 1e-13), ("mixed", 1e-13)):
+            x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+            ctx.solve(At, b, prec, out=x)
+            r = torch.linalg.vector_norm(b - A @ x)
+            berr = float(r / (torch.linalg.matrix_norm(A) * torch.linalg.vector_norm(x) +
+                              torch.linalg.vector_norm(b)))
+            assert berr < bound, (prec, berr)
+    finally:
+        ctx.close()
