@@ -6,14 +6,20 @@
 //                     Gauss rule (Integrate<kernel,Gauss2D>,
 //                     lib/bem2d_quadrature.h:37-65, selected for non-adjacent
 //                     elements at :283-287); coalesced column-major stores
-//  near_fp64_kernel   one warp per self/adjacent pair: graded rules
+//  near_kernel        one warp per self/adjacent pair: graded rules
 //                     (IntegrateIdent :67-109 with AdaptedGauss1; Integrate
 //                     with AdaptedGauss3 / AdaptedGauss2 for next / prev,
-//                     :271-282), fused  alpha*K + beta*M  epilogue
+//                     :271-282), fused  alpha*K + beta*M  epilogue; element
+//                     geometry tabulated per warp at the rules' distinct
+//                     coordinates; the mixed-precision variant evaluates
+//                     the Bessel functions in float-float
 //  ident_kernel       EvalIdent (lib/bem2d_quadrature.cpp:79-127)
 //  rhs_kernel         DotProdBasFuns (lib/bem2d_quadrature.h:111-156)
+#include <algorithm>
+
 #include "common.cuh"
 #include "ff.cuh"
+#include "kernel_ff.cuh"
 
 namespace bem2d_gpu {
 
@@ -192,27 +198,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-template <int KERNEL>
-__device__ __forceinline__ void pair_point(const DevGeom& g, int ui, int uj,
-                                           int e1, int e2, double s, double t,
-                                           double k, double kq, double eq,
-                                           double* re, double* im) {
-  const double* p1 = g.param + 8 * (size_t)e1;
-  const double* p2 = g.param + 8 * (size_t)e2;
-  const ElemPt a = elem_eval(g.kind[e1], p1, s);
-  const ElemPt b = elem_eval(g.kind[e2], p2, t);
-  double n1x, n1y, n2x, n2y;
-  elem_normal(a, &n1x, &n1y);
-  elem_normal(b, &n2x, &n2y);
-  double kr, ki;
-  kernel_d<KERNEL>(k, kq, eq, a.mx, a.my, b.mx, b.my, n1x, n1y, n2x, n2y, &kr, &ki);
-  const double f = basis_eval(g.unk_kind[ui], g.unk_param[ui], s) *
-                   basis_eval(g.unk_kind[uj], g.unk_param[uj], t) *
-                   elem_jac(a) * elem_jac(b);
-  *re = kr * f;
-  *im = ki * f;
-}
-
 // mass-matrix entry of a same-index pair (EvalIdent's inner loop)
 __device__ __forceinline__ double mass_entry(const DevGeom& g, const DevRules& r,
                                              int ui, int uj) {
@@ -227,70 +212,170 @@ __device__ __forceinline__ double mass_entry(const DevGeom& g, const DevRules& r
   return m;
 }
 
-template <int KERNEL>
+// Element geometry at the distinct coordinates of a rule, per warp in shared
+// memory (structure of arrays): Map, Normal and |J| phi, phi the basis
+// function of the pair's unknown on that element.
+struct GeoTab {
+  double* x;
+  double* y;
+  double* nx;
+  double* ny;
+  double* f;
+};
+
+__device__ __forceinline__ void geo_fill(const DevGeom& g, int e, int u, const double* vals, int n,
+                                         bool mirror, const GeoTab& tb, int off, int lane) {
+  const double* prm = g.param + 8 * (size_t)e;
+  for (int v = lane; v < n; v += 32) {
+    const double s = mirror ? 1 - vals[v] : vals[v];
+    const ElemPt p = elem_eval(g.kind[e], prm, s);
+    double nx, ny;
+    elem_normal(p, &nx, &ny);
+    tb.x[off + v] = p.mx;
+    tb.y[off + v] = p.my;
+    tb.nx[off + v] = nx;
+    tb.ny[off + v] = ny;
+    tb.f[off + v] = elem_jac(p) * basis_eval(g.unk_kind[u], g.unk_param[u], s);
+  }
+}
+
+// K(x, y) (re1, im1) and, if PAIR, K(y, x) (re2, im2) at a test point x
+// (normal n1) and a trial point y (normal n2).  FP64: kernel_d; MIXED: the
+// distance and the normal factors from the FP64 difference w = x - y, the
+// Bessel functions and the kernel in float-float.
+template <int KERNEL, bool MIXED, bool PAIR>
+__device__ __forceinline__ void near_point(double k, double kq, double eq, const KConstFF& kc,
+                                           const float* tab, double ax, double ay, double n1x,
+                                           double n1y, double bx, double by, double n2x,
+                                           double n2y, double* re1, double* im1, double* re2,
+                                           double* im2) {
+  if (!MIXED) {
+    if (PAIR)
+      kernel_d_pair<KERNEL>(k, kq, eq, ax, ay, bx, by, n1x, n1y, n2x, n2y, re1, im1, re2, im2);
+    else
+      kernel_d<KERNEL>(k, kq, eq, ax, ay, bx, by, n1x, n1y, n2x, n2y, re1, im1);
+    return;
+  }
+  const double wx = ax - bx, wy = ay - by;
+  const ff dx = ff_from_double(wx), dy = ff_from_double(wy);
+  const ff d2 = ff_add_fast(ff_sqr(dx), ff_sqr(dy));
+  const ff id = ff_rsqrt(d2);  // 1/d
+  const BesselFF b = bessel01_ff(ff_mul(ff_mul(d2, id), kc.k), ff_mul(id, kc.invk), tab);
+  ff cd1 = ff_make(0.0f, 0.0f), cd2 = ff_make(0.0f, 0.0f);
+  if (KERNEL != BEM2D_KERNEL_SINGLE) {
+    const double n1w = fma(n1x, wx, n1y * wy);  // n_x . (x - y)
+    const double n2w = fma(n2x, wx, n2y * wy);  // n_y . (x - y)
+    cd1 = ff_mul(ff_from_double(KERNEL == BEM2D_KERNEL_DOUBLE ? -n2w : n1w), id);
+    if (PAIR) cd2 = ff_mul(ff_from_double(KERNEL == BEM2D_KERNEL_DOUBLE ? n1w : -n2w), id);
+  }
+  const ffc K1 = kernel_from_bessel<KERNEL>(b, cd1, kc);
+  *re1 = ff_to_double(K1.re);
+  *im1 = ff_to_double(K1.im);
+  if (PAIR) {
+    if (KERNEL == BEM2D_KERNEL_SINGLE) {
+      *re2 = *re1;
+      *im2 = *im1;
+    } else {
+      const ffc K2 = kernel_from_bessel<KERNEL>(b, cd2, kc);
+      *re2 = ff_to_double(K2.re);
+      *im2 = ff_to_double(K2.im);
+    }
+  }
+}
+
+template <int KERNEL, bool MIXED>
 __global__ void __launch_bounds__(256)
-near_fp64_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs,
-                 int npairs, double k, double eta, double alpha, double beta,
-                 double2* __restrict__ out, long long ld, float2* __restrict__ out32,
-                 long long ld32) {
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npairs, double k,
+            double eta, double alpha, double beta, KConstFF kc, const float* gtab, int cap_s,
+            int cap_t, double2* __restrict__ out, long long ld, float2* __restrict__ out32,
+            long long ld32) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* tab = reinterpret_cast<float*>(smem_raw);  // e^{ix} table (MIXED)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cap = cap_s + cap_t;
+  double* base = reinterpret_cast<double*>(smem_raw + 1024) + (size_t)warp * 5 * cap;
+  const GeoTab S{base, base + cap, base + 2 * cap, base + 3 * cap, base + 4 * cap};
+  if (MIXED) {
+    for (int v = threadIdx.x; v < 256; v += blockDim.x) tab[v] = gtab[v];
+    __syncthreads();
+  }
+  const int wid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (wid >= npairs) return;
   const NearPair pr = pairs[wid];
   const int e1 = g.unk_elem[pr.i], e2 = g.unk_elem[pr.j];
   const double kq = 0.25 * k, eq = 0.25 * eta;
   double acc_re = 0.0, acc_im = 0.0;
+  double u1, u2;  // unused second orientation
   if (pr.rule == RULE_SELF) {
     // IntegrateIdent: Duffy split, points (x, (1-y)x) and (1-x, 1-x+yx),
-    // both weighted by x * w.
+    // both weighted by x * w.  Test-side geometry from the table (x values,
+    // then 1 - x); trial-side evaluated per point.
+    geo_fill(g, e1, pr.i, r.u1, r.nu1, false, S, 0, lane);
+    geo_fill(g, e1, pr.i, r.u1, r.nu1, true, S, r.nu1, lane);
+    __syncwarp();
+    const double* p2 = g.param + 8 * (size_t)e2;
     for (int p = lane; p < r.n1; p += 32) {
       const double x = r.r1[3 * p], y = r.r1[3 * p + 1], w = r.r1[3 * p + 2];
-      double re, im;
-      pair_point<KERNEL>(g, pr.i, pr.j, e1, e2, x, (1 - y) * x, k, kq, eq, &re, &im);
-      acc_re = fma(re, x * w, acc_re);
-      acc_im = fma(im, x * w, acc_im);
-      pair_point<KERNEL>(g, pr.i, pr.j, e1, e2, 1 - x, 1 - x + y * x, k, kq, eq, &re, &im);
-      acc_re = fma(re, x * w, acc_re);
-      acc_im = fma(im, x * w, acc_im);
-    }
-  } else if (pr.rule == RULE_G3_PAIR) {
-    // (i, j) with AdaptedGauss3 at (x, y), (j, i) with its mirror
-    // AdaptedGauss2 at (y, x): the same point pairs, one evaluation each
-    double acc2_re = 0.0, acc2_im = 0.0;
-    for (int p = lane; p < r.n3; p += 32) {
-      const double x = r.r3[3 * p], y = r.r3[3 * p + 1], w = r.r3[3 * p + 2];
-      const ElemPt a = elem_eval(g.kind[e1], g.param + 8 * (size_t)e1, x);
-      const ElemPt b = elem_eval(g.kind[e2], g.param + 8 * (size_t)e2, y);
-      double n1x, n1y, n2x, n2y;
-      elem_normal(a, &n1x, &n1y);
-      elem_normal(b, &n2x, &n2y);
-      double r1, i1, r2, i2;
-      kernel_d_pair<KERNEL>(k, kq, eq, a.mx, a.my, b.mx, b.my, n1x, n1y, n2x, n2y, &r1, &i1,
-                            &r2, &i2);
-      const double f = basis_eval(g.unk_kind[pr.i], g.unk_param[pr.i], x) *
-                       basis_eval(g.unk_kind[pr.j], g.unk_param[pr.j], y) * elem_jac(a) *
-                       elem_jac(b) * w;
-      acc_re = fma(r1, f, acc_re);
-      acc_im = fma(i1, f, acc_im);
-      acc2_re = fma(r2, f, acc2_re);
-      acc2_im = fma(i2, f, acc2_im);
-    }
-    acc2_re = warp_sum(acc2_re);
-    acc2_im = warp_sum(acc2_im);
-    if (lane == 0) {
-      const double re = alpha * acc2_re, im = alpha * acc2_im;
-      out[(size_t)pr.i * ld + pr.j] = make_double2(re, im);
-      if (out32) out32[(size_t)pr.i * ld32 + pr.j] = make_float2((float)re, (float)im);
+      const int si = r.k1[p] & 0xffff;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int a = si + h * r.nu1;
+        const double t = h == 0 ? (1 - y) * x : 1 - x + y * x;
+        const ElemPt b = elem_eval(g.kind[e2], p2, t);
+        double n2x, n2y, re, im;
+        elem_normal(b, &n2x, &n2y);
+        near_point<KERNEL, MIXED, false>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
+                                         b.mx, b.my, n2x, n2y, &re, &im, &u1, &u2);
+        const double f =
+            S.f[a] * (elem_jac(b) * basis_eval(g.unk_kind[pr.j], g.unk_param[pr.j], t));
+        acc_re = fma(re * f, x * w, acc_re);
+        acc_im = fma(im * f, x * w, acc_im);
+      }
     }
   } else {
-    const double* rule = pr.rule == RULE_G2 ? r.r2 : r.r3;
-    const int np = pr.rule == RULE_G2 ? r.n2 : r.n3;
-    for (int p = lane; p < np; p += 32) {
-      const double x = rule[3 * p], y = rule[3 * p + 1], w = rule[3 * p + 2];
-      double re, im;
-      pair_point<KERNEL>(g, pr.i, pr.j, e1, e2, x, y, k, kq, eq, &re, &im);
-      acc_re = fma(re, w, acc_re);
-      acc_im = fma(im, w, acc_im);
+    // AdaptedGauss2 / AdaptedGauss3: test geometry at the rule's x values,
+    // trial geometry at its y values.  RULE_G3_PAIR: (i, j) with
+    // AdaptedGauss3 at (x, y) and (j, i) with its mirror AdaptedGauss2 at
+    // (y, x), the same point pairs, one evaluation each.
+    const bool g2 = pr.rule == RULE_G2;
+    const double* rule = g2 ? r.r2 : r.r3;
+    const int* key = g2 ? r.k2 : r.k3;
+    const int np = g2 ? r.n2 : r.n3;
+    geo_fill(g, e1, pr.i, g2 ? r.u2 : r.u3, g2 ? r.nu2 : r.nu3, false, S, 0, lane);
+    geo_fill(g, e2, pr.j, g2 ? r.v2 : r.v3, g2 ? r.nv2 : r.nv3, false, S, cap_s, lane);
+    __syncwarp();
+    if (pr.rule == RULE_G3_PAIR) {
+      double acc2_re = 0.0, acc2_im = 0.0;
+      for (int p = lane; p < np; p += 32) {
+        const int kk = key[p];
+        const int a = kk & 0xffff, b = cap_s + (kk >> 16);
+        double r1, i1, r2, i2;
+        near_point<KERNEL, MIXED, true>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
+                                        S.x[b], S.y[b], S.nx[b], S.ny[b], &r1, &i1, &r2, &i2);
+        const double f = S.f[a] * S.f[b] * rule[3 * p + 2];
+        acc_re = fma(r1, f, acc_re);
+        acc_im = fma(i1, f, acc_im);
+        acc2_re = fma(r2, f, acc2_re);
+        acc2_im = fma(i2, f, acc2_im);
+      }
+      acc2_re = warp_sum(acc2_re);
+      acc2_im = warp_sum(acc2_im);
+      if (lane == 0) {
+        const double re = alpha * acc2_re, im = alpha * acc2_im;
+        out[(size_t)pr.i * ld + pr.j] = make_double2(re, im);
+        if (MIXED) out32[(size_t)pr.i * ld32 + pr.j] = make_float2((float)re, (float)im);
+      }
+    } else {
+      for (int p = lane; p < np; p += 32) {
+        const int kk = key[p];
+        const int a = kk & 0xffff, b = cap_s + (kk >> 16);
+        double re, im;
+        near_point<KERNEL, MIXED, false>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
+                                         S.x[b], S.y[b], S.nx[b], S.ny[b], &re, &im, &u1, &u2);
+        const double f = S.f[a] * S.f[b] * rule[3 * p + 2];
+        acc_re = fma(re, f, acc_re);
+        acc_im = fma(im, f, acc_im);
+      }
     }
   }
   acc_re = warp_sum(acc_re);
@@ -299,29 +384,79 @@ near_fp64_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs,
     double re = alpha * acc_re, im = alpha * acc_im;
     if (pr.same && beta != 0.0) re = fma(beta, mass_entry(g, r, pr.i, pr.j), re);
     out[(size_t)pr.j * ld + pr.i] = make_double2(re, im);
-    if (out32) out32[(size_t)pr.j * ld32 + pr.i] = make_float2((float)re, (float)im);
+    if (MIXED) out32[(size_t)pr.j * ld32 + pr.i] = make_float2((float)re, (float)im);
   }
 }
 
-void launch_near_fp64(const DevGeom& g, const DevRules& r, const NearPair* pairs,
-                      int npairs, int kernel, double k, double eta, double alpha,
-                      double beta, double2* out, long long ld, cudaStream_t s,
-                      float2* out32, long long ld32) {
-  if (npairs == 0) return;
-  const int blocks = (npairs * 32 + 255) / 256;
+// Table capacities (entries per warp) of the near-field kernel for rules r.
+static void near_caps(const DevRules& r, int* cap_s, int* cap_t) {
+  *cap_s = std::max(2 * r.nu1, std::max(r.nu2, r.nu3));
+  *cap_t = std::max(r.nv2, r.nv3);
+}
+
+size_t near_table_bytes(const DevRules& r) {
+  int cs, ct;
+  near_caps(r, &cs, &ct);
+  return sizeof(double) * 5 * (size_t)(cs + ct);
+}
+
+template <int KERNEL, bool MIXED>
+static void launch_near_k(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                          double k, double eta, double alpha, double beta, const float* tab,
+                          double2* out, long long ld, float2* out32, long long ld32,
+                          cudaStream_t s) {
+  int cs, ct;
+  near_caps(r, &cs, &ct);
+  const size_t per_warp = std::max<size_t>(near_table_bytes(r), 8);  // L = 0: empty rules
+  // warps per block: up to 8, within 96 KB of shared memory
+  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024 - 1024) / per_warp));
+  const size_t smem = 1024 + per_warp * wpb;
+  const int blocks = (npairs + wpb - 1) / wpb;
+  auto fn = near_kernel<KERNEL, MIXED>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  fn<<<blocks, 32 * wpb, smem, s>>>(g, r, pairs, npairs, k, eta, alpha, beta,
+                                     make_kconst(k, eta), tab, cs, ct, out, ld, out32, ld32);
+}
+
+template <bool MIXED>
+static void launch_near_m(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                          int kernel, double k, double eta, double alpha, double beta,
+                          const float* tab, double2* out, long long ld, float2* out32,
+                          long long ld32, cudaStream_t s) {
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      near_fp64_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
+      launch_near_k<BEM2D_KERNEL_SINGLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
+                                                out, ld, out32, ld32, s);
       break;
     case BEM2D_KERNEL_DOUBLE:
-      near_fp64_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
+      launch_near_k<BEM2D_KERNEL_DOUBLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
+                                                out, ld, out32, ld32, s);
       break;
     case BEM2D_KERNEL_CONJDOUBLE:
-      near_fp64_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
+      launch_near_k<BEM2D_KERNEL_CONJDOUBLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta,
+                                                    tab, out, ld, out32, ld32, s);
       break;
     default:
-      near_fp64_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 256, 0, s>>>(g, r, pairs, npairs, k, eta, alpha, beta, out, ld, out32, ld32);
+      launch_near_k<BEM2D_KERNEL_COMBINED, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
+                                                  out, ld, out32, ld32, s);
   }
+}
+
+int launch_near(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                int kernel, double k, double eta, double alpha, double beta, double2* out,
+                long long ld, cudaStream_t s, float2* out32, long long ld32) {
+  if (npairs == 0) return BEM2D_OK;
+  if (out32) {
+    const float* tab = expi_table_dev();
+    if (!tab) return BEM2D_ERR_NOMEM;
+    launch_near_m<true>(g, r, pairs, npairs, kernel, k, eta, alpha, beta, tab, out, ld, out32,
+                        ld32, s);
+  } else {
+    launch_near_m<false>(g, r, pairs, npairs, kernel, k, eta, alpha, beta, nullptr, out, ld,
+                         nullptr, 0, s);
+  }
+  return BEM2D_OK;
 }
 
 // ---------------------------------------------------------------------------

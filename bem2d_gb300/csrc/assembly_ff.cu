@@ -6,21 +6,20 @@
 // difference of the two elements in FP64, node offsets from the centres in
 // float-float, so |x - y| keeps ~48 bits relative to itself even for
 // neighbouring elements.  Entries whose element pair admits k|x - y| <= 4
-// anywhere (bounded with the element radii) are deferred to an FP64 pass,
-// where the small-argument Hankel pieces live; adjacent and identical pairs
-// belong to the FP64 near-field kernel as in the FP64 path.  Each entry is
-// stored twice: complex128 (refinement residual) and complex64 (the LU).
+// anywhere (bounded with the element radii) are deferred to a second
+// float-float pass (deferred_ff_kernel, one thread per element pair), which
+// carries the small-argument Bessel branch; keeping them out of the tile
+// loop keeps its warps on one branch.  Adjacent and identical pairs belong to
+// the near-field kernel as in the FP64 path.  Each entry is stored twice:
+// complex128 (refinement residual) and complex64 (the LU).
 #include <mutex>
 
 #include "common.cuh"
 #include "ff.cuh"
 #include "hankel_ff.cuh"
+#include "kernel_ff.cuh"
 
 namespace bem2d_gpu {
-
-struct KConstFF {
-  ff k, invk, kq, eq, amp0;
-};
 
 // The distance-dependent part of the kernel at one node pair: 1/d, the
 // asymptotic P/Q factors of H0 and H1, the amplitude sqrt(2/(pi x)) and
@@ -196,8 +195,8 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
     const double dxc = crow.x - cen[kTileF + cc].x, dyc = crow.y - cen[kTileF + cc].y;
     const float dist = sqrtf((float)(dxc * dxc + dyc * dyc));
     if (kf * (dist * (1.0f - 1e-6f) - rrow - rad[kTileF + cc]) <= kDeferX) {
-      // small arguments somewhere on this pair: FP64 pass (or here, if the
-      // list is full).  One list item per pair: (row, col) with the flags
+      // small arguments somewhere on this pair: second pass (or here, in
+      // FP64, if the list is full).  One list item per pair: (row, col) with the flags
       // kDeferRC / kDeferCR in the top bits of .x for the directions needed.
       const unsigned slot = atomicAdd(dl.count, 1u);
       if (slot < dl.capacity) {
@@ -284,47 +283,81 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
 }
 
 template <int KERNEL>
-__global__ void deferred_fp64_kernel(NodeTable t, int ng, double k, double eta, double alpha,
-                                     const int2* __restrict__ ij, const unsigned* count,
-                                     unsigned cap, double2* __restrict__ out, long long ld,
-                                     float2* __restrict__ out32, long long ld32) {
+__global__ void __launch_bounds__(128)
+deferred_ff_kernel(NodeTableFF tf, int ng, KConstFF kc, double alpha, const int2* __restrict__ ij,
+                   const unsigned* count, unsigned cap, double2* __restrict__ out, long long ld,
+                   float2* __restrict__ out32, long long ld32, const float* gtab) {
   // one item = one element pair; both orientations share every distance
-  // and Hankel evaluation
+  // and Bessel evaluation.  Same pair geometry as far_ff_kernel: the centre
+  // difference in FP64, node offsets in ff.
+  __shared__ float tab[256];
+  for (int v = threadIdx.x; v < 256; v += blockDim.x) tab[v] = gtab[v];
+  __syncthreads();
   const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= min(*count, cap)) return;
   const int2 e = ij[p];
   const int row = e.x & kDeferIdx, col = e.y;
   const bool want_rc = (e.x & kDeferRC) != 0, want_cr = (e.x & kDeferCR) != 0;
-  const double kq = 0.25 * k, eq = 0.25 * eta;
-  double r1 = 0.0, i1 = 0.0, r2 = 0.0, i2 = 0.0;
+  const double2 cr0 = tf.c[row], cc0 = tf.c[col];
+  const ff Dx = ff_from_double(cr0.x - cc0.x), Dy = ff_from_double(cr0.y - cc0.y);
+  ffc arc, acr;
+  arc.re = arc.im = acr.re = acr.im = ff_make(0.0f, 0.0f);
+#pragma unroll 1
   for (int q1 = 0; q1 < ng; ++q1) {
     const size_t a = (size_t)row * ng + q1;
-    const double x1 = t.x[a], y1 = t.y[a], n1x = t.nx[a], n1y = t.ny[a], w1 = t.w[a];
+    const float2 a0 = tf.ox[a], a1 = tf.oy[a], a2 = tf.nx[a], a3 = tf.ny[a], a4 = tf.w[a];
+    const ff ox1 = ff_make(a0.x, a0.y), oy1 = ff_make(a1.x, a1.y);
+    const ff n1x = ff_make(a2.x, a2.y), n1y = ff_make(a3.x, a3.y), w1 = ff_make(a4.x, a4.y);
+#pragma unroll 1
     for (int q2 = 0; q2 < ng; ++q2) {
       const size_t b = (size_t)col * ng + q2;
-      double vr1, vi1, vr2, vi2;
-      kernel_d_pair<KERNEL>(k, kq, eq, x1, y1, t.x[b], t.y[b], n1x, n1y, t.nx[b], t.ny[b], &vr1,
-                            &vi1, &vr2, &vi2);
-      const double ww = w1 * t.w[b];
-      r1 = fma(vr1, ww, r1);
-      i1 = fma(vi1, ww, i1);
-      r2 = fma(vr2, ww, r2);
-      i2 = fma(vi2, ww, i2);
+      const float2 b0 = tf.ox[b], b1 = tf.oy[b], b2 = tf.nx[b], b3 = tf.ny[b], b4 = tf.w[b];
+      // w = x - y, x a node of the row element, y of the column element
+      const ff dx = ff_add_fast(Dx, ff_add_fast(ox1, ff_make(-b0.x, -b0.y)));
+      const ff dy = ff_add_fast(Dy, ff_add_fast(oy1, ff_make(-b1.x, -b1.y)));
+      const ff d2 = ff_add_fast(ff_sqr(dx), ff_sqr(dy));
+      const ff id = ff_rsqrt(d2);  // 1/d
+      const ff x = ff_mul(ff_mul(d2, id), kc.k);
+      const BesselFF bs = bessel01_ff(x, ff_mul(id, kc.invk), tab);
+      const ff ww = ff_mul(w1, ff_make(b4.x, b4.y));
+      ff cd_rc = ff_make(0.0f, 0.0f), cd_cr = ff_make(0.0f, 0.0f);
+      if (KERNEL != BEM2D_KERNEL_SINGLE) {
+        const ff n1w = ff_mul(ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy)), id);
+        const ff n2w = ff_mul(ff_add_fast(ff_mul(ff_make(b2.x, b2.y), dx),
+                                          ff_mul(ff_make(b3.x, b3.y), dy)), id);
+        if (KERNEL == BEM2D_KERNEL_DOUBLE) {
+          cd_rc = ff_neg(n2w);  // (row, col): n_y . (y - x) / d
+          cd_cr = n1w;          // (col, row): n_x . (x - y) / d
+        } else {
+          cd_rc = n1w;
+          cd_cr = ff_neg(n2w);
+        }
+      }
+      const ffc K1 = kernel_from_bessel<KERNEL>(bs, cd_rc, kc);
+      arc.re = ff_add_fast(arc.re, ff_mul(K1.re, ww));
+      arc.im = ff_add_fast(arc.im, ff_mul(K1.im, ww));
+      if (KERNEL == BEM2D_KERNEL_SINGLE) {
+        acr = arc;
+      } else {
+        const ffc K2 = kernel_from_bessel<KERNEL>(bs, cd_cr, kc);
+        acr.re = ff_add_fast(acr.re, ff_mul(K2.re, ww));
+        acr.im = ff_add_fast(acr.im, ff_mul(K2.im, ww));
+      }
     }
   }
   if (want_rc) {
-    out[(size_t)col * ld + row] = make_double2(alpha * r1, alpha * i1);
-    out32[(size_t)col * ld32 + row] = make_float2((float)(alpha * r1), (float)(alpha * i1));
+    const double re = alpha * ff_to_double(arc.re), im = alpha * ff_to_double(arc.im);
+    out[(size_t)col * ld + row] = make_double2(re, im);
+    out32[(size_t)col * ld32 + row] = make_float2((float)re, (float)im);
   }
   if (want_cr) {
-    out[(size_t)row * ld + col] = make_double2(alpha * r2, alpha * i2);
-    out32[(size_t)row * ld32 + col] = make_float2((float)(alpha * r2), (float)(alpha * i2));
+    const double re = alpha * ff_to_double(acr.re), im = alpha * ff_to_double(acr.im);
+    out[(size_t)row * ld + col] = make_double2(re, im);
+    out32[(size_t)row * ld32 + col] = make_float2((float)re, (float)im);
   }
 }
 
-// Device copy of the e^{i x} reduction table, made once per device (the
-// current one); thread-safe.
-static const float* expi_table_dev() {
+const float* expi_table_dev() {
   constexpr int kMaxDev = 64;
   static std::mutex mu;
   static float* tab[kMaxDev] = {};
@@ -347,12 +380,7 @@ template <int KERNEL>
 static int launch_far_ff_k(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, int ng,
                             double k, double eta, double alpha, double2* out, long long ld,
                             float2* out32, long long ld32, DeferList dl, cudaStream_t s) {
-  KConstFF kc;
-  kc.k = ff_from_double(k);
-  kc.invk = ff_from_double(1.0 / k);
-  kc.kq = ff_from_double(0.25 * k);
-  kc.eq = ff_from_double(0.25 * eta);
-  kc.amp0 = ff_from_double(0.79788456080286535588);  // sqrt(2/pi)
+  const KConstFF kc = make_kconst(k, eta);
   const size_t smem = sizeof(double2) * kTileF * (kTileF + 1) + sizeof(unsigned) * kTileF +
                       sizeof(float) * 256 + sizeof(double2) * 2 * kTileF +
                       sizeof(float2) * 10 * ng * kTileF + sizeof(float) * 2 * kTileF +
@@ -395,27 +423,28 @@ int launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, i
 }
 
 // Grid sized by the list capacity; threads beyond the device-side count exit.
-void launch_deferred_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
-                          double eta, double alpha, const DeferList& dl, unsigned n,
-                          double2* out, long long ld, float2* out32, long long ld32,
-                          cudaStream_t s) {
-  (void)g;
-  (void)n;
-  if (dl.capacity == 0) return;
+int launch_deferred(const NodeTableFF& tf, int ng, int kernel, double k, double eta,
+                    double alpha, const DeferList& dl, double2* out, long long ld,
+                    float2* out32, long long ld32, cudaStream_t s) {
+  if (dl.capacity == 0) return BEM2D_OK;
+  const float* tab = expi_table_dev();
+  if (!tab) return BEM2D_ERR_NOMEM;
+  const KConstFF kc = make_kconst(k, eta);
   const unsigned blocks = (dl.capacity + 127) / 128;
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      deferred_fp64_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      deferred_ff_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 128, 0, s>>>(tf, ng, kc, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32, tab);
       break;
     case BEM2D_KERNEL_DOUBLE:
-      deferred_fp64_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      deferred_ff_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 128, 0, s>>>(tf, ng, kc, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32, tab);
       break;
     case BEM2D_KERNEL_CONJDOUBLE:
-      deferred_fp64_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      deferred_ff_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 128, 0, s>>>(tf, ng, kc, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32, tab);
       break;
     default:
-      deferred_fp64_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 128, 0, s>>>(t, ng, k, eta, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32);
+      deferred_ff_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 128, 0, s>>>(tf, ng, kc, alpha, dl.ij, dl.count, dl.capacity, out, ld, out32, ld32, tab);
   }
+  return BEM2D_OK;
 }
 
 }  // namespace bem2d_gpu

@@ -228,6 +228,27 @@ static HostRules make_rules(int L, int N, double sigma) {
   return r;
 }
 
+// Distinct x and y values of a rule (exact equality: points of boxes that
+// share an interval are computed by the same expression) and, per point,
+// their indices packed as x | y << 16.
+struct RuleIndex {
+  std::vector<double> u, v;
+  std::vector<int> k;
+};
+
+static RuleIndex index_rule(const std::vector<double>& r) {
+  RuleIndex ri;
+  std::map<double, int> mu, mv;
+  for (size_t p = 0; p + 2 < r.size(); p += 3) {
+    const auto a = mu.emplace(r[p], (int)mu.size());
+    if (a.second) ri.u.push_back(r[p]);
+    const auto b = mv.emplace(r[p + 1], (int)mv.size());
+    if (b.second) ri.v.push_back(r[p + 1]);
+    ri.k.push_back(a.first->second | (b.first->second << 16));
+  }
+  return ri;
+}
+
 static int get_rules(bem2d_ctx* c, const bem2d_quad* q, DevRules* out) {
   const RuleKey key{q->L, q->N, q->sigma};
   auto it = c->rules.find(key);
@@ -236,15 +257,25 @@ static int get_rules(bem2d_ctx* c, const bem2d_quad* q, DevRules* out) {
     return BEM2D_OK;
   }
   const HostRules h = make_rules(q->L, q->N, q->sigma);
+  const RuleIndex i1 = index_rule(h.r1), i2 = index_rule(h.r2), i3 = index_rule(h.r3);
+  // near-field geometry tables: one warp's must fit in shared memory
+  const size_t cap = std::max(2 * i1.u.size(), std::max(i2.u.size(), i3.u.size())) +
+                     std::max(i2.v.size(), i3.v.size());
+  if (cap > 4096)
+    return fail(c, BEM2D_ERR_ARG, "quadrature rule too large for the near-field kernel");
   std::vector<double> all;
-  all.insert(all.end(), h.gx.begin(), h.gx.end());
-  all.insert(all.end(), h.gw.begin(), h.gw.end());
-  all.insert(all.end(), h.r1.begin(), h.r1.end());
-  all.insert(all.end(), h.r2.begin(), h.r2.end());
-  all.insert(all.end(), h.r3.begin(), h.r3.end());
+  for (const std::vector<double>* v : {&h.gx, &h.gw, &h.r1, &h.r2, &h.r3, &i1.u, &i2.u, &i2.v,
+                                       &i3.u, &i3.v})
+    all.insert(all.end(), v->begin(), v->end());
+  const size_t nd = all.size();
+  const size_t nk = i1.k.size() + i2.k.size() + i3.k.size();
   void* d = nullptr;
-  CUDA_TRY(c, cudaMalloc(&d, sizeof(double) * std::max<size_t>(all.size(), 1)));
-  CUDA_TRY(c, cudaMemcpy(d, all.data(), sizeof(double) * all.size(), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMalloc(&d, sizeof(double) * std::max<size_t>(nd, 1) + sizeof(int) * nk));
+  CUDA_TRY(c, cudaMemcpy(d, all.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
+  std::vector<int> keys;
+  for (const RuleIndex* ri : {&i1, &i2, &i3}) keys.insert(keys.end(), ri->k.begin(), ri->k.end());
+  int* dk = reinterpret_cast<int*>(static_cast<double*>(d) + nd);
+  CUDA_TRY(c, cudaMemcpy(dk, keys.data(), sizeof(int) * nk, cudaMemcpyHostToDevice));
   const double* p = static_cast<const double*>(d);
   DevRules r;
   r.ng = q->N;
@@ -256,6 +287,19 @@ static int get_rules(bem2d_ctx* c, const bem2d_quad* q, DevRules* out) {
   r.n2 = (int)h.r2.size() / 3;
   r.r3 = r.r2 + h.r2.size();
   r.n3 = (int)h.r3.size() / 3;
+  r.u1 = r.r3 + h.r3.size();
+  r.nu1 = (int)i1.u.size();
+  r.u2 = r.u1 + i1.u.size();
+  r.nu2 = (int)i2.u.size();
+  r.v2 = r.u2 + i2.u.size();
+  r.nv2 = (int)i2.v.size();
+  r.u3 = r.v2 + i2.v.size();
+  r.nu3 = (int)i3.u.size();
+  r.v3 = r.u3 + i3.u.size();
+  r.nv3 = (int)i3.v.size();
+  r.k1 = dk;
+  r.k2 = dk + i1.k.size();
+  r.k3 = r.k2 + i2.k.size();
   c->rules[key] = std::make_pair(d, r);
   *out = r;
   return BEM2D_OK;
@@ -443,16 +487,17 @@ static int assemble_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, do
   ++c->launches;
   CHECK_LAUNCH(c);
   t = tic(c, BEM2D_PHASE_NEAR);
-  launch_near_fp64(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
-                   c->stream);
+  launch_near(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld, c->stream);
   toc(c, t);
   if (st.npairs) ++c->launches;
   CHECK_LAUNCH(c);
   return BEM2D_OK;
 }
 
-// Mixed assembly: float-float far field + FP64 deferred and near-field
-// entries, into a complex128 (A, ld) and a complex64 (A32, ld32) matrix.
+// Mixed assembly: Bessel functions in float-float throughout (far field,
+// deferred and near-field entries; geometry and quadrature sums in FP64 for
+// the near field), into a complex128 (A, ld) and a complex64 (A32, ld32)
+// matrix.
 static int assemble_mixed_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, double eta,
                               double alpha, double beta, double2* A, long long ld, float2* A32,
                               long long ld32) {
@@ -471,14 +516,16 @@ static int assemble_mixed_dev(bem2d_ctx* c, const Staged& st, int kernel, double
   if (launch_far_ff(st.g, st.t, st.tf, st.r.ng, kernel, k, eta, alpha, A, ld, A32, ld32, dl,
                     c->stream) != BEM2D_OK)
     return fail(c, BEM2D_ERR_NOMEM, "device table for the far-field kernel");
-  launch_deferred_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, dl, 0, A, ld, A32, ld32,
-                       c->stream);
+  if (launch_deferred(st.tf, st.r.ng, kernel, k, eta, alpha, dl, A, ld, A32, ld32,
+                      c->stream) != BEM2D_OK)
+    return fail(c, BEM2D_ERR_NOMEM, "device table for the deferred far-field kernel");
   toc(c, t);
   c->launches += 2;
   CHECK_LAUNCH(c);
   t = tic(c, BEM2D_PHASE_NEAR);
-  launch_near_fp64(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
-                   c->stream, A32, ld32);
+  if (launch_near(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld,
+                  c->stream, A32, ld32) != BEM2D_OK)
+    return fail(c, BEM2D_ERR_NOMEM, "device table for the near-field kernel");
   toc(c, t);
   if (st.npairs) ++c->launches;
   CHECK_LAUNCH(c);

@@ -241,6 +241,19 @@ struct DevRules {
   const double* r1;      // [3*n1] x, y, w
   const double* r2;
   const double* r3;
+  // Distinct coordinates of each rule, for the near-field geometry tables:
+  // u1 [nu1] the x values of AdaptedGauss1; u2/v2 [nu2]/[nv2] and u3/v3 the
+  // x and y values of AdaptedGauss2/3.  k1/k2/k3 [n*]: per point, the index
+  // of its x value (low 16 bits) and of its y value (high 16 bits).
+  int nu1, nu2, nv2, nu3, nv3;
+  const double* u1;
+  const double* u2;
+  const double* v2;
+  const double* u3;
+  const double* v3;
+  const int* k1;
+  const int* k2;
+  const int* k3;
 };
 
 // ---- launch interfaces (assembly.cu) ------------------------------------
@@ -270,8 +283,9 @@ struct NodeTableFF {
 void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
                        const NodeTableFF* tf, cudaStream_t s);
 
-// Entries the float-float far kernel leaves to FP64 (an argument k|x-y| <= 4
-// somewhere on the element pair): (row, column) list with a counter.
+// Entries the float-float far kernel leaves to a second pass (an argument
+// k|x-y| <= 4 somewhere on the element pair): (row, column) list with a
+// counter.
 struct DeferList {
   int2* ij;
   unsigned* count;
@@ -285,18 +299,24 @@ int launch_far_ff(const DevGeom& g, const NodeTable& t, const NodeTableFF& tf, i
                   int kernel, double k, double eta, double alpha, double2* out,
                   long long ld, float2* out32, long long ld32, DeferList dl,
                   cudaStream_t s);
-// FP64 evaluation of the deferred entries (both outputs).
-void launch_deferred_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
-                          double k, double eta, double alpha, const DeferList& dl,
-                          unsigned n, double2* out, long long ld, float2* out32,
-                          long long ld32, cudaStream_t s);
+// Float-float evaluation of the deferred entries, small-argument Bessel
+// branch included (both outputs).  Returns BEM2D_ERR_NOMEM if the device
+// reduction table could not be made.
+int launch_deferred(const NodeTableFF& tf, int ng, int kernel, double k, double eta,
+                    double alpha, const DeferList& dl, double2* out, long long ld,
+                    float2* out32, long long ld32, cudaStream_t s);
 void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
                      double k, double eta, double alpha, double2* out,
                      long long ld, cudaStream_t s);
-void launch_near_fp64(const DevGeom& g, const DevRules& r, const NearPair* pairs,
-                      int npairs, int kernel, double k, double eta, double alpha,
-                      double beta, double2* out, long long ld, cudaStream_t s,
-                      float2* out32 = nullptr, long long ld32 = 0);
+// Near field (self and adjacent pairs).  out32 == nullptr: FP64 kernel
+// evaluation into out.  Otherwise the mixed-precision variant (float-float
+// Bessel functions) writes both out and out32.  Returns BEM2D_ERR_NOMEM if
+// the device reduction table could not be made.
+int launch_near(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                int kernel, double k, double eta, double alpha, double beta, double2* out,
+                long long ld, cudaStream_t s, float2* out32 = nullptr, long long ld32 = 0);
+// Shared-memory bytes per warp of the near-field geometry tables for rules r.
+size_t near_table_bytes(const DevRules& r);
 void launch_ident(const DevGeom& g, const DevRules& r, const NearPair* pairs,
                   int npairs, double2* out, long long ld, cudaStream_t s);
 void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,

@@ -150,4 +150,37 @@ __host__ __device__ __forceinline__ ff ff_rcp(ff a) {
   return fast_two_sum(y, y * e);
 }
 
+// Natural logarithm of a > 0 (normal hi part).  a = 2^e m with m in
+// [sqrt(1/2), sqrt(2)); log m = 2 atanh(u) = 2 (u + u^3/3 + u^5/5 + ...),
+// u = (m - 1)/(m + 1), |u| <= 0.172, so u^2 <= 0.0295.  m - 1 is exact
+// (Sterbenz), which keeps the relative accuracy of log m near m = 1.  The
+// series terms through u^8/9 are carried in ff, the rest (below 2e-9) in
+// FP32; log 2 is the ff pair nearest to it.
+__host__ __device__ __forceinline__ ff ff_log(ff a) {
+  int e;
+  float m = frexpf(a.hi, &e);  // a.hi = m 2^e, m in [1/2, 1)
+  if (m < 0.70710678f) {
+    m *= 2.0f;
+    --e;
+  }
+  const float ml = ldexpf(a.lo, -e);
+  const ff num = two_sum(m - 1.0f, ml);
+  const ff den = ff_add_f(two_sum(m, 1.0f), ml);
+  const ff u = ff_mul(num, ff_rcp(den));
+  const ff u2 = ff_sqr(u);
+  const float v = u2.hi;
+  const float tail =
+      v * fmaf(v, fmaf(v, fmaf(v, fmaf(v, fmaf(v, fmaf(v, 1.0f / 25.0f, 1.0f / 23.0f),
+                                                 1.0f / 21.0f), 1.0f / 19.0f), 1.0f / 17.0f),
+                         1.0f / 15.0f), 1.0f / 13.0f) + 1.0f / 11.0f;
+  ff s = ff_add_f(ff_make(0.1111111119389534f, -8.278422947149977e-10f), v * tail);  // 1/9
+  s = ff_add_fast(ff_make(0.1428571492433548f, -6.38621200366174e-09f), ff_mul(u2, s));  // 1/7
+  s = ff_add_fast(ff_make(0.20000000298023224f, -2.9802322831784522e-09f), ff_mul(u2, s));  // 1/5
+  s = ff_add_fast(ff_make(0.3333333432674408f, -9.934107758624577e-09f), ff_mul(u2, s));     // 1/3
+  s = ff_add_fast(ff_make(1.0f, 0.0f), ff_mul(u2, s));
+  const ff lm = ff_mul(ff_scale2(u, 2.0f), s);
+  const ff l2 = ff_mul_f(ff_make(0.6931471824645996f, -1.9046542121259336e-09f), (float)e);
+  return ff_add(l2, lm);
+}
+
 }  // namespace bem2d_gpu

@@ -191,7 +191,7 @@ def main():
                    % (suffix, max(map(len, small)), max(map(len, mid)), max(map(len, far))))
     with open(os.path.join(HERE, "hankel_coeffs.h"), "w") as f:
         f.write("\n".join(out) + "\n")
-    # float-float tables for x >= 4 (four intervals)
+    # float-float tables: x >= 4 (four intervals) and x <= 4
     out = ["// Generated by gen_hankel.py: float-float pieces of the Hankel evaluator",
            "// for x >= 4 (see hankel_ff.cuh).  Do not edit by hand.",
            "#pragma once", '#include "ff.cuh"', "", "namespace bem2d_gpu {", ""]
@@ -202,6 +202,11 @@ def main():
                    % (X, xhi if xhi else "inf", X, X, mp.nstr(slo, 6), mp.nstr(slo, 6)))
         out.append("// s = (%d/x)^2" % X)
         out.append(emit_ff_polys(idx, polys))
+    # index 4: the small-argument pieces A0, A1, B0, B1 (x <= 4) in t = x^2/8 - 1
+    small = [fit(f, 2e-18) for f in small_funcs()]
+    out.append("// x <= 4: J0 = A0, J1 = x A1, Y0 = (2/pi) ln x J0 + B0,")
+    out.append("//         Y1 = (2/pi) ln x J1 - 2/(pi x) + x B1;  t = x^2/8 - 1")
+    out.append(emit_ff_polys(len(FF_INTERVALS), small))
     out.append("}  // namespace bem2d_gpu")
     with open(os.path.join(HERE, "hankel_ff_coeffs.h"), "w") as f:
         f.write("\n".join(out) + "\n")

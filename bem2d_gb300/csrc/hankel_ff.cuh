@@ -1,10 +1,11 @@
-// Far-field kernel evaluation in float-float arithmetic (FP32 pipe) for
-// arguments x = k d >= 4: H0 and H1 in modulus-phase form
+// Kernel evaluation in float-float arithmetic (FP32 pipe).  For arguments
+// x = k d >= 4: H0 and H1 in modulus-phase form
 //   H_nu(x) = sqrt(2/(pi x)) (P_nu + i Q_nu) e^{i(x - (2 nu + 1) pi/4)}
 // with P, Q from hankel_ff_coeffs.h (four intervals of x), and e^{i(x-pi/4)}
 // from a Cody-Waite reduction modulo 2 pi/64 plus short Taylor polynomials
 // around a 64-entry table of e^{i(2 pi j/64 - pi/4)}.  Accuracy ~1e-14
-// relative to |H|; the same source builds on the host for accuracy tests.
+// relative to |H|.  bessel01_ff adds the small arguments (x <= 4) from the
+// power-series form.  The same source builds on the host for accuracy tests.
 #pragma once
 
 #include "ff.cuh"
@@ -93,6 +94,39 @@ __host__ __device__ __forceinline__ void pq_ff(float xhi, ff ix, ff* p0, ff* q0,
     *p1 = hkff_2_2(t);
     *q1 = ff_mul(hkff_2_3(t), q);
   }
+}
+
+struct BesselFF {
+  ff j0, y0, j1, y1;
+};
+
+// J0, Y0, J1, Y1 at any x > 0 given x and ix = 1/x.  x <= 4: the
+// power-series form (A&S 9.1.10-9.1.13) with the regular parts A0, A1, B0,
+// B1 as polynomials in t = x^2/8 - 1 and the logarithm from ff_log; x > 4:
+// the modulus-phase form above.  Absolute accuracy ~1e-14 of max(1, |H|).
+__host__ __device__ __forceinline__ BesselFF bessel01_ff(ff x, ff ix, const float* tab) {
+  BesselFF r;
+  if (x.hi <= 4.0f) {
+    const ff t = ff_add_f(ff_scale2(ff_sqr(x), 0.125f), -1.0f);
+    const ff a0 = hkff_4_0(t), a1 = hkff_4_1(t), b0 = hkff_4_2(t), b1 = hkff_4_3(t);
+    const ff two_pi = ff_make(0.6366197466850281f, 2.5682552973194106e-08f);  // 2/pi
+    const ff lx = ff_mul(two_pi, ff_log(x));
+    r.j0 = a0;
+    r.j1 = ff_mul(x, a1);
+    r.y0 = ff_add_fast(ff_mul(lx, a0), b0);
+    r.y1 = ff_add_fast(ff_add_fast(ff_mul(lx, r.j1), ff_mul(x, b1)), ff_neg(ff_mul(two_pi, ix)));
+  } else {
+    ff p0, q0, p1, q1;
+    pq_ff(x.hi, ix, &p0, &q0, &p1, &q1);
+    const ff amp = ff_mul(ff_make(0.7978845834732056f, -2.2670340271702116e-08f), ff_sqrt(ix));
+    const ffc e = expi_ff(x, tab);  // c + i s = e^{i(x - pi/4)}
+    // J0 + i Y0 = amp (P0 + i Q0)(c + i s);  J1 + i Y1 = amp (P1 + i Q1)(s - i c)
+    r.j0 = ff_mul(amp, ff_add_fast(ff_mul(p0, e.re), ff_neg(ff_mul(q0, e.im))));
+    r.y0 = ff_mul(amp, ff_add_fast(ff_mul(p0, e.im), ff_mul(q0, e.re)));
+    r.j1 = ff_mul(amp, ff_add_fast(ff_mul(p1, e.im), ff_mul(q1, e.re)));
+    r.y1 = ff_mul(amp, ff_add_fast(ff_mul(q1, e.im), ff_neg(ff_mul(p1, e.re))));
+  }
+  return r;
 }
 
 // Host-side table of e^{i(2 pi j/64 - pi/4)} as ff pairs (4 floats per j).

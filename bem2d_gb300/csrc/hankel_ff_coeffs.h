@@ -141,4 +141,57 @@ __host__ __device__ __forceinline__ ff hkff_3_3(ff t) {
   return y;
 }
 
+// x <= 4: J0 = A0, J1 = x A1, Y0 = (2/pi) ln x J0 + B0,
+//         Y1 = (2/pi) ln x J1 - 2/(pi x) + x B1;  t = x^2/8 - 1
+__host__ __device__ __forceinline__ ff hkff_4_0(ff t) {
+  const float tail = fmaf(fmaf(fmaf(1.529983246e-14f, t.hi, -1.087432336e-12f), t.hi, 6.474430020e-11f), t.hi, -3.177438757e-09f);
+  ff y = ff_add_f(ff_make(1.257728002e-07f, 6.118954153e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(-3.910342002e-06f, 2.304720406e-14f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.228174167e-05f, -1.769930123e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.578954165e-03f, 2.818224126e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.835270040e-02f, 2.126934046e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.310320646e-01f, 1.043430009e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(4.795280695e-01f, 1.265485583e-08f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-5.659599900e-01f, 1.626348123e-08f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.965480894e-01f, -5.885435694e-09f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_4_1(ff t) {
+  const float tail = fmaf(fmaf(fmaf(-4.590114570e-14f, t.hi, 2.990587812e-12f), t.hi, -1.618607470e-10f), t.hi, 7.149236758e-09f);
+  ff y = ff_add_f(ff_make(-2.515456003e-07f, -1.224162170e-14f), t.hi * tail);
+  y = ff_add_fast(ff_make(6.843098618e-06f, -1.537591262e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.384226052e-04f, -4.621060912e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.973692561e-03f, 1.102912692e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.835270040e-02f, -2.126934046e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(9.827404469e-02f, 2.942717847e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-2.397640347e-01f, -6.327427915e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.414899975e-01f, -4.065870307e-09f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_4_2(ff t) {
+  const float tail = fmaf(fmaf(fmaf(-3.123848023e-14f, t.hi, 2.161122843e-12f), t.hi, -1.248063597e-10f), t.hi, 5.915436141e-09f);
+  ff y = ff_add_f(ff_make(-2.248562510e-07f, -7.426550359e-16f), t.hi * tail);
+  y = ff_add_fast(ff_make(6.662166470e-06f, 1.510437410e-15f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.482141961e-04f, -3.824222623e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.351704985e-03f, -2.312123062e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-2.466011606e-02f, 5.956617422e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.503964961e-01f, -6.117502505e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-4.036971033e-01f, -5.002281256e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(5.092768744e-02f, 7.692527726e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(5.583839417e-01f, -2.265648646e-08f), ff_mul(t, y));
+  return y;
+}
+__host__ __device__ __forceinline__ ff hkff_4_3(ff t) {
+  const float tail = fmaf(fmaf(fmaf(fmaf(-1.229939591e-15f, t.hi, 9.248676857e-14f), t.hi, -5.851945664e-12f), t.hi, 3.067759657e-10f), t.hi, -1.305164243e-08f);
+  ff y = ff_add_f(ff_make(4.394457278e-07f, 1.166257748e-15f), t.hi * tail);
+  y = ff_add_fast(ff_make(-1.133734986e-05f, 4.390675920e-13f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.146563056e-04f, 4.818976381e-12f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-2.806317061e-03f, 2.627576282e-11f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(2.306634001e-02f, -2.263386423e-10f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(-1.007763892e-01f, -2.230016616e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(1.516679525e-01f, -6.702047806e-09f), ff_mul(t, y));
+  y = ff_add_fast(ff_make(8.248634636e-02f, 3.589323505e-09f), ff_mul(t, y));
+  return y;
+}
+
 }  // namespace bem2d_gpu

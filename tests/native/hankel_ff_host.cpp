@@ -33,3 +33,23 @@ extern "C" void hankel01_ff_host(int n, const double* x, double* out) {
     out[4 * i + 3] = -ff_to_double(ff_mul(amp, h1.re));
   }
 }
+
+// out[4i..4i+3] = J0, Y0, J1, Y1 at x[i] > 0 through bessel01_ff (both the
+// small-argument and the modulus-phase branch)
+extern "C" void bessel01_ff_host(int n, const double* x, double* out) {
+  float tab[256];
+  expi_table(tab);
+  for (int i = 0; i < n; ++i) {
+    const ff xf = ff_from_double(x[i]);
+    const BesselFF b = bessel01_ff(xf, ff_rcp(xf), tab);
+    out[4 * i] = ff_to_double(b.j0);
+    out[4 * i + 1] = ff_to_double(b.y0);
+    out[4 * i + 2] = ff_to_double(b.j1);
+    out[4 * i + 3] = ff_to_double(b.y1);
+  }
+}
+
+// out[i] = log(x[i]) through ff_log
+extern "C" void log_ff_host(int n, const double* x, double* out) {
+  for (int i = 0; i < n; ++i) out[i] = ff_to_double(ff_log(ff_from_double(x[i])));
+}

@@ -78,7 +78,50 @@ def hkff(tmp_path_factory):
         lib.hankel01_ff_host(ctypes.c_int(len(x)), x.ctypes.data_as(ctypes.c_void_p),
                              o.ctypes.data_as(ctypes.c_void_p))
         return o[:, 0] + 1j * o[:, 1], o[:, 2] + 1j * o[:, 3]
+
+    def b(x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        o = np.zeros((len(x), 4))
+        lib.bessel01_ff_host(ctypes.c_int(len(x)), x.ctypes.data_as(ctypes.c_void_p),
+                             o.ctypes.data_as(ctypes.c_void_p))
+        return o
+
+    def lg(x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        o = np.zeros(len(x))
+        lib.log_ff_host(ctypes.c_int(len(x)), x.ctypes.data_as(ctypes.c_void_p),
+                        o.ctypes.data_as(ctypes.c_void_p))
+        return o
+    f.bessel = b
+    f.log = lg
     return f
+
+
+def _ff_round(x):
+    """x rounded to the nearest float-float (as the evaluators receive it)."""
+    hi = x.astype(np.float32).astype(np.float64)
+    return hi + (x - hi).astype(np.float32).astype(np.float64)
+
+
+def test_float_float_small_argument_against_mpmath(hkff):
+    """bessel01_ff over 1e-7 <= x <= 40, with the small-argument branch
+    (x <= 4: series form and the float-float logarithm) and the join at 4:
+    J0, Y0, J1, Y1 within 3e-14 of max(1, |value|) and ff_log within 1e-13
+    absolute, both at the float-float-rounded argument."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(5)
+    x = _ff_round(np.concatenate([10 ** rng.uniform(-7, np.log10(40), 800),
+                                  np.linspace(3.99, 4.01, 41), np.linspace(0.85, 0.95, 21)]))
+    o = hkff.bessel(x)
+    ref = np.array([[float(mp.besselj(0, mp.mpf(v))), float(mp.bessely(0, mp.mpf(v))),
+                     float(mp.besselj(1, mp.mpf(v))), float(mp.bessely(1, mp.mpf(v)))]
+                    for v in x])
+    err = np.abs(o - ref) / np.maximum(1.0, np.abs(ref))
+    assert err.max() < 3e-14, (err.max(axis=0), x[err.argmax() // 4])
+    lg = hkff.log(x)
+    lref = np.array([float(mp.log(mp.mpf(v))) for v in x])
+    assert np.abs(lg - lref).max() < 1e-13
 
 
 def test_float_float_against_mpmath(hkff):
