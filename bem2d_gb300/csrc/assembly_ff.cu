@@ -43,32 +43,19 @@ __device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KCo
   return h;
 }
 
-// Kernel value from the shared terms.  dot: the normal factor of the
-// double-layer kernels (n_x . (x - y) for the adjoint double layer at
-// (x, y), n_y . (y - x) for the double layer); unused by SINGLE.
-template <int KERNEL>
-__device__ __forceinline__ ffc kernel_from_terms(const HankelTermsFF& h, ff dot,
-                                                 const KConstFF& kc) {
-  ffc F;
-  if (KERNEL == BEM2D_KERNEL_SINGLE) {
-    // (i/4) H0:  F = (i/4)(P0 + i Q0)
-    F.re = ff_scale2(ff_neg(h.q0), 0.25f);
-    F.im = ff_scale2(h.p0, 0.25f);
-  } else {
-    const ff cc = ff_mul(ff_mul(dot, h.y), kc.kq);  // (k/4) n.w/d
-    // -i (k/4) c H1 with H1 = -i amp (P1 + i Q1) E  ->  -(k/4) c (P1 + i Q1)
-    F.re = ff_neg(ff_mul(cc, h.p1));
-    F.im = ff_neg(ff_mul(cc, h.q1));
-    if (KERNEL == BEM2D_KERNEL_COMBINED) {
-      F.re = ff_add_fast(F.re, ff_mul(kc.eq, h.p0));
-      F.im = ff_add_fast(F.im, ff_mul(kc.eq, h.q0));
-    }
-  }
-  // K = amp E F
-  ffc K;
-  K.re = ff_mul(h.amp, ff_add_fast(ff_mul(h.e.re, F.re), ff_neg(ff_mul(h.e.im, F.im))));
-  K.im = ff_mul(h.amp, ff_add_fast(ff_mul(h.e.re, F.im), ff_mul(h.e.im, F.re)));
-  return K;
+// E (P + i Q) and a complex value times a real one (ff).
+__device__ __forceinline__ ffc ffc_mul_pq(const ffc& e, ff p, ff q) {
+  ffc r;
+  r.re = ff_add_fast(ff_mul(e.re, p), ff_neg(ff_mul(e.im, q)));
+  r.im = ff_add_fast(ff_mul(e.re, q), ff_mul(e.im, p));
+  return r;
+}
+
+__device__ __forceinline__ ffc ffc_scale(const ffc& z, ff a) {
+  ffc r;
+  r.re = ff_mul(z.re, a);
+  r.im = ff_mul(z.im, a);
+  return r;
 }
 
 // One entry in FP64 from the FP64 node table (deferred entries).
@@ -232,30 +219,42 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
         const ff dx = ff_add_fast(Dx, ff_add_fast(ox1, ff_make(-b0.x, -b0.y)));
         const ff dy = ff_add_fast(Dy, ff_add_fast(oy1, ff_make(-b1.x, -b1.y)));
         const HankelTermsFF h = hankel_terms_ff(dx, dy, kc, tab);
-        const ff ww = ff_mul(w1, ff_make(b4.x, b4.y));
-        ff dot_rc = ff_make(0.0f, 0.0f), dot_cr = ff_make(0.0f, 0.0f);
-        if (KERNEL != BEM2D_KERNEL_SINGLE) {
+        const ff aw = ff_mul(h.amp, ff_mul(w1, ff_make(b4.x, b4.y)));  // amp w_x w_y
+        if (KERNEL == BEM2D_KERNEL_SINGLE) {
+          // K w_x w_y = (i/4) aw E (P0 + i Q0), the same in both orientations
+          const ffc Z = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_scale2(aw, 0.25f));
+          if (rc) {
+            arc.re = ff_add_fast(arc.re, ff_neg(Z.im));
+            arc.im = ff_add_fast(arc.im, Z.re);
+          }
+          if (cr) {
+            acr.re = ff_add_fast(acr.re, ff_neg(Z.im));
+            acr.im = ff_add_fast(acr.im, Z.re);
+          }
+        } else {
+          // K w_x w_y = Z0 - dot Z1 with Z1 = aw (k/4)/d E (P1 + i Q1) and, for
+          // the combined operator, Z0 = aw (eta/4) E (P0 + i Q0); dot is the
+          // orientation's normal factor (n_y . (y - x) for the double layer
+          // at (x, y), n_x . (x - y) otherwise)
+          const ffc Z1 = ffc_scale(ffc_mul_pq(h.e, h.p1, h.q1), ff_mul(aw, ff_mul(kc.kq, h.y)));
+          ffc Z0;
+          Z0.re = Z0.im = ff_make(0.0f, 0.0f);
+          if (KERNEL == BEM2D_KERNEL_COMBINED)
+            Z0 = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(aw, kc.eq));
           const ff n1w = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));  // n_x . (x - y)
           const ff n2w = ff_add_fast(ff_mul(ff_make(b2.x, b2.y), dx),
                                      ff_mul(ff_make(b3.x, b3.y), dy));  // n_y . (x - y)
-          if (KERNEL == BEM2D_KERNEL_DOUBLE) {
-            dot_rc = ff_neg(n2w);  // (row, col): n_y . (y - x)
-            dot_cr = n1w;          // (col, row): n_x . (x - y)
-          } else {
-            dot_rc = n1w;          // (row, col): n_x . (x - y)
-            dot_cr = ff_neg(n2w);  // (col, row): n_y . (y - x)
+          // (row, col): -dot = n2w (double layer) or -n1w; (col, row): the reverse
+          const ff m_rc = KERNEL == BEM2D_KERNEL_DOUBLE ? n2w : ff_neg(n1w);
+          const ff m_cr = KERNEL == BEM2D_KERNEL_DOUBLE ? ff_neg(n1w) : n2w;
+          if (rc) {
+            arc.re = ff_add_fast(arc.re, ff_add_fast(Z0.re, ff_mul(m_rc, Z1.re)));
+            arc.im = ff_add_fast(arc.im, ff_add_fast(Z0.im, ff_mul(m_rc, Z1.im)));
           }
-        }
-        if (rc) {
-          const ffc K = kernel_from_terms<KERNEL>(h, dot_rc, kc);
-          arc.re = ff_add_fast(arc.re, ff_mul(K.re, ww));
-          arc.im = ff_add_fast(arc.im, ff_mul(K.im, ww));
-        }
-        if (cr) {
-          const ffc K = KERNEL == BEM2D_KERNEL_SINGLE ? kernel_from_terms<KERNEL>(h, dot_rc, kc)
-                                                      : kernel_from_terms<KERNEL>(h, dot_cr, kc);
-          acr.re = ff_add_fast(acr.re, ff_mul(K.re, ww));
-          acr.im = ff_add_fast(acr.im, ff_mul(K.im, ww));
+          if (cr) {
+            acr.re = ff_add_fast(acr.re, ff_add_fast(Z0.re, ff_mul(m_cr, Z1.re)));
+            acr.im = ff_add_fast(acr.im, ff_add_fast(Z0.im, ff_mul(m_cr, Z1.im)));
+          }
         }
       }
     }

@@ -333,6 +333,9 @@ cudaStream_t ctx_stream(const bem2d_ctx* c);
 long long* ctx_launches(bem2d_ctx* c);
 // Worker contexts (own stream and workspace each) of the batched sweep.
 std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c);
+// Makes c a sweep worker: a high-priority stream for the factor/solve phase
+// of its scattering solves and throughput-sized LU panels.
+int ctx_make_sweep_worker(bem2d_ctx* c);
 // Records msg as the context's last error and returns code.
 int ctx_fail(bem2d_ctx* c, int code, const char* msg);
 
@@ -349,6 +352,11 @@ struct LuWork {
   void* pack = nullptr;
   size_t pack_bytes = 0;
   void* dinv;            // inverses of the 64 x 64 diagonal blocks of L and U
+  // complex64 register-window panel: minimum rows per CTA (0: the default,
+  // which spreads a panel over up to 16 CTAs for the shortest column chain;
+  // larger values use fewer, fuller CTAs, so that more panels of concurrent
+  // factorisations fit on the GPU at once)
+  int min_rows = 0;
 };
 
 // Bytes of LuWork::scratch the panel kernels need for n unknowns.

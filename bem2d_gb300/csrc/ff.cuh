@@ -31,6 +31,16 @@ __host__ __device__ __forceinline__ ff ff_make(float h, float l) {
   return r;
 }
 
+// Round-to-nearest product that the compiler may not contract into a later
+// add (an error-free transformation needs the rounded product itself).
+__host__ __device__ __forceinline__ float f_mul_rn(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
 // s + e = a + b exactly (any magnitudes)
 __host__ __device__ __forceinline__ ff two_sum(float a, float b) {
   const float s = a + b;
@@ -48,7 +58,7 @@ __host__ __device__ __forceinline__ ff fast_two_sum(float a, float b) {
 
 // p + e = a * b exactly
 __host__ __device__ __forceinline__ ff two_prod(float a, float b) {
-  const float p = a * b;
+  const float p = f_mul_rn(a, b);
   const float e = fmaf(a, b, -p);
   return ff_make(p, e);
 }
@@ -90,7 +100,7 @@ __host__ __device__ __forceinline__ ff ff_add_f(ff a, float b) {
 }
 
 __host__ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  const float p = a.hi * b.hi;
+  const float p = f_mul_rn(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e = fmaf(a.hi, b.lo, e);
   e = fmaf(a.lo, b.hi, e);
@@ -98,17 +108,31 @@ __host__ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
 }
 
 __host__ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
-  const float p = a.hi * b;
+  const float p = f_mul_rn(a.hi, b);
   float e = fmaf(a.hi, b, -p);
   e = fmaf(a.lo, b, e);
   return fast_two_sum(p, e);
 }
 
 __host__ __device__ __forceinline__ ff ff_sqr(ff a) {
-  const float p = a.hi * a.hi;
+  const float p = f_mul_rn(a.hi, a.hi);
   float e = fmaf(a.hi, a.hi, -p);
   e = fmaf(a.hi + a.hi, a.lo, e);
   return fast_two_sum(p, e);
+}
+
+// One Horner step c + t y when |c.hi| >= |t y| is known in advance (the
+// polynomial generator checks |c_k| >= sum_{j>k} |c_j| for |t| <= 1): the
+// product is left unnormalised and c.hi + p is split by a fast two-sum.
+// Same accuracy as ff_add_fast(c, ff_mul(t, y)), fewer operations.
+__host__ __device__ __forceinline__ ff ff_horner_fast(ff c, ff t, ff y) {
+  const float p = f_mul_rn(t.hi, y.hi);
+  float e = fmaf(t.hi, y.hi, -p);
+  e = fmaf(t.hi, y.lo, e);
+  e = fmaf(t.lo, y.hi, e);
+  const float s = c.hi + p;
+  const float err = p - (s - c.hi);
+  return fast_two_sum(s, err + (e + c.lo));
 }
 
 // exact scaling by a power of two
@@ -154,8 +178,9 @@ __host__ __device__ __forceinline__ ff ff_rcp(ff a) {
 // [sqrt(1/2), sqrt(2)); log m = 2 atanh(u) = 2 (u + u^3/3 + u^5/5 + ...),
 // u = (m - 1)/(m + 1), |u| <= 0.172, so u^2 <= 0.0295.  m - 1 is exact
 // (Sterbenz), which keeps the relative accuracy of log m near m = 1.  The
-// series terms through u^8/9 are carried in ff, the rest (below 2e-9) in
-// FP32; log 2 is the ff pair nearest to it.
+// series terms through u^8/9 are carried in ff (each coefficient bounds the
+// rest of the series, so the fast Horner step applies), the rest (below
+// 2e-9) in FP32; log 2 is the ff pair nearest to it.
 __host__ __device__ __forceinline__ ff ff_log(ff a) {
   int e;
   float m = frexpf(a.hi, &e);  // a.hi = m 2^e, m in [1/2, 1)
@@ -174,10 +199,10 @@ __host__ __device__ __forceinline__ ff ff_log(ff a) {
                                                  1.0f / 21.0f), 1.0f / 19.0f), 1.0f / 17.0f),
                          1.0f / 15.0f), 1.0f / 13.0f) + 1.0f / 11.0f;
   ff s = ff_add_f(ff_make(0.1111111119389534f, -8.278422947149977e-10f), v * tail);  // 1/9
-  s = ff_add_fast(ff_make(0.1428571492433548f, -6.38621200366174e-09f), ff_mul(u2, s));  // 1/7
-  s = ff_add_fast(ff_make(0.20000000298023224f, -2.9802322831784522e-09f), ff_mul(u2, s));  // 1/5
-  s = ff_add_fast(ff_make(0.3333333432674408f, -9.934107758624577e-09f), ff_mul(u2, s));     // 1/3
-  s = ff_add_fast(ff_make(1.0f, 0.0f), ff_mul(u2, s));
+  s = ff_horner_fast(ff_make(0.1428571492433548f, -6.38621200366174e-09f), u2, s);  // 1/7
+  s = ff_horner_fast(ff_make(0.20000000298023224f, -2.9802322831784522e-09f), u2, s);  // 1/5
+  s = ff_horner_fast(ff_make(0.3333333432674408f, -9.934107758624577e-09f), u2, s);     // 1/3
+  s = ff_horner_fast(ff_make(1.0f, 0.0f), u2, s);
   const ff lm = ff_mul(ff_scale2(u, 2.0f), s);
   const ff l2 = ff_mul_f(ff_make(0.6931471824645996f, -1.9046542121259336e-09f), (float)e);
   return ff_add(l2, lm);

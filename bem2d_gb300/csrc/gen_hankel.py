@@ -144,7 +144,8 @@ FF_TAIL_BOUND = 1.5e-8
 def emit_ff_polys(idx, polys):
     """Compensated evaluation of monomial polynomials in t (|t| <= 1): the
     tail sum_{k>=m} c_k t^(k-m), bounded by FF_TAIL_BOUND, in FP32 Horner on
-    t.hi; the head c_0 .. c_{m-1} in float-float Horner."""
+    t.hi; the head c_0 .. c_{m-1} in float-float Horner, with the cheaper
+    ff_horner_fast step wherever |c_k| bounds the rest of the polynomial."""
     out = []
     for i, p in enumerate(polys):
         tails = [sum(abs(v) for v in p[k:]) for k in range(len(p))] + [0]
@@ -161,9 +162,15 @@ def emit_ff_polys(idx, polys):
         else:
             hi, lo = split_ff(p[m - 1])
             lines.append("  ff y = ff_make(%.9ef, %.9ef);" % (hi, lo))
-        for c in reversed(p[:m - 1]):
-            hi, lo = split_ff(c)
-            lines.append("  y = ff_add_fast(ff_make(%.9ef, %.9ef), ff_mul(t, y));" % (hi, lo))
+        for kk in reversed(range(m - 1)):
+            hi, lo = split_ff(p[kk])
+            # |y| <= sum_{j>kk} |c_j| on |t| <= 1; the fast step needs
+            # |c_kk| >= |t y| (margin for the float rounding of c_kk)
+            if abs(p[kk]) >= tails[kk + 1] * (1 + 1e-6):
+                lines.append("  y = ff_horner_fast(ff_make(%.9ef, %.9ef), t, y);" % (hi, lo))
+            else:
+                lines.append("  y = ff_add_fast(ff_make(%.9ef, %.9ef), ff_mul(t, y));"
+                             % (hi, lo))
         lines.append("  return y;")
         lines.append("}")
         out.append("\n".join(lines))

@@ -1191,8 +1191,9 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     const int rows_target = sizeof(T) == sizeof(float2) ? kPanelThreads : 64;
     bool done = false;
     if (sizeof(T) == sizeof(float2)) {  // register-window panel
+      const int min_rpb = std::min(kWinMaxRows, w.min_rows > 0 ? w.min_rows : kRowsMinRpb);
       for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
-        int C = std::max(1, std::min(cmax, (H + kRowsMinRpb - 1) / kRowsMinRpb));
+        int C = std::max(1, std::min(cmax, (H + min_rpb - 1) / min_rpb));
         while ((H + C - 1) / C > kWinMaxRows) ++C;
         if (C > cmax) continue;
         const int rpb = (H + C - 1) / C;

@@ -10,7 +10,11 @@
 // order) and run the complete single-problem path on their stream.  Small
 // problems do not fill the 152 SMs on their own (their LU is bound by the
 // latency of the panel steps), so several in flight at once keep the GPU
-// busy; the largest items start first so the tail is short.
+// busy; the largest items start first so the tail is short.  A worker's
+// assembly kernels (grids of thousands of CTAs) run on its normal stream,
+// its factorisation and solve on a high-priority one: the block scheduler
+// then gives SM slots freed by one worker's assembly to another worker's
+// panel chain first, instead of queueing that chain behind the whole grid.
 //
 // The worker contexts live in the parent context and keep their workspaces
 // between calls, so a repeated sweep allocates nothing after the first.
@@ -27,7 +31,7 @@
 #include "common.cuh"
 
 namespace {
-constexpr int kDefaultWorkers = 8;
+constexpr int kDefaultWorkers = 16;
 constexpr int kMaxWorkers = 32;
 }  // namespace
 
@@ -51,6 +55,8 @@ extern "C" int bem2d_sweep_solve(bem2d_ctx* c, int nk, const bem2d_geometry* geo
     const int rc = bem2d_ctx_create(ctx_device(c), &w);
     if (rc) return ctx_fail(c, rc, "could not create a sweep worker context");
     workers.push_back(w);
+    if (ctx_make_sweep_worker(w) != BEM2D_OK)
+      return ctx_fail(c, BEM2D_ERR_CUDA, bem2d_ctx_last_error(w));
   }
   // largest problems first
   std::vector<int> order(nk);

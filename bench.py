@@ -44,7 +44,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 QUAD = (3, 5, 0.15)
-SWEEP_WORKERS = 8
+SWEEP_WORKERS = 16
 
 
 def workload(name):
@@ -302,6 +302,9 @@ def run_only(args):
     A = torch.empty((n, n), dtype=torch.complex128, device="cuda") \
         if args.only == "assembly" else None
     x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    if args.only == "sweep":  # as the headline: geometry staged once, device results
+        holds = [capi._GeomHold(p[0]) for p in probs]
+        outs = [torch.zeros(h.n, dtype=torch.complex128, device="cuda") for h in holds]
     step_ms = []
     for it in range(args.warmup + args.steps):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -311,8 +314,8 @@ def run_only(args):
         if args.only == "assembly":
             ctx.discrete_kernel(arrays, "combined", k, eta, QUAD, 2.0, 1.0, out=A)
         elif args.only == "sweep":
-            ctx.sweep_solve([p[0] for p in probs], [p[1] for p in probs], w["d"],
-                            [p[2] for p in probs], QUAD, "mixed", nworkers=args.workers)
+            ctx.sweep_solve(holds, [p[1] for p in probs], w["d"], [p[2] for p in probs], QUAD,
+                            "mixed", nworkers=args.workers, outs=outs)
         else:
             ctx.scattering_solve(arrays, k, w["d"], eta, QUAD, precision=args.only, out=x)
         e1.record()

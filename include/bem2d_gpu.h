@@ -248,8 +248,9 @@ int bem2d_scattering_solve(bem2d_ctx* ctx, const bem2d_geometry* geom,
  * (geoms[i], k[i], eta[i] or k[i] if eta is NULL; one incident direction):
  * replaces the serial per-wavenumber loop of the reference's sweeps
  * (normcomps/ellipsenormcond.cpp:66-128, which rebuilds the geometry and
- * the system for every k).  nworkers (<= 0: 8) host workers, each with its
- * own stream and workspace, run the problems concurrently, largest first.
+ * the system for every k).  nworkers (<= 0: 16) host workers, each with its
+ * own streams and workspace, run the problems concurrently, largest first;
+ * a worker's factorisation and solve run on a high-priority stream.
  * x[i] (geoms[i].n_unk complex128, host or device) and infos[i] (may be
  * NULL) receive each solution; results equal bem2d_scattering_solve's.
  * Returns when every problem is done; on failure the first error (the
