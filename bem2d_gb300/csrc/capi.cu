@@ -1048,6 +1048,9 @@ struct LzNames<double2> {
   static constexpr const char* W = "nr_W";
   static constexpr const char* h = "nr_h";
   static constexpr const char* sc = "nr_sc";
+  static constexpr const char* Q2 = "nr_Q2";
+  static constexpr const char* W2 = "nr_W2";
+  static constexpr const char* Z = "nr_Z";
 };
 template <>
 struct LzNames<float2> {
@@ -1057,6 +1060,9 @@ struct LzNames<float2> {
   static constexpr const char* W = "nr32_W";
   static constexpr const char* h = "nr32_h";
   static constexpr const char* sc = "nr32_sc";
+  static constexpr const char* Q2 = "nr32_Q2";
+  static constexpr const char* W2 = "nr32_W2";
+  static constexpr const char* Z = "nr32_Z";
 };
 
 // Batched Lanczos (full reorthogonalisation, two Gram-Schmidt passes) for
@@ -1069,7 +1075,9 @@ struct LzNames<float2> {
 template <typename T>
 static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int nang,
                             const double* dth, double tol, int mmax, const double2* start,
-                            double* lam_out, T* ritz, bool full_reorth = true) {
+                            double* lam_out, T* ritz, bool full_reorth = true,
+                            double rtol = 0.0, double etol = 0.0,
+                            const double* gap_in = nullptr, double* gap_out = nullptr) {
   int rc = 0;
   const long long qs = (long long)n * (mmax + 1);  // per-angle basis stride
   T* Q = static_cast<T*>(ws(c, LzNames<T>::Q, sizeof(T) * (size_t)qs * nang, &rc));
@@ -1102,70 +1110,200 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // v0t is released below
   }
   std::vector<std::vector<double>> al(nang), be(nang);
-  std::vector<double> lam(nang, 0.0), prev(nang, NAN);
+  std::vector<double> lam(nang, 0.0), prev(nang, NAN), dlam(nang, 0.0);
   std::vector<int> stable(nang, 0);
   std::vector<T> hh((size_t)(mmax + 2) * nang);
   const int ldh = mmax + 2;
   int steps = 0;
+  // Deflation: an angle whose value has converged leaves the batch (its
+  // Ritz vector, if wanted, is formed on the way out), and the others are
+  // gathered to the front slots (basis and next vector, into a second
+  // buffer), so later steps cost in proportion to the angles still
+  // iterating.  slot_angle[s]: the angle of slot s; na: slots in use.
+  std::vector<int> slot_angle(nang);
+  for (int a = 0; a < nang; ++a) slot_angle[a] = a;
+  int na = nang;
+  T* Qalt = static_cast<T*>(ws(c, LzNames<T>::Q2, sizeof(T) * (size_t)qs * nang, &rc));
+  T* Walt = static_cast<T*>(ws(c, LzNames<T>::W2, sizeof(T) * (size_t)n * nang, &rc));
+  int* dmap = static_cast<int*>(ws(c, "nr_map", sizeof(int) * 2 * nang, &rc));
+  double* dthc = static_cast<double*>(ws(c, "nr_thc", sizeof(double) * nang, &rc));
+  if (!Qalt || !Walt || !dmap || !dthc) return rc;
+  // K-split partials of the products: the most any batch width needs
+  size_t zwork_bytes = 0;
+  for (int m = 1; m <= nang; ++m) zwork_bytes = std::max(zwork_bytes, zgemm_work_bytes(n, m, sizeof(T)));
+  void* zwork = zwork_bytes ? ws(c, LzNames<T>::Z, zwork_bytes, &rc) : nullptr;
+  if (zwork_bytes && !zwork) return rc;
+  std::vector<double> th_h(nang);
+  CUDA_TRY(c, cudaMemcpyAsync(th_h.data(), dth, sizeof(double) * nang, cudaMemcpyDeviceToHost,
+                              c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(dthc, dth, sizeof(double) * nang, cudaMemcpyDeviceToDevice,
+                              c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const double* theta = dthc;
+  // Ritz vectors u = Q_s y_s of slots sl (y the unit eigenvector of T_s for
+  // lambda_max, st steps) into ritz[angle]: the slots' bases gathered to
+  // Qalt, W' = 0 - Qalt (-y), scattered to the angles' columns
+  auto emit_ritz = [&](const std::vector<int>& sl, int st) -> int {
+    const int m = (int)sl.size();
+    if (!ritz || m == 0) return BEM2D_OK;
+    std::vector<int> ang(m);
+    for (int i = 0; i < m; ++i) {
+      const int a = sl[i];
+      std::vector<double> e(be[a].begin(), be[a].begin() + (st - 1));
+      const std::vector<double> sv = tridiag_eigenvector(al[a], e, lam[a]);
+      if (gap_out)
+        gap_out[slot_angle[a]] =
+            st > 1 ? lam[a] - tridiag_kth_largest(al[a], e, 2, 1e-6) : 0.0;
+      for (int r = 0; r < st; ++r)
+        hh[(size_t)i * ldh + r] = {(decltype(hh[0].x))(-sv[r]), (decltype(hh[0].x))0};
+      ang[i] = slot_angle[a];
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(h, hh.data(), sizeof(T) * (size_t)ldh * m, cudaMemcpyHostToDevice,
+                                c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(dmap, sl.data(), sizeof(int) * m, cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(dmap + nang, ang.data(), sizeof(int) * m, cudaMemcpyHostToDevice,
+                                c->stream));
+    launch_gather_slots(Q, qs, Qalt, qs, (long long)st * n, dmap, m, c->stream);
+    CUDA_TRY(c, cudaMemsetAsync(Walt, 0, sizeof(T) * (size_t)n * m, c->stream));
+    launch_batched_sub(Qalt, qs, n, st, Walt, n, h, ldh, m, c->stream);
+    launch_scatter_slots(Walt, (long long)n, ritz, (long long)n, (long long)n, dmap + nang, m,
+                         c->stream);
+    c->launches += 3;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // hh, sl, ang are host memory
+    return BEM2D_OK;
+  };
   for (int j = 0; j < mmax; ++j) {
     const T* Qj = Q + (size_t)j * n;
-    launch_zgemm(false, dA, la, n, Qj, qs, nang, Y1, n, c->stream);
-    launch_zgemm(true, dA, la, n, Qj, qs, nang, Y2, n, c->stream);
-    launch_herm_combine(n, Y1, Y2, n, dth, W, n, nang, c->stream);
+    launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
+    launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+    launch_herm_combine(n, Y1, Y2, n, theta, W, n, na, c->stream);
     // Gram-Schmidt (two passes) against q_0..q_j, or, without full
     // reorthogonalisation, against q_{j-1}, q_j only (the three-term
     // recurrence: the extreme Ritz value converges all the same)
     const int w0 = full_reorth ? 0 : std::max(0, j - 1), nw = j + 1 - w0;
     const T* Qw = Q + (size_t)w0 * n;
-    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(hh.data(), h, sizeof(T) * (size_t)ldh * nang, cudaMemcpyDeviceToHost, c->stream));
-    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
-    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
-    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, nang, c->stream);
-    launch_batched_norm2(n, W, n, sc, nang, c->stream);
-    CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * nang, cudaMemcpyDeviceToHost, c->stream));
+    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, na, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(hh.data(), h, sizeof(T) * (size_t)ldh * na, cudaMemcpyDeviceToHost, c->stream));
+    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, na, c->stream);
+    launch_batched_dots(Qw, qs, n, nw, W, n, h, ldh, na, c->stream);
+    launch_batched_sub(Qw, qs, n, nw, W, n, h, ldh, na, c->stream);
+    launch_batched_norm2(n, W, n, sc, na, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(nn.data(), sc, sizeof(double) * na, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->launches += 8;
     CHECK_LAUNCH(c);
     steps = j + 1;
-    bool all = true;
-    for (int a = 0; a < nang; ++a) {
+    for (int a = 0; a < na; ++a) {
       al[a].push_back(hh[(size_t)a * ldh + (j - w0)].x);
       const double b = std::sqrt(nn[a]);
       inv[a] = b > 1e-300 ? 1.0 / b : 0.0;
-      lam[a] = tridiag_lmax(al[a], be[a]);
+      // Ritz values interlace: the previous value bounds the new one below.
+      // The value is resolved to 1e-4 of its last change (to roundoff once
+      // it has settled), which is all the convergence tests need.
+      {
+        const double lp = lam[a];
+        lam[a] = j == 0 ? al[a][0]
+                        : tridiag_lmax_from(al[a], be[a], lp, 2.0 * dlam[a], 1e-4 * dlam[a]);
+        dlam[a] = j == 0 ? std::fabs(lam[a]) : std::fabs(lam[a] - lp);
+      }
       const double scale = std::max(std::fabs(lam[a]), 1e-300);
-      if (std::fabs(lam[a] - prev[a]) <= tol * scale || b <= 1e-300) {
+      if (rtol > 0 || etol > 0) {
+        // Ritz-pair criteria, relative to the size of H seen so far
+        // (hs = max |lambda|, |alpha_i|, beta_i), with r = beta_{j+1} |s_j|
+        // the residual estimate (s the unit eigenvector of T for
+        // lambda_max), computed once the value has settled to 1e-5:
+        //  rtol: r <= rtol hs (the Ritz vector has converged);
+        //  etol: the value has moved by at most etol hs in this step and
+        //        the error estimate min(r, r^2 / (theta_1 - theta_2)) is at
+        //        most etol hs (for Hermitian H an eigenvalue lies within r
+        //        of the Ritz value, within r^2 / gap for an isolated one).
+        bool conv = b <= 1e-300;
+        const bool warm = gap_in != nullptr;
+        if (!conv && (warm || (j >= 3 && std::fabs(lam[a] - prev[a]) <= 1e-5 * scale))) {
+          double hs = scale;
+          for (const double v : al[a]) hs = std::max(hs, std::fabs(v));
+          for (const double v : be[a]) hs = std::max(hs, v);
+          const std::vector<double> sv = tridiag_eigenvector(al[a], be[a], lam[a]);
+          const double r = b * std::fabs(sv[j]);
+          if (rtol > 0) {
+            conv = r <= rtol * hs;
+          } else if (warm || std::fabs(lam[a] - prev[a]) <= etol * hs) {
+            // gap to the rest of the spectrum: the smaller of the warm
+            // start's estimate and this tridiagonal's theta_1 - theta_2
+            double gap = warm ? gap_in[slot_angle[a]] : INFINITY;
+            if (j >= 1) gap = std::min(gap, lam[a] - tridiag_kth_largest(al[a], be[a], 2, 1e-6));
+            conv = std::min(r, gap > 0 ? r * r / gap : r) <= etol * hs;
+          }
+        }
+        stable[a] = conv ? 2 : 0;
+      } else if (std::fabs(lam[a] - prev[a]) <= tol * scale || b <= 1e-300) {
         ++stable[a];
       } else {
         stable[a] = 0;
       }
       prev[a] = lam[a];
       be[a].push_back(b);
-      if (stable[a] < 2 || j < 3) all = false;
     }
-    if (all) break;
+    {
+      std::vector<int> keep, done;
+      keep.reserve(na);
+      for (int a = 0; a < na; ++a) {
+        if (stable[a] >= 2 && (j >= 3 || gap_in)) {
+          lam[a] = tridiag_lmax_from(al[a], be[a], lam[a], 0.0, 0.0);  // to roundoff
+          lam_out[slot_angle[a]] = lam[a];
+          done.push_back(a);
+        } else {
+          keep.push_back(a);
+        }
+      }
+      if ((rc = emit_ritz(done, j + 1))) return rc;
+      if (keep.empty()) {
+        na = 0;
+        break;
+      }
+      if ((int)keep.size() < na) {
+        const int nk = (int)keep.size();
+        for (int i = 0; i < nk; ++i) {
+          const int a = keep[i];
+          if (a == i) continue;
+          al[i] = std::move(al[a]);
+          be[i] = std::move(be[a]);
+          lam[i] = lam[a];
+          dlam[i] = dlam[a];
+          prev[i] = prev[a];
+          stable[i] = stable[a];
+          inv[i] = inv[a];
+          slot_angle[i] = slot_angle[a];
+          th_h[i] = th_h[a];
+        }
+        CUDA_TRY(c, cudaMemcpyAsync(dmap, keep.data(), sizeof(int) * nk, cudaMemcpyHostToDevice,
+                                    c->stream));
+        CUDA_TRY(c, cudaMemcpyAsync(dthc, th_h.data(), sizeof(double) * nk,
+                                    cudaMemcpyHostToDevice, c->stream));
+        launch_gather_slots(Q, qs, Qalt, qs, (long long)(j + 1) * n, dmap, nk, c->stream);
+        launch_gather_slots(W, (long long)n, Walt, (long long)n, (long long)n, dmap, nk,
+                            c->stream);
+        c->launches += 2;
+        std::swap(Q, Qalt);
+        std::swap(W, Walt);
+        na = nk;
+        // keep.data() and th_h are read by the copies above
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      }
+    }
     // q_{j+1} = w / beta
-    CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
-    launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, nang, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * na, cudaMemcpyHostToDevice, c->stream));
+    launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, na, c->stream);
     ++c->launches;
   }
-  for (int a = 0; a < nang; ++a) lam_out[a] = lam[a];
-  if (ritz) {
-    // u_a = Q_a s_a, s_a the eigenvector of T_a for lambda_max: W = 0,
-    // W -= Q (-s)
-    for (int a = 0; a < nang; ++a) {
-      std::vector<double> e(be[a].begin(), be[a].begin() + (steps - 1));
-      const std::vector<double> sv = tridiag_eigenvector(al[a], e, lam[a]);
-      for (int i = 0; i < steps; ++i)
-        hh[(size_t)a * ldh + i] = {(decltype(hh[0].x))(-sv[i]), (decltype(hh[0].x))0};
-    }
-    CUDA_TRY(c, cudaMemcpyAsync(h, hh.data(), sizeof(T) * (size_t)ldh * nang, cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(c, cudaMemsetAsync(ritz, 0, sizeof(T) * (size_t)n * nang, c->stream));
-    launch_batched_sub(Q, qs, n, steps, ritz, n, h, ldh, nang, c->stream);
-    ++c->launches;
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // hh is host memory
+  // mmax reached: the angles still iterating report their last values
+  std::vector<int> rest;
+  for (int a = 0; a < na; ++a) {
+    lam[a] = tridiag_lmax_from(al[a], be[a], lam[a], 0.0, 0.0);
+    lam_out[slot_angle[a]] = lam[a];
+    rest.push_back(a);
   }
+  if ((rc = emit_ritz(rest, steps))) return rc;
   return BEM2D_OK;
 }
 
@@ -1430,24 +1568,37 @@ int bem2d_num_range(bem2d_ctx* c, int n, const void* A, int64_t lda, int nang,
   CUDA_TRY(c, cudaMemcpyAsync(dth, theta, sizeof(double) * nang, cudaMemcpyHostToDevice, c->stream));
   const int mmax = std::min(n, 160);
   if (precision == BEM2D_PREC_FP64)
-    return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, nullptr, lmax, nullptr);
-  // mixed: complex64 Lanczos (three-term recurrence, cold start: every
-  // angle's largest eigenvalue is found from its own Krylov space) to
-  // ~1e-6, then complex128 Lanczos (full reorthogonalisation) started from
-  // the complex64 Ritz vectors, all angles in one batch
+    return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, nullptr, lmax, nullptr,
+                                     true, 0.0, tol);
+  // mixed: complex64 Lanczos (full reorthogonalisation, cold start: every
+  // angle's largest eigenvalue is found from its own Krylov space) until
+  // each Ritz pair's residual is below 1e-7 |H| (a Ritz vector converged
+  // near single precision, whose Rayleigh quotient is already within
+  // ~1e-14 |H|^2 / gap), then complex128 Lanczos (full reorthogonalisation)
+  // started from those Ritz vectors, all angles in one batch, each until
+  // its error estimate min(r, r^2 / gap) is below tol times |H| (r the
+  // complex128 residual, gap the smaller of the complex64 estimate and the
+  // current tridiagonal's): with a complex64 residual near 1e-6, most angles
+  // are done after the first complex128 product
   float2* A32 = static_cast<float2*>(ws(c, "nr_A32", sizeof(float2) * (size_t)n * n, &rc));
   float2* R32 = static_cast<float2*>(ws(c, "nr_R32", sizeof(float2) * (size_t)n * nang, &rc));
   double2* S64 = static_cast<double2*>(ws(c, "nr_S64", sizeof(double2) * (size_t)n * nang, &rc));
   if (!A32 || !R32 || !S64) return rc;
   launch_to_c64(dA, la, A32, n, n, n, c->stream);
   ++c->launches;
-  std::vector<double> l32(nang);
+  std::vector<double> l32(nang), gap(nang);
   if ((rc = numrange_lanczos<float2>(c, n, A32, n, nang, dth, 1e-6, mmax, nullptr, l32.data(), R32,
-                                     false)))
+                                     true, 1e-7, 0.0, nullptr, gap.data())))
     return rc;
+  // the complex64 gap theta_1 - theta_2 over-estimates the true gap while
+  // theta_2 is still rising: a quarter of it, less the complex64 noise
+  double hs = 0.0;
+  for (int a = 0; a < nang; ++a) hs = std::max(hs, std::fabs(l32[a]));
+  for (int a = 0; a < nang; ++a) gap[a] = std::max(0.0, 0.25 * gap[a] - 1e-6 * hs);
   launch_widen(n, R32, n, S64, n, nang, c->stream);
   ++c->launches;
-  return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, S64, lmax, nullptr);
+  return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, S64, lmax, nullptr, true,
+                                   0.0, tol, gap.data());
 }
 
 int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,

@@ -140,28 +140,35 @@ void launch_mvh(const double2* A, long long lda, int n, const double2* x, double
 }
 
 // ---- matrix-matrix products: C (n x m) = op(A) (n x n) B (n x m) -------------
-// op = A or A^H; 64 x 64 output tiles, K in chunks of 16, 4 x 4 per thread.
-// T = double2 (complex128) or float2 (complex64).
-template <typename T, bool HERM>
+// op = A or A^H; 64 x BN output tiles (BN = 64, 16 or 4 by the width m),
+// K in chunks of 16; 256 threads as TX x TY, each RA x RB outputs.  The K
+// range may be split over gridDim.z: split z writes its partial product to
+// C + z * cz and zgemm_reduce_kernel adds the partials in a fixed order
+// (deterministic), so that narrow products (few Lanczos vectors) still
+// fill the GPU.  T = double2 (complex128) or float2 (complex64).
+template <typename T, bool HERM, int BN>
 __global__ void __launch_bounds__(256)
 zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict__ B,
-             long long ldb, int m, T* __restrict__ C, long long ldc) {
+             long long ldb, int m, T* __restrict__ C, long long ldc, int kchunk, long long cz) {
+  constexpr int TY = BN >= 16 ? 16 : BN, TX = 256 / TY, RA = 64 / TX, RB = BN / TY;
   __shared__ T As[16][64 + 1];
-  __shared__ T Bs[16][64 + 1];
+  __shared__ T Bs[16][BN + 1];
   const T zero = CTraits<T>::make(0, 0);
-  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * 64;
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  T acc[4][4];
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * BN;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int kb = blockIdx.z * kchunk, ke = min(n, kb + kchunk);
+  T* Cz = C + (size_t)blockIdx.z * cz;
+  T acc[RA][RB];
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < RA; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = zero;
-  for (int k0 = 0; k0 < n; k0 += 16) {
+    for (int b = 0; b < RB; ++b) acc[a][b] = zero;
+  for (int k0 = kb; k0 < ke; k0 += 16) {
     for (int v = threadIdx.x; v < 16 * 64; v += 256) {
       const int kk = v / 64, ii = v - kk * 64;
       const int i = i0 + ii, k = k0 + kk;
       T a = zero;
-      if (i < n && k < n) {
+      if (i < n && k < ke) {
         if (HERM) {
           const T t = A[(size_t)i * lda + k];  // (A^H)_{ik} = conj(A_{ki})
           a = CTraits<T>::make(t.x, -t.y);
@@ -171,54 +178,108 @@ zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict_
       }
       As[kk][ii] = a;
     }
-    for (int v = threadIdx.x; v < 16 * 64; v += 256) {
+    for (int v = threadIdx.x; v < 16 * BN; v += 256) {
       const int jj = v / 16, kk = v - jj * 16;
       const int j = j0 + jj, k = k0 + kk;
-      Bs[kk][jj] = (j < m && k < n) ? B[(size_t)j * ldb + k] : zero;
+      Bs[kk][jj] = (j < m && k < ke) ? B[(size_t)j * ldb + k] : zero;
     }
     __syncthreads();
 #pragma unroll 4
     for (int kk = 0; kk < 16; ++kk) {
-      T av[4], bv[4];
+      T av[RA], bv[RB];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) av[a] = As[kk][tx + 16 * a];
+      for (int a = 0; a < RA; ++a) av[a] = As[kk][tx + TX * a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][ty + 16 * b];
+      for (int b = 0; b < RB; ++b) bv[b] = Bs[kk][ty + TY * b];
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int a = 0; a < RA; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = cfma(av[a], bv[b], acc[a][b]);
+        for (int b = 0; b < RB; ++b) acc[a][b] = cfma(av[a], bv[b], acc[a][b]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    const int j = j0 + ty + 16 * b;
+  for (int b = 0; b < RB; ++b) {
+    const int j = j0 + ty + TY * b;
     if (j >= m) continue;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int i = i0 + tx + 16 * a;
-      if (i < n) C[(size_t)j * ldc + i] = acc[a][b];
+    for (int a = 0; a < RA; ++a) {
+      const int i = i0 + tx + TX * a;
+      if (i < n) Cz[(size_t)j * ldc + i] = acc[a][b];
     }
   }
 }
 
+// C (ldc) = sum over z < nz of P + z cz (leading dimension n), z in order
+template <typename T>
+__global__ void zgemm_reduce_kernel(const T* __restrict__ P, long long cz, int nz, int n, int m,
+                                    T* __restrict__ C, long long ldc) {
+  const int j = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || j >= m) return;
+  T s = P[(size_t)j * n + i];
+  for (int z = 1; z < nz; ++z) {
+    const T v = P[(size_t)z * cz + (size_t)j * n + i];
+    s.x += v.x;
+    s.y += v.y;
+  }
+  C[(size_t)j * ldc + i] = s;
+}
+
+// K splits for an n x m product: enough CTAs for two per SM (152 SMs), each
+// split at least 256 deep
+static int zgemm_splits(int n, int m, int bn) {
+  const long long tiles = (long long)((n + 63) / 64) * ((m + bn - 1) / bn);
+  const long long want = (2 * 152 + tiles - 1) / tiles;
+  return (int)std::max<long long>(1, std::min<long long>(want, n / 256));
+}
+
+static int zgemm_bn(int m) { return m <= 4 ? 4 : (m <= 16 ? 16 : 64); }
+
+size_t zgemm_work_bytes(int n, int m, size_t elem) {
+  const int z = zgemm_splits(n, m, zgemm_bn(m));
+  return z > 1 ? elem * (size_t)z * n * m : 0;
+}
+
+template <typename T, int BN>
+static void zgemm_bn_t(bool herm, const T* A, long long lda, int n, const T* B, long long ldb,
+                       int m, T* C, long long ldc, T* P, int z, cudaStream_t s) {
+  const int kchunk = ((n + z - 1) / z + 15) / 16 * 16;
+  dim3 g((n + 63) / 64, (m + BN - 1) / BN, z);
+  T* out = z > 1 ? P : C;
+  const long long lo = z > 1 ? n : ldc, cz = z > 1 ? (long long)n * m : 0;
+  if (herm)
+    zgemm_kernel<T, true, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz);
+  else
+    zgemm_kernel<T, false, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz);
+  if (z > 1)
+    zgemm_reduce_kernel<T><<<dim3((n + 255) / 256, m), 256, 0, s>>>(P, cz, z, n, m, C, ldc);
+}
+
 template <typename T>
 static void zgemm_t(bool herm, const T* A, long long lda, int n, const T* B, long long ldb, int m,
-                    T* C, long long ldc, cudaStream_t s) {
-  dim3 g((n + 63) / 64, (m + 63) / 64);
-  if (herm)
-    zgemm_kernel<T, true><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
+                    T* C, long long ldc, void* work, size_t work_bytes, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return;
+  const int bn = zgemm_bn(m);
+  int z = zgemm_splits(n, m, bn);
+  if (z > 1 && work_bytes < sizeof(T) * (size_t)z * n * m) z = 1;  // no room: one pass
+  T* P = static_cast<T*>(work);
+  if (bn == 4)
+    zgemm_bn_t<T, 4>(herm, A, lda, n, B, ldb, m, C, ldc, P, z, s);
+  else if (bn == 16)
+    zgemm_bn_t<T, 16>(herm, A, lda, n, B, ldb, m, C, ldc, P, z, s);
   else
-    zgemm_kernel<T, false><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, C, ldc);
+    zgemm_bn_t<T, 64>(herm, A, lda, n, B, ldb, m, C, ldc, P, z, s);
 }
 void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
-                  long long ldb, int m, double2* C, long long ldc, cudaStream_t s) {
-  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, s);
+                  long long ldb, int m, double2* C, long long ldc, void* work,
+                  size_t work_bytes, cudaStream_t s) {
+  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, work, work_bytes, s);
 }
 void launch_zgemm(bool herm, const float2* A, long long lda, int n, const float2* B,
-                  long long ldb, int m, float2* C, long long ldc, cudaStream_t s) {
-  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, s);
+                  long long ldb, int m, float2* C, long long ldc, void* work,
+                  size_t work_bytes, cudaStream_t s) {
+  zgemm_t(herm, A, lda, n, B, ldb, m, C, ldc, work, work_bytes, s);
 }
 
 // ---- batched vector kernels (columns of n x m blocks) ----------------------
@@ -325,6 +386,30 @@ __global__ void widen_kernel(int n, const float2* __restrict__ src, long long ss
   dst[(size_t)c * dstride + r] = make_double2(v.x, v.y);
 }
 
+template <typename T>
+__global__ void gather_slots_kernel(const T* __restrict__ src, long long sstride,
+                                    T* __restrict__ dst, long long dstride, long long len,
+                                    const int* __restrict__ map) {
+  const int i = blockIdx.y;
+  const T* a = src + (size_t)map[i] * sstride;
+  T* b = dst + (size_t)i * dstride;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < len;
+       r += (long long)gridDim.x * blockDim.x)
+    b[r] = a[r];
+}
+
+template <typename T>
+__global__ void scatter_slots_kernel(const T* __restrict__ src, long long sstride,
+                                     T* __restrict__ dst, long long dstride, long long len,
+                                     const int* __restrict__ map) {
+  const int i = blockIdx.y;
+  const T* a = src + (size_t)i * sstride;
+  T* b = dst + (size_t)map[i] * dstride;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < len;
+       r += (long long)gridDim.x * blockDim.x)
+    b[r] = a[r];
+}
+
 #define BEM2D_BATCHED_LAUNCHERS(T)                                                            \
   void launch_batched_dots(const T* Q, long long qstride, int n, int j, const T* W,           \
                            long long wstride, T* h, int ldh, int nb, cudaStream_t s) {        \
@@ -351,6 +436,20 @@ __global__ void widen_kernel(int n, const float2* __restrict__ src, long long ss
                            cudaStream_t s) {                                                  \
     herm_combine_kernel<T><<<dim3((n + 127) / 128, nb), 128, 0, s>>>(n, Y1, Y2, stride, theta, \
                                                                     W, wstride);              \
+  }                                                                                           \
+  void launch_gather_slots(const T* src, long long sstride, T* dst, long long dstride,        \
+                           long long len, const int* map, int nmap, cudaStream_t s) {         \
+    if (nmap <= 0 || len <= 0) return;                                                        \
+    const long long bx = std::min<long long>((len + 255) / 256, 64);                         \
+    gather_slots_kernel<T><<<dim3((unsigned)bx, nmap), 256, 0, s>>>(src, sstride, dst,       \
+                                                                   dstride, len, map);       \
+  }                                                                                           \
+  void launch_scatter_slots(const T* src, long long sstride, T* dst, long long dstride,       \
+                            long long len, const int* map, int nmap, cudaStream_t s) {        \
+    if (nmap <= 0 || len <= 0) return;                                                        \
+    const long long bx = std::min<long long>((len + 255) / 256, 64);                         \
+    scatter_slots_kernel<T><<<dim3((unsigned)bx, nmap), 256, 0, s>>>(src, sstride, dst,      \
+                                                                    dstride, len, map);      \
   }
 BEM2D_BATCHED_LAUNCHERS(double2)
 BEM2D_BATCHED_LAUNCHERS(float2)
@@ -428,6 +527,50 @@ bool tridiag_eigenvalues(std::vector<double> d, std::vector<double> e, std::vect
 // number of eigenvalues below x): O(n) per step, about 60 steps to full
 // precision, against O(n^2) for a complete QL sweep.
 double tridiag_lmax(const std::vector<double>& d, const std::vector<double>& e) {
+  return tridiag_kth_largest(d, e, 1, 2.2e-16);
+}
+
+double tridiag_lmax_from(const std::vector<double>& d, const std::vector<double>& e, double lo,
+                         double step, double atol) {
+  const int n = (int)d.size();
+  double scale = 0.0;  // Gershgorin bound of |spectrum|
+  for (int i = 0; i < n; ++i)
+    scale = std::max(scale, std::fabs(d[i]) + (i > 0 ? std::fabs(e[i - 1]) : 0.0) +
+                                (i + 1 < n ? std::fabs(e[i]) : 0.0));
+  if (!(scale > 0)) return 0.0;
+  auto all_below = [&](double x) {  // every eigenvalue < x
+    double q = 1.0;
+    for (int i = 0; i < n; ++i) {
+      q = d[i] - x - (i > 0 ? e[i - 1] * e[i - 1] / q : 0.0);
+      if (q == 0.0) q = -1e-300 * scale;
+      if (q >= 0) return false;
+    }
+    return true;
+  };
+  if (!(lo >= -scale)) lo = -scale;
+  const double tol = std::max(atol, 2.2e-16 * scale);
+  // grow the step until lo + step is an upper bound; lo stays a lower bound
+  double dx = std::max(step, 4.0 * tol);
+  double hi = lo + dx;
+  for (int it = 0; it < 200 && !all_below(hi); ++it) {
+    lo = hi;
+    dx *= 4.0;
+    hi = std::min(lo + dx, scale * (1.0 + 1e-15) + 1e-300);
+    if (hi <= lo) break;
+  }
+  for (int it = 0; it < 200 && hi - lo > tol; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (all_below(mid))
+      hi = mid;
+    else
+      lo = mid;
+  }
+  return lo;  // a lower bound again, for the next call
+}
+
+double tridiag_kth_largest(const std::vector<double>& d, const std::vector<double>& e, int k,
+                           double rel) {
   const int n = (int)d.size();
   double lo = INFINITY, hi = -INFINITY;
   for (int i = 0; i < n; ++i) {  // Gershgorin bounds
@@ -446,11 +589,11 @@ double tridiag_lmax(const std::vector<double>& d, const std::vector<double>& e) 
     }
     return cnt;
   };
-  for (int it = 0; it < 200 && hi - lo > 2.2e-16 * std::max(scale, 1e-300); ++it) {
+  for (int it = 0; it < 200 && hi - lo > rel * std::max(scale, 1e-300); ++it) {
     const double mid = 0.5 * (lo + hi);
     if (mid <= lo || mid >= hi) break;
-    if (below(mid) == n)
-      hi = mid;  // every eigenvalue below mid
+    if (below(mid) > n - k)
+      hi = mid;  // fewer than k eigenvalues at or above mid
     else
       lo = mid;
   }

@@ -44,6 +44,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 QUAD = (3, 5, 0.15)
+# numerical range (config 5b): both arms stop each angle at the same error
+# estimate, 1e-11 of |H| (ten times below the 1e-10 accuracy bar)
+NR_TOL = 1e-11
 SWEEP_WORKERS = 16
 
 
@@ -225,7 +228,7 @@ def run_aux(args):
                                           ctx.change_basis(A, M, bstart, out=B))),
                 ("study", lambda: ph.__setitem__(
                     "out", ctx.norm_cond(B) if args.workload == "square8192_normcond"
-                    else ctx.num_range_lmax(B, thetas, precision="mixed")))):
+                    else ctx.num_range_lmax(B, thetas, tol=NR_TOL, precision="mixed")))):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
@@ -266,7 +269,7 @@ def run_aux(args):
         e1 = torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record()
-        lm64 = ctx.num_range_lmax(B, thetas, precision="fp64")
+        lm64 = ctx.num_range_lmax(B, thetas, tol=NR_TOL, precision="fp64")
         e1.record()
         e1.synchronize()
         t64 = e0.elapsed_time(e1)
@@ -275,14 +278,17 @@ def run_aux(args):
                              "unit": "1/s"}
         res["mixed_over_fp64_study"] = t64 / phases["study"]
         res["mixed_vs_fp64_max_rel_err"] = float(np.max(np.abs(lm - lm64)) / np.max(np.abs(lm64)))
-        errs = []
+        errs, errs64 = [], []
         for j in range(0, 360, 45):
             z = complex(np.cos(thetas[j]), np.sin(thetas[j]))
             H = 0.5 * (z * Bt + np.conj(z) * Bt.conj().T)
             ev = float(torch.linalg.eigvalsh(H)[-1])
             errs.append(abs(lm[j] - ev) / max(abs(ev), 1e-300))
+            errs64.append(abs(lm64[j] - ev) / max(abs(ev), 1e-300))
         res["result"] = {"lambda_max_min": float(np.min(lm)), "lambda_max_max": float(np.max(lm))}
+        res["config"]["tol"] = NR_TOL
         res["max_rel_err_vs_dense_eigvalsh"] = max(errs)
+        res["plain_fp64"]["max_rel_err_vs_dense_eigvalsh"] = max(errs64)
         res["checked_angles"] = 8
     print(json.dumps(res))
 
@@ -436,7 +442,7 @@ def run_ours(args):
                "note": "8N^3/3 real flops (zgetrf count) per factorisation, N=%d; peak shown "
                        "is the FP32 CUDA-core pipe, the trailing update runs on the tensor "
                        "cores" % nb},
-        "far": {"bound": "fp32", "kernel": "far_ff_kernel + deferred_fp64_kernel",
+        "far": {"bound": "fp32", "kernel": "far_ff_kernel + deferred_ff_kernel",
                 "achieved": far_flops / (ph_mixed["far"] * 1e-3) / 1e12,
                 "note": "100 flops per kernel evaluation (frozen convention), "
                         "25 (N^2-3N) evaluations per launch, N=%d" % nb},

@@ -215,12 +215,14 @@ int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double
  * nang angles th_j: the eigenvalue step of NumRange
  * (lib/bem2d_mathroutines.cpp:590-653, zheev per angle; the smallest
  * eigenvalue at th is -lmax at th + pi).  Lanczos with full
- * reorthogonalisation, all angles in one block of matrix products, until
- * lmax moves by less than tol (relative; tol <= 0 selects 1e-13).
- * BEM2D_PREC_FP64: complex128 throughout.  BEM2D_PREC_MIXED: complex64
- * Lanczos (three-term recurrence, cold start) to 1e-6, then complex128 Lanczos
- * (full reorthogonalisation) started from its Ritz
- * vectors (same tolerance). */
+ * reorthogonalisation, all angles in one block of matrix products; an angle
+ * leaves the block once its error estimate min(r, r^2 / gap) is below tol
+ * times the size of the Hermitian part seen so far (tol <= 0 selects
+ * 1e-13; r the Ritz pair's residual, which bounds the distance to an
+ * eigenvalue, gap the distance to the next Ritz value).  BEM2D_PREC_FP64:
+ * complex128 throughout.  BEM2D_PREC_MIXED: complex64 Lanczos (cold start)
+ * to a residual of 1e-7 |H|, then complex128 Lanczos started from its Ritz
+ * vectors, with the complex64 gap estimates (same tolerance). */
 int bem2d_num_range(bem2d_ctx* ctx, int n, const void* A, int64_t lda, int nang,
                     const double* theta, double tol, int precision, double* lmax);
 
