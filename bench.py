@@ -94,6 +94,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, ws, device):
+    """Element-wise maximum of per-rank step times over all ranks: the step
+    time of a replica run is its slowest rank's.  One rank: unchanged."""
+    vals = [float(v) for v in values]
+    if ws <= 1:
+        return vals
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 def clocks_start(path):
     try:
         f = open(path, "w")
@@ -457,12 +469,7 @@ def run_ours(args):
     t_mixed = sum(ms_mixed) / len(ms_mixed)
     t_e2e = sum(ms_e2e) / len(ms_e2e)
     t_fp64 = sum(ms_fp64) / len(ms_fp64)
-    per_rank = np.array([t_mixed, t_e2e, t_fp64])
-    if ws > 1:
-        t = torch.tensor(per_rank, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        per_rank = t.cpu().numpy()
-    t_mixed, t_e2e, t_fp64 = (float(v) for v in per_rank)
+    t_mixed, t_e2e, t_fp64 = max_over_ranks([t_mixed, t_e2e, t_fp64], ws, "cuda")
     if rank != 0:
         return
     entries = float(sum(n * n for n in ns))
@@ -470,7 +477,7 @@ def run_ours(args):
         "metric": "solves/s", "value": ws * P * 1e3 / t_mixed, "unit": "solves/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64 LU + f64 refinement; f64 near field, float-float far field",
+        "dtype": "c64 LU + f64 refinement; float-float Bessel functions, f64 geometry",
         "data": "synthetic",
         "config": {"workload": w["desc"], "problems_per_step": P,
                    "n_unknowns": ns[0] if P == 1 else [min(ns), max(ns)],
