@@ -139,6 +139,13 @@ class _GeomHold:
         self.n = len(a["unk_elem"])
 
 
+def _k(k, eta):
+    """Wavenumber (real or complex) as (re, im) and the coupling eta, whose
+    default is Re k (CombinedSingleConjDouble(k), lib/bem2d_kernel.cpp:89)."""
+    kc = complex(k)
+    return kc.real, kc.imag, (kc.real if eta is None else float(eta))
+
+
 def quad(q=(3, 5, 0.15)):
     return Quad_c(int(q[0]), int(q[1]), float(q[2]))
 
@@ -202,10 +209,10 @@ class Context:
         ld = n
         if hasattr(out, "stride"):  # torch: column-major view, or row-major storage of A^T
             ld = out.stride(1) if out.stride(0) == 1 else out.stride(0)
-        eta = float(k) if eta is None else float(eta)
+        kr, ki, eta = _k(k, eta)
         qq = quad(q)
         self._check(self.lib.bem2d_discrete_kernel(
-            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], kr, ki,
             eta, float(alpha), float(beta), _ptr(out), ld))
         return out
 
@@ -219,10 +226,10 @@ class Context:
             out = np.zeros((n, n), dtype=np.complex128, order="F")
         if out32 is None:
             out32 = np.zeros((n, n), dtype=np.complex64, order="F")
-        eta = float(k) if eta is None else float(eta)
+        kr, ki, eta = _k(k, eta)
         qq = quad(q)
         self._check(self.lib.bem2d_discrete_kernel_mixed(
-            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], float(k), 0.0,
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), KERNEL[kernel], kr, ki,
             eta, float(alpha), float(beta), _ptr(out), _ld(out, n), _ptr(out32),
             _ld(out32, n)))
         return out, out32
@@ -242,10 +249,10 @@ class Context:
         gh = _GeomHold(g)
         if out is None:
             out = np.zeros(gh.n, dtype=np.complex128)
-        eta = float(k) if eta is None else float(eta)
+        kr, ki, eta = _k(k, eta)
         qq = quad(q)
         self._check(self.lib.bem2d_dot_prod_basfuns(
-            self.h, ctypes.byref(gh.c), ctypes.byref(qq), FUN[fun], float(k), 0.0,
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), FUN[fun], kr, ki,
             float(direction[0]), float(direction[1]), eta, float(scale), _ptr(out)))
         return out
 
@@ -327,9 +334,10 @@ class Context:
         c = np.ascontiguousarray(coeffs, dtype=np.complex128)
         pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
         out = np.zeros(len(pts), dtype=np.complex128)
+        kr, ki, eta = _k(k, eta)
         qq = quad(q)
         self._check(self.lib.bem2d_eval_kernel(self.h, ctypes.byref(gh.c), ctypes.byref(qq),
-                                               KERNEL[kernel], float(k), 0.0, float(eta),
+                                               KERNEL[kernel], kr, ki, eta,
                                                _ptr(c), len(pts), _ptr(pts), _ptr(out)))
         return out
 
@@ -338,11 +346,11 @@ class Context:
         gh = _GeomHold(g)
         if out is None:
             out = np.zeros(gh.n, dtype=np.complex128)
-        eta = float(k) if eta is None else float(eta)
+        kr, ki, eta = _k(k, eta)
         qq = quad(q)
         info = SolveInfo_c()
         self._check(self.lib.bem2d_scattering_solve(
-            self.h, ctypes.byref(gh.c), ctypes.byref(qq), float(k), 0.0, eta,
+            self.h, ctypes.byref(gh.c), ctypes.byref(qq), kr, ki, eta,
             float(direction[0]), float(direction[1]), PREC[precision], float(tol), _ptr(out),
             ctypes.byref(info)))
         self.last_info = (info.info, info.iterations, info.residual)

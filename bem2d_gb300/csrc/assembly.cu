@@ -78,9 +78,10 @@ void launch_node_table(const DevGeom& g, const DevRules& r, NodeTable t,
 constexpr int kTile = 32;
 constexpr int kFarThreads = 256;
 
-template <int KERNEL, int NG>
+// CK: complex wavenumber k + i ki (complex-argument Hankel functions).
+template <int KERNEL, int NG, bool CK>
 __global__ void __launch_bounds__(kFarThreads)
-far_fp64_kernel(DevGeom g, NodeTable t, int ng_rt, double k, double eta,
+far_fp64_kernel(DevGeom g, NodeTable t, int ng_rt, double k, double ki, double eta,
                 double alpha, double2* __restrict__ out, long long ld) {
   const int ng = NG > 0 ? NG : ng_rt;
   extern __shared__ double smem[];
@@ -144,8 +145,12 @@ far_fp64_kernel(DevGeom g, NodeTable t, int ng_rt, double k, double eta,
       for (int q2 = 0; q2 < ng; ++q2) {  // fully unrolled when NG > 0
         const int o2 = q2 * kTile + cc;
         double re, im;
-        kernel_d<KERNEL>(k, kq, eq, x1, y1, cs[o2], cs[SZ + o2], n1x, n1y,
-                         cs[2 * SZ + o2], cs[3 * SZ + o2], &re, &im);
+        if (CK)
+          kernel_c<KERNEL>(k, ki, eq, x1, y1, cs[o2], cs[SZ + o2], n1x, n1y,
+                           cs[2 * SZ + o2], cs[3 * SZ + o2], &re, &im);
+        else
+          kernel_d<KERNEL>(k, kq, eq, x1, y1, cs[o2], cs[SZ + o2], n1x, n1y,
+                           cs[2 * SZ + o2], cs[3 * SZ + o2], &re, &im);
         const double ww = w1 * cs[4 * SZ + o2];
         acc_re = fma(re, ww, acc_re);
         acc_im = fma(im, ww, acc_im);
@@ -155,38 +160,54 @@ far_fp64_kernel(DevGeom g, NodeTable t, int ng_rt, double k, double eta,
   }
 }
 
-template <int KERNEL>
-static void launch_far_k(const DevGeom& g, const NodeTable& t, int ng, double k,
+template <int KERNEL, bool CK>
+static void launch_far_k(const DevGeom& g, const NodeTable& t, int ng, double k, double ki,
                          double eta, double alpha, double2* out, long long ld,
                          cudaStream_t s) {
   const size_t smem = sizeof(double) * 10 * ng * kTile + sizeof(long long) * 4 * kTile;
   dim3 grid((g.n_unk + kTile - 1) / kTile, (g.n_unk + kTile - 1) / kTile);
-  if (ng == 5) {
-    far_fp64_kernel<KERNEL, 5><<<grid, kFarThreads, smem, s>>>(g, t, ng, k, eta, alpha, out, ld);
-  } else {
-    auto fn = far_fp64_kernel<KERNEL, 0>;
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    fn<<<grid, kFarThreads, smem, s>>>(g, t, ng, k, eta, alpha, out, ld);
+  if constexpr (!CK) {  // the complex-k kernel keeps its node loop rolled
+    if (ng == 5) {
+      far_fp64_kernel<KERNEL, 5, false><<<grid, kFarThreads, smem, s>>>(g, t, ng, k, ki, eta,
+                                                                        alpha, out, ld);
+      return;
+    }
+  }
+  auto fn = far_fp64_kernel<KERNEL, 0, CK>;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  fn<<<grid, kFarThreads, smem, s>>>(g, t, ng, k, ki, eta, alpha, out, ld);
+}
+
+template <bool CK>
+static void launch_far_any(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                           double ki, double eta, double alpha, double2* out, long long ld,
+                           cudaStream_t s) {
+  switch (kernel) {
+    case BEM2D_KERNEL_SINGLE:
+      launch_far_k<BEM2D_KERNEL_SINGLE, CK>(g, t, ng, k, ki, eta, alpha, out, ld, s);
+      break;
+    case BEM2D_KERNEL_DOUBLE:
+      launch_far_k<BEM2D_KERNEL_DOUBLE, CK>(g, t, ng, k, ki, eta, alpha, out, ld, s);
+      break;
+    case BEM2D_KERNEL_CONJDOUBLE:
+      launch_far_k<BEM2D_KERNEL_CONJDOUBLE, CK>(g, t, ng, k, ki, eta, alpha, out, ld, s);
+      break;
+    default:
+      launch_far_k<BEM2D_KERNEL_COMBINED, CK>(g, t, ng, k, ki, eta, alpha, out, ld, s);
   }
 }
 
 void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
                      double k, double eta, double alpha, double2* out,
                      long long ld, cudaStream_t s) {
-  switch (kernel) {
-    case BEM2D_KERNEL_SINGLE:
-      launch_far_k<BEM2D_KERNEL_SINGLE>(g, t, ng, k, eta, alpha, out, ld, s);
-      break;
-    case BEM2D_KERNEL_DOUBLE:
-      launch_far_k<BEM2D_KERNEL_DOUBLE>(g, t, ng, k, eta, alpha, out, ld, s);
-      break;
-    case BEM2D_KERNEL_CONJDOUBLE:
-      launch_far_k<BEM2D_KERNEL_CONJDOUBLE>(g, t, ng, k, eta, alpha, out, ld, s);
-      break;
-    default:
-      launch_far_k<BEM2D_KERNEL_COMBINED>(g, t, ng, k, eta, alpha, out, ld, s);
-  }
+  launch_far_any<false>(g, t, ng, kernel, k, 0.0, eta, alpha, out, ld, s);
+}
+
+void launch_far_fp64_ck(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                        double ki, double eta, double alpha, double2* out, long long ld,
+                        cudaStream_t s) {
+  launch_far_any<true>(g, t, ng, kernel, k, ki, eta, alpha, out, ld, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -242,13 +263,22 @@ __device__ __forceinline__ void geo_fill(const DevGeom& g, int e, int u, const d
 // K(x, y) (re1, im1) and, if PAIR, K(y, x) (re2, im2) at a test point x
 // (normal n1) and a trial point y (normal n2).  FP64: kernel_d; MIXED: the
 // distance and the normal factors from the FP64 difference w = x - y, the
-// Bessel functions and the kernel in float-float.
-template <int KERNEL, bool MIXED, bool PAIR>
-__device__ __forceinline__ void near_point(double k, double kq, double eq, const KConstFF& kc,
+// Bessel functions and the kernel in float-float.  CK (FP64 only): complex
+// wavenumber k + i ki.
+template <int KERNEL, bool MIXED, bool PAIR, bool CK>
+__device__ __forceinline__ void near_point(double k, double ki, double kq, double eq,
+                                           const KConstFF& kc,
                                            const float* tab, double ax, double ay, double n1x,
                                            double n1y, double bx, double by, double n2x,
                                            double n2y, double* re1, double* im1, double* re2,
                                            double* im2) {
+  if (CK) {
+    if (PAIR)
+      kernel_c_pair<KERNEL>(k, ki, eq, ax, ay, bx, by, n1x, n1y, n2x, n2y, re1, im1, re2, im2);
+    else
+      kernel_c<KERNEL>(k, ki, eq, ax, ay, bx, by, n1x, n1y, n2x, n2y, re1, im1);
+    return;
+  }
   if (!MIXED) {
     if (PAIR)
       kernel_d_pair<KERNEL>(k, kq, eq, ax, ay, bx, by, n1x, n1y, n2x, n2y, re1, im1, re2, im2);
@@ -283,10 +313,10 @@ __device__ __forceinline__ void near_point(double k, double kq, double eq, const
   }
 }
 
-template <int KERNEL, bool MIXED>
+template <int KERNEL, bool MIXED, bool CK>
 __global__ void __launch_bounds__(256)
 near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npairs, double k,
-            double eta, double alpha, double beta, KConstFF kc, const float* gtab, int cap_s,
+            double ki, double eta, double alpha, double beta, KConstFF kc, const float* gtab, int cap_s,
             int cap_t, double2* __restrict__ out, long long ld, float2* __restrict__ out32,
             long long ld32) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -324,8 +354,9 @@ near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npair
         const ElemPt b = elem_eval(g.kind[e2], p2, t);
         double n2x, n2y, re, im;
         elem_normal(b, &n2x, &n2y);
-        near_point<KERNEL, MIXED, false>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
-                                         b.mx, b.my, n2x, n2y, &re, &im, &u1, &u2);
+        near_point<KERNEL, MIXED, false, CK>(k, ki, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a],
+                                             S.ny[a], b.mx, b.my, n2x, n2y, &re, &im, &u1,
+                                             &u2);
         const double f =
             S.f[a] * (elem_jac(b) * basis_eval(g.unk_kind[pr.j], g.unk_param[pr.j], t));
         acc_re = fma(re * f, x * w, acc_re);
@@ -350,8 +381,9 @@ near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npair
         const int kk = key[p];
         const int a = kk & 0xffff, b = cap_s + (kk >> 16);
         double r1, i1, r2, i2;
-        near_point<KERNEL, MIXED, true>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
-                                        S.x[b], S.y[b], S.nx[b], S.ny[b], &r1, &i1, &r2, &i2);
+        near_point<KERNEL, MIXED, true, CK>(k, ki, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a],
+                                            S.ny[a], S.x[b], S.y[b], S.nx[b], S.ny[b], &r1,
+                                            &i1, &r2, &i2);
         const double f = S.f[a] * S.f[b] * rule[3 * p + 2];
         acc_re = fma(r1, f, acc_re);
         acc_im = fma(i1, f, acc_im);
@@ -370,8 +402,9 @@ near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npair
         const int kk = key[p];
         const int a = kk & 0xffff, b = cap_s + (kk >> 16);
         double re, im;
-        near_point<KERNEL, MIXED, false>(k, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a], S.ny[a],
-                                         S.x[b], S.y[b], S.nx[b], S.ny[b], &re, &im, &u1, &u2);
+        near_point<KERNEL, MIXED, false, CK>(k, ki, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a],
+                                             S.ny[a], S.x[b], S.y[b], S.nx[b], S.ny[b], &re,
+                                             &im, &u1, &u2);
         const double f = S.f[a] * S.f[b] * rule[3 * p + 2];
         acc_re = fma(re, f, acc_re);
         acc_im = fma(im, f, acc_im);
@@ -400,9 +433,10 @@ size_t near_table_bytes(const DevRules& r) {
   return sizeof(double) * 5 * (size_t)(cs + ct);
 }
 
-template <int KERNEL, bool MIXED>
+template <int KERNEL, bool MIXED, bool CK>
 static void launch_near_k(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
-                          double k, double eta, double alpha, double beta, const float* tab,
+                          double k, double ki, double eta, double alpha, double beta,
+                          const float* tab,
                           double2* out, long long ld, float2* out32, long long ld32,
                           cudaStream_t s) {
   int cs, ct;
@@ -412,34 +446,34 @@ static void launch_near_k(const DevGeom& g, const DevRules& r, const NearPair* p
   const int wpb = (int)std::max<size_t>(1, std::min<size_t>(8, (96 * 1024 - 1024) / per_warp));
   const size_t smem = 1024 + per_warp * wpb;
   const int blocks = (npairs + wpb - 1) / wpb;
-  auto fn = near_kernel<KERNEL, MIXED>;
+  auto fn = near_kernel<KERNEL, MIXED, CK>;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  fn<<<blocks, 32 * wpb, smem, s>>>(g, r, pairs, npairs, k, eta, alpha, beta,
+  fn<<<blocks, 32 * wpb, smem, s>>>(g, r, pairs, npairs, k, ki, eta, alpha, beta,
                                      make_kconst(k, eta), tab, cs, ct, out, ld, out32, ld32);
 }
 
-template <bool MIXED>
+template <bool MIXED, bool CK>
 static void launch_near_m(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
-                          int kernel, double k, double eta, double alpha, double beta,
+                          int kernel, double k, double ki, double eta, double alpha, double beta,
                           const float* tab, double2* out, long long ld, float2* out32,
                           long long ld32, cudaStream_t s) {
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      launch_near_k<BEM2D_KERNEL_SINGLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
-                                                out, ld, out32, ld32, s);
+      launch_near_k<BEM2D_KERNEL_SINGLE, MIXED, CK>(g, r, pairs, npairs, k, ki, eta, alpha,
+                                                    beta, tab, out, ld, out32, ld32, s);
       break;
     case BEM2D_KERNEL_DOUBLE:
-      launch_near_k<BEM2D_KERNEL_DOUBLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
-                                                out, ld, out32, ld32, s);
+      launch_near_k<BEM2D_KERNEL_DOUBLE, MIXED, CK>(g, r, pairs, npairs, k, ki, eta, alpha,
+                                                    beta, tab, out, ld, out32, ld32, s);
       break;
     case BEM2D_KERNEL_CONJDOUBLE:
-      launch_near_k<BEM2D_KERNEL_CONJDOUBLE, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta,
-                                                    tab, out, ld, out32, ld32, s);
+      launch_near_k<BEM2D_KERNEL_CONJDOUBLE, MIXED, CK>(g, r, pairs, npairs, k, ki, eta, alpha,
+                                                        beta, tab, out, ld, out32, ld32, s);
       break;
     default:
-      launch_near_k<BEM2D_KERNEL_COMBINED, MIXED>(g, r, pairs, npairs, k, eta, alpha, beta, tab,
-                                                  out, ld, out32, ld32, s);
+      launch_near_k<BEM2D_KERNEL_COMBINED, MIXED, CK>(g, r, pairs, npairs, k, ki, eta, alpha,
+                                                      beta, tab, out, ld, out32, ld32, s);
   }
 }
 
@@ -450,12 +484,21 @@ int launch_near(const DevGeom& g, const DevRules& r, const NearPair* pairs, int 
   if (out32) {
     const float* tab = expi_table_dev();
     if (!tab) return BEM2D_ERR_NOMEM;
-    launch_near_m<true>(g, r, pairs, npairs, kernel, k, eta, alpha, beta, tab, out, ld, out32,
-                        ld32, s);
+    launch_near_m<true, false>(g, r, pairs, npairs, kernel, k, 0.0, eta, alpha, beta, tab, out,
+                               ld, out32, ld32, s);
   } else {
-    launch_near_m<false>(g, r, pairs, npairs, kernel, k, eta, alpha, beta, nullptr, out, ld,
-                         nullptr, 0, s);
+    launch_near_m<false, false>(g, r, pairs, npairs, kernel, k, 0.0, eta, alpha, beta, nullptr,
+                                out, ld, nullptr, 0, s);
   }
+  return BEM2D_OK;
+}
+
+int launch_near_ck(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                   int kernel, double k, double ki, double eta, double alpha, double beta,
+                   double2* out, long long ld, cudaStream_t s) {
+  if (npairs == 0) return BEM2D_OK;
+  launch_near_m<false, true>(g, r, pairs, npairs, kernel, k, ki, eta, alpha, beta, nullptr, out,
+                             ld, nullptr, 0, s);
   return BEM2D_OK;
 }
 
@@ -477,8 +520,9 @@ void launch_ident(const DevGeom& g, const DevRules& r, const NearPair* pairs,
 
 // ---------------------------------------------------------------------------
 // b_u = scale * sum_q f(x_q) |J| phi_u w_q, f one of the plane-wave
-// functionals (lib/bem2d_fun.h:14-93).
-__global__ void rhs_kernel(int n, NodeTable t, int ng, int fun, double k,
+// functionals (lib/bem2d_fun.h:14-93).  The wavenumber is k + i ki:
+// e^{i (k + i ki) d.x} = e^{-ki d.x} e^{i k d.x}.
+__global__ void rhs_kernel(int n, NodeTable t, int ng, int fun, double k, double ki,
                            double dx, double dy, double eta, double scale,
                            double2* __restrict__ out) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
@@ -486,9 +530,15 @@ __global__ void rhs_kernel(int n, NodeTable t, int ng, int fun, double k,
   double acc_re = 0.0, acc_im = 0.0;
   for (int q = 0; q < ng; ++q) {
     const size_t o = (size_t)u * ng + q;
-    const double ph = k * (dx * t.x[o] + dy * t.y[o]);
+    const double dd = dx * t.x[o] + dy * t.y[o];
+    const double ph = k * dd;
     double fs, fc;
     sincos(ph, &fs, &fc);
+    if (ki != 0.0) {
+      const double a = exp(-ki * dd);
+      fs *= a;
+      fc *= a;
+    }
     double vr, vi;
     if (fun == BEM2D_FUN_PLANEWAVE) {
       vr = fc;
@@ -497,6 +547,10 @@ __global__ void rhs_kernel(int n, NodeTable t, int ng, int fun, double k,
       const double nd = t.nx[o] * dx + t.ny[o] * dy;
       vr = -k * fs * nd;  // i k f (n.d)
       vi = k * fc * nd;
+      if (ki != 0.0) {  // the i * (i ki) f (n.d) part
+        vr -= ki * fc * nd;
+        vi -= ki * fs * nd;
+      }
       if (fun == BEM2D_FUN_COMBINEDPLANEWAVE) {  // - i eta f
         vr += eta * fs;
         vi -= eta * fc;
@@ -510,8 +564,8 @@ __global__ void rhs_kernel(int n, NodeTable t, int ng, int fun, double k,
 
 void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
                 double dx, double dy, double eta, double scale, double2* out,
-                cudaStream_t s) {
-  rhs_kernel<<<(g.n_unk + 127) / 128, 128, 0, s>>>(g.n_unk, t, ng, fun, k, dx, dy,
+                cudaStream_t s, double ki) {
+  rhs_kernel<<<(g.n_unk + 127) / 128, 128, 0, s>>>(g.n_unk, t, ng, fun, k, ki, dx, dy,
                                                    eta, scale, out);
 }
 
@@ -519,9 +573,10 @@ void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
 // Potential of a density at points (EvalKernel, lib/bem2d_quadrature.h:184-228):
 // out[p] = sum_u c_u sum_q K(x_p, y_uq) W_uq, both normals the source node's.
 // One thread per point; unknowns staged through shared memory in chunks.
-template <int KERNEL>
+// CK: complex wavenumber k + i ki.
+template <int KERNEL, bool CK>
 __global__ void __launch_bounds__(128)
-potential_kernel(int nunk, NodeTable t, int ng, double k, double eta,
+potential_kernel(int nunk, NodeTable t, int ng, double k, double ki, double eta,
                  const double2* __restrict__ coef, int npts, const double* __restrict__ pts,
                  double2* __restrict__ out) {
   __shared__ double sx[128], sy[128], snx[128], sny[128], sw[128];
@@ -546,12 +601,17 @@ potential_kernel(int nunk, NodeTable t, int ng, double k, double eta,
     const int cnt = min(128, total - base);
     if (p < npts) {
       for (int i = 0; i < cnt; ++i) {
-        double kr, ki;
-        kernel_d<KERNEL>(k, kq, eq, px, py, sx[i], sy[i], snx[i], sny[i], snx[i], sny[i], &kr,
-                         &ki);
+        double kvr, kvi;
+        if (CK)
+          kernel_c<KERNEL>(k, ki, eq, px, py, sx[i], sy[i], snx[i], sny[i], snx[i], sny[i],
+                           &kvr, &kvi);
+        else
+          kernel_d<KERNEL>(k, kq, eq, px, py, sx[i], sy[i], snx[i], sny[i], snx[i], sny[i],
+                           &kvr, &kvi);
         // coefficient * kernel * weight
         const double2 c = sc[i];
-        const double vr = (c.x * kr - c.y * ki) * sw[i], vi = (c.x * ki + c.y * kr) * sw[i];
+        const double vr = (c.x * kvr - c.y * kvi) * sw[i],
+                     vi = (c.x * kvi + c.y * kvr) * sw[i];
         ar += vr;
         ai += vi;
       }
@@ -560,23 +620,37 @@ potential_kernel(int nunk, NodeTable t, int ng, double k, double eta,
   if (p < npts) out[p] = make_double2(ar, ai);
 }
 
-void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
-                      double eta, const double2* coef, int npts, const double* pts,
-                      double2* out, cudaStream_t s) {
+template <bool CK>
+static void launch_potential_k(const DevGeom& g, const NodeTable& t, int ng, int kernel,
+                               double k, double ki, double eta, const double2* coef, int npts,
+                               const double* pts, double2* out, cudaStream_t s) {
   const int blocks = (npts + 127) / 128;
   switch (kernel) {
     case BEM2D_KERNEL_SINGLE:
-      potential_kernel<BEM2D_KERNEL_SINGLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      potential_kernel<BEM2D_KERNEL_SINGLE, CK>
+          <<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, ki, eta, coef, npts, pts, out);
       break;
     case BEM2D_KERNEL_DOUBLE:
-      potential_kernel<BEM2D_KERNEL_DOUBLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      potential_kernel<BEM2D_KERNEL_DOUBLE, CK>
+          <<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, ki, eta, coef, npts, pts, out);
       break;
     case BEM2D_KERNEL_CONJDOUBLE:
-      potential_kernel<BEM2D_KERNEL_CONJDOUBLE><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      potential_kernel<BEM2D_KERNEL_CONJDOUBLE, CK>
+          <<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, ki, eta, coef, npts, pts, out);
       break;
     default:
-      potential_kernel<BEM2D_KERNEL_COMBINED><<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, eta, coef, npts, pts, out);
+      potential_kernel<BEM2D_KERNEL_COMBINED, CK>
+          <<<blocks, 128, 0, s>>>(g.n_unk, t, ng, k, ki, eta, coef, npts, pts, out);
   }
+}
+
+void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                      double eta, const double2* coef, int npts, const double* pts,
+                      double2* out, cudaStream_t s, double ki) {
+  if (ki != 0.0)
+    launch_potential_k<true>(g, t, ng, kernel, k, ki, eta, coef, npts, pts, out, s);
+  else
+    launch_potential_k<false>(g, t, ng, kernel, k, 0.0, eta, coef, npts, pts, out, s);
 }
 
 }  // namespace bem2d_gpu

@@ -476,23 +476,36 @@ static int stage(bem2d_ctx* c, const bem2d_geometry* g, const bem2d_quad* q, boo
   return BEM2D_OK;
 }
 
+// Complex wavenumbers k_re + i k_im (the reference's AMOS branch) are
+// accepted with Re k > 0 and arg k >= -pi/3, the domain of the
+// complex-argument Hankel evaluator (hankel_c.cuh).
 static int check_k(bem2d_ctx* c, double k_re, double k_im) {
-  if (k_im != 0.0)
-    return fail(c, BEM2D_ERR_UNSUPPORTED, "complex wavenumbers (k.im=%g) are not supported", k_im);
-  if (!std::isfinite(k_re)) return fail(c, BEM2D_ERR_ARG, "wavenumber is not finite");
+  if (!std::isfinite(k_re) || !std::isfinite(k_im))
+    return fail(c, BEM2D_ERR_ARG, "wavenumber is not finite");
+  if (k_im != 0.0 && !(k_re > 0.0 && k_im >= -std::sqrt(3.0) * k_re))
+    return fail(c, BEM2D_ERR_UNSUPPORTED,
+                "complex wavenumber %g%+gi is outside Re k > 0, arg k >= -pi/3", k_re, k_im);
   return BEM2D_OK;
 }
 
-// Assemble beta*M + alpha*K into a device matrix (ld).
+// Assemble beta*M + alpha*K into a device matrix (ld); ki != 0: complex
+// wavenumber k + i ki.
 static int assemble_dev(bem2d_ctx* c, const Staged& st, int kernel, double k, double eta,
-                        double alpha, double beta, double2* A, long long ld) {
+                        double alpha, double beta, double2* A, long long ld, double ki = 0.0) {
   int t = tic(c, BEM2D_PHASE_FAR);
-  launch_far_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, A, ld, c->stream);
+  if (ki != 0.0)
+    launch_far_fp64_ck(st.g, st.t, st.r.ng, kernel, k, ki, eta, alpha, A, ld, c->stream);
+  else
+    launch_far_fp64(st.g, st.t, st.r.ng, kernel, k, eta, alpha, A, ld, c->stream);
   toc(c, t);
   ++c->launches;
   CHECK_LAUNCH(c);
   t = tic(c, BEM2D_PHASE_NEAR);
-  launch_near(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld, c->stream);
+  if (ki != 0.0)
+    launch_near_ck(st.g, st.r, st.pairs, st.npairs, kernel, k, ki, eta, alpha, beta, A, ld,
+                   c->stream);
+  else
+    launch_near(st.g, st.r, st.pairs, st.npairs, kernel, k, eta, alpha, beta, A, ld, c->stream);
   toc(c, t);
   if (st.npairs) ++c->launches;
   CHECK_LAUNCH(c);
@@ -655,7 +668,7 @@ int bem2d_discrete_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_
   Staged st;
   if ((rc = stage(c, geom, quad, true, true, &st))) return rc;
   return with_matrix_out(c, out, ld, geom->n_unk, [&](double2* A, long long lda) {
-    return assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, lda);
+    return assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, lda, k_im);
   });
 }
 
@@ -683,7 +696,16 @@ int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
                   : static_cast<float2*>(ws(c, "out32", sizeof(float2) * (size_t)n * n, &rc));
   if (!B) return rc;
   const long long la = d64 ? ld : n, lb = d32 ? ld32 : n;
-  if ((rc = assemble_mixed_dev(c, st, kernel, k_re, eta, alpha, beta, A, la, B, lb))) return rc;
+  if (k_im != 0.0) {
+    // complex wavenumber: FP64 assembly (complex-argument Hankel functions),
+    // then its complex64 rounding
+    if ((rc = assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, la, k_im))) return rc;
+    launch_to_c64(A, la, B, lb, n, n, c->stream);
+    ++c->launches;
+    CHECK_LAUNCH(c);
+  } else if ((rc = assemble_mixed_dev(c, st, kernel, k_re, eta, alpha, beta, A, la, B, lb))) {
+    return rc;
+  }
   if (!d64)
     CUDA_TRY(c, cudaMemcpy2DAsync(out, sizeof(double2) * ld, A, sizeof(double2) * n,
                                   sizeof(double2) * n, n, cudaMemcpyDeviceToHost, c->stream));
@@ -729,7 +751,7 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   double2* b = dev ? static_cast<double2*>(out)
                    : static_cast<double2*>(ws(c, "rhs_out", sizeof(double2) * n, &rc));
   if (!b) return rc;
-  launch_rhs(st.g, st.t, st.r.ng, fun, k_re, dir_x, dir_y, eta, scale, b, c->stream);
+  launch_rhs(st.g, st.t, st.r.ng, fun, k_re, dir_x, dir_y, eta, scale, b, c->stream, k_im);
   ++c->launches;
   CHECK_LAUNCH(c);
   if (!dev)
@@ -979,16 +1001,18 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   double2* b = static_cast<double2*>(ws(c, "sys_b", sizeof(double2) * n, &rc));
   if (!b) return rc;
   const bool mixed = precision == BEM2D_PREC_MIXED;
-  if (mixed) {
+  // complex wavenumbers: FP64 assembly; the mixed solver converts A itself
+  const bool mixed_asm = mixed && k_im == 0.0;
+  if (mixed_asm) {
     float2* A32 = static_cast<float2*>(ws(c, "lu32", sizeof(float2) * (size_t)n * n, &rc));
     if (!A32) return rc;
     if ((rc = assemble_mixed_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n, A32, n)))
       return rc;
-  } else if ((rc = assemble_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n))) {
+  } else if ((rc = assemble_dev(c, st, BEM2D_KERNEL_COMBINED, k_re, eta, 2.0, 1.0, A, n, k_im))) {
     return rc;
   }
   launch_rhs(st.g, st.t, st.r.ng, BEM2D_FUN_COMBINEDPLANEWAVE, k_re, dir_x, dir_y, eta, 2.0, b,
-             c->stream);
+             c->stream, k_im);
   ++c->launches;
   CHECK_LAUNCH(c);
   const bool xdev = is_device_ptr(x);
@@ -1000,7 +1024,7 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   // assembly grids; the next call's assembly waits for this phase.
   PhaseStream ps(c);
   if ((rc = ps.begin())) return rc;
-  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info, mixed))) return rc;
+  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info, mixed_asm))) return rc;
   if (!xdev) {
     CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1624,7 +1648,7 @@ int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad
   const bool odev = is_device_ptr(out);
   double2* dO = dev_out(c, out, (size_t)npts, "ek_o", &rc);
   if (!dO) return rc;
-  launch_potential(st.g, st.t, st.r.ng, kernel, k_re, eta, dc, npts, dp, dO, c->stream);
+  launch_potential(st.g, st.t, st.r.ng, kernel, k_re, eta, dc, npts, dp, dO, c->stream, k_im);
   ++c->launches;
   CHECK_LAUNCH(c);
   if (!odev)

@@ -10,7 +10,7 @@
 #include <vector>
 
 #include "../../include/bem2d_gpu.h"
-#include "hankel.cuh"
+#include "hankel_c.cuh"
 
 namespace bem2d_gpu {
 
@@ -218,6 +218,69 @@ __device__ __forceinline__ void kernel_d_pair(double kk, double kq, double eq, d
   }
 }
 
+// ---- kernels with a complex wavenumber k = kr + i ki ----------------------
+// The reference's complex-k branches (lib/bem2d_kernel.cpp:15-112, AMOS
+// zbesh through BesselH0/H1(complex)); eta stays real, as there.
+//   S = (i/4) H0(k d),  D' = -(i k/4) H1(k d) (n1.(x-y))/d,
+//   D = -(i k/4) H1(k d) (n2.(y-x))/d,  combined = D' - i eta S.
+// eq = eta/4.
+template <int KERNEL>
+__device__ __forceinline__ void kernel_c(double kr, double ki, double eq, double xx, double xy,
+                                         double yx, double yy, double n1x, double n1y,
+                                         double n2x, double n2y, double* re, double* im) {
+  const double wx = xx - yx, wy = xy - yy;
+  const double d = sqrt(wx * wx + wy * wy);
+  cd h0, h1;
+  hankel01_c(cd{kr * d, ki * d}, &h0, &h1);
+  if (KERNEL == BEM2D_KERNEL_SINGLE) {
+    *re = -0.25 * h0.im;
+    *im = 0.25 * h0.re;
+  } else {
+    const double dot = (KERNEL == BEM2D_KERNEL_DOUBLE) ? -(n2x * wx + n2y * wy)
+                                                       : (n1x * wx + n1y * wy);
+    const double c = 0.25 * dot / d;
+    const cd p = cd_mul(cd{kr, ki}, h1);  // k H1
+    *re = c * p.im;
+    *im = -c * p.re;
+    if (KERNEL == BEM2D_KERNEL_COMBINED) {
+      *re = fma(eq, h0.re, *re);
+      *im = fma(eq, h0.im, *im);
+    }
+  }
+}
+
+// Both orientations of a pair (see kernel_d_pair), complex wavenumber.
+template <int KERNEL>
+__device__ __forceinline__ void kernel_c_pair(double kr, double ki, double eq, double xx,
+                                              double xy, double yx, double yy, double n1x,
+                                              double n1y, double n2x, double n2y, double* re1,
+                                              double* im1, double* re2, double* im2) {
+  const double wx = xx - yx, wy = xy - yy;
+  const double d = sqrt(wx * wx + wy * wy);
+  cd h0, h1;
+  hankel01_c(cd{kr * d, ki * d}, &h0, &h1);
+  if (KERNEL == BEM2D_KERNEL_SINGLE) {
+    *re1 = *re2 = -0.25 * h0.im;
+    *im1 = *im2 = 0.25 * h0.re;
+  } else {
+    const double n1w = n1x * wx + n1y * wy, n2w = n2x * wx + n2y * wy;
+    const double dot1 = (KERNEL == BEM2D_KERNEL_DOUBLE) ? -n2w : n1w;
+    const double dot2 = (KERNEL == BEM2D_KERNEL_DOUBLE) ? n1w : -n2w;
+    const double c1 = 0.25 * dot1 / d, c2 = 0.25 * dot2 / d;
+    const cd p = cd_mul(cd{kr, ki}, h1);
+    *re1 = c1 * p.im;
+    *im1 = -c1 * p.re;
+    *re2 = c2 * p.im;
+    *im2 = -c2 * p.re;
+    if (KERNEL == BEM2D_KERNEL_COMBINED) {
+      *re1 = fma(eq, h0.re, *re1);
+      *im1 = fma(eq, h0.im, *im1);
+      *re2 = fma(eq, h0.re, *re2);
+      *im2 = fma(eq, h0.im, *im2);
+    }
+  }
+}
+
 // ---- near-pair rules -------------------------------------------------------
 // RULE_G3_PAIR: the pair (i, j), j the next element of i, integrated with
 // AdaptedGauss3 together with its reverse (j, i), whose rule AdaptedGauss2
@@ -308,6 +371,11 @@ int launch_deferred(const NodeTableFF& tf, int ng, int kernel, double k, double 
 void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
                      double k, double eta, double alpha, double2* out,
                      long long ld, cudaStream_t s);
+// FP64 far field with a complex wavenumber k + i ki (complex-argument Hankel
+// functions).
+void launch_far_fp64_ck(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
+                        double ki, double eta, double alpha, double2* out, long long ld,
+                        cudaStream_t s);
 // Near field (self and adjacent pairs).  out32 == nullptr: FP64 kernel
 // evaluation into out.  Otherwise the mixed-precision variant (float-float
 // Bessel functions) writes both out and out32.  Returns BEM2D_ERR_NOMEM if
@@ -315,17 +383,23 @@ void launch_far_fp64(const DevGeom& g, const NodeTable& t, int ng, int kernel,
 int launch_near(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
                 int kernel, double k, double eta, double alpha, double beta, double2* out,
                 long long ld, cudaStream_t s, float2* out32 = nullptr, long long ld32 = 0);
+// FP64 near field with a complex wavenumber k + i ki.
+int launch_near_ck(const DevGeom& g, const DevRules& r, const NearPair* pairs, int npairs,
+                   int kernel, double k, double ki, double eta, double alpha, double beta,
+                   double2* out, long long ld, cudaStream_t s);
 // Shared-memory bytes per warp of the near-field geometry tables for rules r.
 size_t near_table_bytes(const DevRules& r);
 void launch_ident(const DevGeom& g, const DevRules& r, const NearPair* pairs,
                   int npairs, double2* out, long long ld, cudaStream_t s);
+// ki: imaginary part of the wavenumber (0 for a real k).
 void launch_rhs(const DevGeom& g, const NodeTable& t, int ng, int fun, double k,
                 double dx, double dy, double eta, double scale, double2* out,
-                cudaStream_t s);
+                cudaStream_t s, double ki = 0.0);
 
+// ki: imaginary part of the wavenumber (0 for a real k).
 void launch_potential(const DevGeom& g, const NodeTable& t, int ng, int kernel, double k,
                       double eta, const double2* coef, int npts, const double* pts,
-                      double2* out, cudaStream_t s);
+                      double2* out, cudaStream_t s, double ki = 0.0);
 
 // ---- context accessors (capi.cu) ------------------------------------------
 int ctx_device(const bem2d_ctx* c);

@@ -1,7 +1,8 @@
 // bem2d C++ API (GB300 build): exception tags thrown by the library, named as
 // in the reference (lib/bem2d_exceptions.h).  UnsupportedError (new) marks
-// inputs this build does not evaluate (complex wavenumbers, user-defined
-// element or curve classes, complex-valued bases).
+// inputs this build does not evaluate (complex wavenumbers with arg k below
+// -pi/3, user-defined element or curve classes, complex-valued bases, full
+// spectra).
 #ifndef BEM2D_EXCEPTIONS_H
 #define BEM2D_EXCEPTIONS_H
 

@@ -20,6 +20,11 @@
  *    column `info`, 1-based: the reference throws LapackError); < 0 = one of
  *    the BEM2D_ERR_* codes.  bem2d_ctx_last_error() gives a message.
  *  - A context is not thread-safe; use one per host thread.
+ *  - Wavenumbers are k_re + i k_im.  A complex k (the reference's AMOS zbesh
+ *    branch, lib/bem2d_mathroutines.cpp:44-75) is evaluated in FP64 by the
+ *    complex-argument Hankel evaluator (csrc/hankel_c.cuh) and must satisfy
+ *    k_re > 0 and arg k >= -pi/3 (k_im >= -sqrt(3) k_re), else
+ *    BEM2D_ERR_UNSUPPORTED.  eta stays real, as in the reference.
  */
 #ifndef BEM2D_GPU_H
 #define BEM2D_GPU_H
@@ -38,7 +43,7 @@ extern "C" {
 #define BEM2D_ERR_NONFINITE (-4)   /* NaN/Inf in an assembled entry or a residual */
 #define BEM2D_ERR_NOCONV (-5)      /* iterative refinement / iteration did not converge */
 #define BEM2D_ERR_TIMEOUT (-6)     /* a bounded device-side wait gave up */
-#define BEM2D_ERR_UNSUPPORTED (-7) /* complex wavenumber, unknown element or basis kind */
+#define BEM2D_ERR_UNSUPPORTED (-7) /* k outside arg k >= -pi/3, unknown element or basis kind */
 
 /* ---- element kinds (lib/bem2d_element.h:72-116, lib/bem2d_curvetypes.h) -
  * param row (8 doubles) per element:
@@ -134,11 +139,12 @@ int bem2d_discrete_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom,
                           void* out, int64_t ld);
 
 /* Mixed-precision variant of bem2d_discrete_kernel: same matrix, with the
- * far-field bulk evaluated in compensated single-single (float-float)
- * arithmetic on the FP32 pipe (~1e-14 relative per kernel evaluation) and
- * the near-field, self and small-argument (k|x-y| <= 4) entries in FP64.
+ * Bessel functions of every entry evaluated in compensated single-single
+ * (float-float) arithmetic on the FP32 pipe (~1e-14 relative per kernel
+ * evaluation); the near-field geometry and quadrature sums stay FP64.
  * Writes complex128 (out, ld) and its complex64 rounding (out32, ld32):
- * the residual and LU inputs of the mixed solver.  Requires k > 0. */
+ * the residual and LU inputs of the mixed solver.  Requires k_re > 0.  A
+ * complex k assembles in FP64 (as bem2d_discrete_kernel) and rounds. */
 int bem2d_discrete_kernel_mixed(bem2d_ctx* ctx, const bem2d_geometry* geom,
                                 const bem2d_quad* quad, int kernel, double k_re,
                                 double k_im, double eta, double alpha, double beta,
@@ -239,7 +245,8 @@ int bem2d_eval_kernel(bem2d_ctx* ctx, const bem2d_geometry* geom, const bem2d_qu
  * b = 2 <CombinedPlaneWave(dir, k, eta), phi_i>, x = A^{-1} b.  A and b stay
  * in the context's device workspace; only x (n_unk complex128) is written.
  * BEM2D_PREC_MIXED assembles with bem2d_discrete_kernel_mixed's arithmetic
- * and solves as bem2d_solve_system's mixed mode. */
+ * and solves as bem2d_solve_system's mixed mode (a complex k: FP64 assembly,
+ * then the mixed solve). */
 int bem2d_scattering_solve(bem2d_ctx* ctx, const bem2d_geometry* geom,
                            const bem2d_quad* quad, double k_re, double k_im,
                            double eta, double dir_x, double dir_y,

@@ -21,6 +21,8 @@
 //   op singvals KRE KIM ETA OUTFILE          (SingularValues of ChangeBasis(A,Id))
 //   op timing KRE KIM DX DY ETA OUTFILE      (wall-clock seconds: assemble, solve)
 //   op evalsol KRE KIM DX DY ETA OUTFILE X0 Y0 X1 Y1 ...  (EvalSol at the points)
+//   op hankel OUTFILE ZR0 ZI0 ZR1 ZI1 ...    (BesselH0, BesselH1 of complex z:
+//                                             H0(z0) H1(z0) H0(z1) ... complex128)
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -143,6 +145,17 @@ int main(int argc, char** argv) {
       else if (kname == "conjdouble") m = DiscreteKernel(g, c.quad, ConjDoubleLayer(k));
       else m = DiscreteKernel(g, c.quad, CombinedSingleConjDouble(k, eta));
       WriteComplex(out, *m);
+    } else if (what == "hankel") {
+      std::string out;
+      ss >> out;
+      double zr, zi;
+      Matrix m(1);
+      m.data->clear();
+      while (ss >> zr >> zi) {
+        m.data->push_back(BesselH0(complex(zr, zi)));
+        m.data->push_back(BesselH1(complex(zr, zi)));
+      }
+      WriteComplex(out, m);
     } else if (what == "ident") {
       std::string out;
       ss >> out;

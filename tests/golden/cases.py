@@ -26,6 +26,13 @@ def _dir(theta):
     return (math.cos(theta), math.sin(theta))
 
 
+# trapping domain of the reference's resonance scan (resonances/trapresonance.cpp)
+_TA, _TC = 0.31, 1.0
+_TL = _TC - _TA
+TRAP = [(0.0, 0.0), (-_TC, 0.0), (-_TC, -_TL), (_TL, -_TL), (_TL, 2 * _TC - _TL),
+        (-_TC, 2 * _TC - _TL), (-_TC, 2 * _TA), (0.0, 2 * _TA)]
+
+
 def _two_squares():
     a = G.polygon_uniform([(0, 0), (1, 0), (1, 1), (0, 1)], 6)
     b = G.polygon_uniform([(2, 0), (3, 0), (3, 1), (2, 1)], 6)
@@ -74,6 +81,19 @@ CASES = {
     "square_numrange": dict(geom=lambda: G.polygon_uniform(SQUARE, 16).add_poly_basis(0),
                             k=5.0, direction=(1.0, 0.0), eta=5.0, full=True,
                             numrange=18, singvals=True),
+    # complex wavenumbers k + i kim (the reference's AMOS branch); eta real
+    "trap_ck": dict(geom=lambda: G.polygon_graded_n(TRAP, [8] * 8, 3, 0.15).add_poly_basis(0),
+                    k=6.0, kim=-1.0, direction=(1.0, 0.0), eta=abs(complex(6.0, -1.0)),
+                    full=True, kernels=("single", "conjdouble")),
+    "disk_absorbing_ck": dict(geom=lambda: G.curve_equispaced(G.CIRCLE, 64).add_poly_basis(0),
+                              k=8.0, kim=0.5, direction=(1.0, 0.0), eta=8.0, full=True,
+                              kernels=("double",),
+                              evalsol=[(-1.5, 0.0), (2.0, 1.0), (0.0, -3.0)]),
+    "kite_ck": dict(geom=lambda: G.kite(96).add_poly_basis(0), k=12.0, kim=-3.0,
+                    direction=_dir(seeded_angle(2)), eta=12.0, full=True),
+    "square_poly2_ck": dict(geom=lambda: G.polygon_uniform(SQUARE, 8).add_poly_basis(2),
+                            k=3.0, kim=-0.5, direction=(1.0, 0.0), eta=3.0, full=True,
+                            kernels=("single", "conjdouble")),
 }
 
 QUAD = (3, 5, 0.15)

@@ -49,24 +49,26 @@ def run_case(name, spec):
     g = spec["geom"]()
     n = g.n_unknowns
     k, eta, d = spec["k"], spec["eta"], spec["direction"]
+    kim = spec.get("kim", 0.0)
     out = {}
     with tempfile.TemporaryDirectory() as tmp:
         lines = g.to_refspec(QUAD)
         if spec.get("scattering", True):
-            lines.append("op scattering %.17g 0 %.17g %.17g %.17g %s/sys"
-                         % (k, d[0], d[1], eta, tmp))
+            lines.append("op scattering %.17g %.17g %.17g %.17g %.17g %s/sys"
+                         % (k, kim, d[0], d[1], eta, tmp))
         lines.append("op ident %s/ident.bin" % tmp)
         for kn in spec.get("kernels", ()):
-            lines.append("op kernel %s %.17g 0 %.17g %s/k_%s.bin" % (kn, k, eta, tmp, kn))
+            lines.append("op kernel %s %.17g %.17g %.17g %s/k_%s.bin"
+                         % (kn, k, kim, eta, tmp, kn))
         if spec.get("numrange"):
-            lines.append("op numrange %.17g 0 %.17g %d %s/numrange.txt"
-                         % (k, eta, spec["numrange"], tmp))
+            lines.append("op numrange %.17g %.17g %.17g %d %s/numrange.txt"
+                         % (k, kim, eta, spec["numrange"], tmp))
         if spec.get("singvals"):
-            lines.append("op singvals %.17g 0 %.17g %s/singvals.bin" % (k, eta, tmp))
+            lines.append("op singvals %.17g %.17g %.17g %s/singvals.bin" % (k, kim, eta, tmp))
         if spec.get("evalsol"):
             pts = spec["evalsol"]
-            lines.append("op evalsol %.17g 0 %.17g %.17g %.17g %s/evalsol.bin %s"
-                         % (k, d[0], d[1], eta, tmp,
+            lines.append("op evalsol %.17g %.17g %.17g %.17g %.17g %s/evalsol.bin %s"
+                         % (k, kim, d[0], d[1], eta, tmp,
                             " ".join("%.17g %.17g" % p for p in pts)))
         with open(os.path.join(tmp, "case.txt"), "w") as f:
             f.write("\n".join(lines) + "\n")
@@ -93,16 +95,49 @@ def run_case(name, spec):
         if spec.get("singvals"):
             out["singvals"] = np.fromfile(tmp + "/singvals.bin", dtype=np.float64)
     meta = dict(name=name, n=n, k=k, eta=eta, direction=list(d), quad=list(QUAD))
+    if kim:
+        meta["kim"] = kim
     out["meta"] = np.array(json.dumps(meta))
     return out
+
+
+def hankel_fixture():
+    """BesselH0 / BesselH1 of a complex argument through the reference's own
+    routines (lib/bem2d_mathroutines.cpp:44-75) and the binary128 zbesh shim,
+    at seeded points of the complex evaluator's domain; checked here against
+    scipy.special.hankel1 (AMOS zbesh itself)."""
+    import scipy.special as sp
+    rng = np.random.default_rng(2024)
+    r = 10 ** rng.uniform(-5, np.log10(300), 600)
+    a = rng.uniform(-np.pi / 3, np.pi / 2, 600)
+    z = r * np.exp(1j * a)
+    z = z[z.imag < 60]
+    with tempfile.TemporaryDirectory() as tmp:
+        lines = ["quad 3 5 0.15", "seg 0 0 1 0 0 -1 -1", "basis poly 0",
+                 "op hankel %s/h.bin %s" % (tmp, " ".join("%.17g %.17g" % (x.real, x.imag)
+                                                          for x in z))]
+        with open(os.path.join(tmp, "case.txt"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        subprocess.run([REF_DUMP, os.path.join(tmp, "case.txt")], check=True,
+                       stdout=subprocess.DEVNULL)
+        h = np.fromfile(tmp + "/h.bin", dtype=np.complex128).reshape(-1, 2)
+    for nu in (0, 1):
+        e = np.abs(h[:, nu] - sp.hankel1(nu, z)) / np.abs(sp.hankel1(nu, z)) / (1 + np.abs(z) / 50)
+        assert e.max() < 4e-15, ("zbesh shim vs scipy AMOS", nu, e.max())
+    return dict(z=z, h0=h[:, 0].copy(), h1=h[:, 1].copy())
 
 
 def main():
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"],
                    check=True, stdout=subprocess.DEVNULL)
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or (list(CASES) + ["hankel_ck"])
     for name in names:
+        if name == "hankel_ck":
+            path = os.path.join(ROOT, "tests", "golden", "hankel_ck.npz")
+            np.savez_compressed(path, **hankel_fixture())
+            print("%-16s %7.1f KB" % (name, os.path.getsize(path) / 1024))
+            continue
         res = run_case(name, CASES[name])
         path = os.path.join(ROOT, "tests", "golden", name + ".npz")
         np.savez_compressed(path, **res)

@@ -38,7 +38,9 @@ def built():
     _build.build_oracle(with_reference=False)
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+# The restatement covers real wavenumbers; the complex-k cases are pinned
+# directly against the reference's outputs by the GPU tests.
+@pytest.mark.parametrize("name", sorted(n for n in CASES if not CASES[n].get("kim")))
 def test_port_matches_reference(name):
     z, meta = load(name)
     spec = CASES[name]
