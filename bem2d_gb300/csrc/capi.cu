@@ -1625,6 +1625,76 @@ int bem2d_num_range(bem2d_ctx* c, int n, const void* A, int64_t lda, int nang,
                                    0.0, tol, gap.data());
 }
 
+}  // extern "C"
+
+namespace bem2d_gpu {
+
+// Eigenvalues of the Hermitian M (N x N, device, overwritten): `count`
+// ascending from the smallest or descending from the largest, into out
+// (host or device, count doubles).
+static int spectra_run(bem2d_ctx* c, double2* M, int N, int count, int descending, double* out) {
+  int rc = 0;
+  void* work = ws(c, "sp_work", spectra_work_bytes(N), &rc);
+  if (!work) return rc;
+  const bool odev = is_device_ptr(out);
+  double* dout = odev ? out : static_cast<double*>(ws(c, "sp_out", sizeof(double) * count, &rc));
+  if (!dout) return rc;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      sms < 1)
+    sms = 1;
+  c->launches += launch_tridiag_eigs(M, N, count, descending, work, dout, sms, c->stream);
+  CHECK_LAUNCH(c);
+  if (!odev)
+    CUDA_TRY(c, cudaMemcpyAsync(out, dout, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                                c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEM2D_OK;
+}
+
+}  // namespace bem2d_gpu
+
+extern "C" {
+
+int bem2d_hermitian_eigenvalues(bem2d_ctx* c, int n, const void* A, int64_t lda, double* w) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !w || lda < n) return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (n > BEM2D_SPECTRA_MAX_N)
+    return fail(c, BEM2D_ERR_ARG, "order %d above BEM2D_SPECTRA_MAX_N = %d", n,
+                BEM2D_SPECTRA_MAX_N);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "sp_A", &la, &rc);
+  if (!dA) return rc;
+  double2* M = static_cast<double2*>(ws(c, "sp_M", sizeof(double2) * (size_t)n * n, &rc));
+  if (!M) return rc;
+  launch_herm_from_upper(dA, la, n, M, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  return spectra_run(c, M, n, n, 0, w);
+}
+
+int bem2d_singular_values(bem2d_ctx* c, int n, const void* A, int64_t lda, double* s) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !s || lda < n) return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (n > BEM2D_SPECTRA_MAX_N / 2)
+    return fail(c, BEM2D_ERR_ARG, "order %d above BEM2D_SPECTRA_MAX_N / 2 = %d", n,
+                BEM2D_SPECTRA_MAX_N / 2);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "sp_A", &la, &rc);
+  if (!dA) return rc;
+  const int N = 2 * n;
+  double2* M = static_cast<double2*>(ws(c, "sp_M", sizeof(double2) * (size_t)N * N, &rc));
+  if (!M) return rc;
+  launch_jordan_wielandt(dA, la, n, M, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  return spectra_run(c, M, N, n, 1, s);
+}
+
 int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
                       int kernel, double k_re, double k_im, double eta, const void* coeffs,
                       int npts, const double* points, void* out) {

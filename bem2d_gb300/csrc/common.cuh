@@ -477,4 +477,18 @@ void launch_sumsq(const double2* A, long long ld, int rows, int cols, double* pa
                   double* out, cudaStream_t s);
 size_t sumsq_part_bytes();
 
+// ---- launch interfaces (spectra.cu) ---------------------------------------
+// Work bytes of launch_tridiag_eigs for order N.
+size_t spectra_work_bytes(int N);
+// M (n x n, ld n) = the Hermitian matrix defined by the upper triangle of A.
+void launch_herm_from_upper(const double2* A, long long lda, int n, double2* M, cudaStream_t s);
+// M (2n x 2n, ld 2n) = [0 A; A^H 0].
+void launch_jordan_wielandt(const double2* A, long long lda, int n, double2* M, cudaStream_t s);
+// Householder reduction of the Hermitian M (N x N, ld N, overwritten) to
+// tridiagonal form and bisection for `count` of its eigenvalues: ascending
+// from the smallest, or (descending != 0) descending from the largest, into
+// out (device).  Returns the number of kernels launched.
+long long launch_tridiag_eigs(double2* M, int N, int count, int descending, void* work,
+                              double* out, int sms, cudaStream_t s);
+
 }  // namespace bem2d_gpu

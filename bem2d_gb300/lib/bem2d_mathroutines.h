@@ -45,13 +45,16 @@ Matrix operator*(const Matrix& lhs, const Matrix& rhs);
 
 // ||A||_2 and cond_2(A) from the extreme singular values (GPU Lanczos).
 void L2NormCond(const Matrix& stiff, double& norm, double& cond);
-// All singular values (not available in this build: UnsupportedError).
+// All singular values, descending (GPU Householder tridiagonalisation of
+// [0 A; A^H 0] and bisection).
 void SingularValues(const Matrix& stiff, pdvector& singvals);
 // x = m^{-1} rhs (GPU LU; precision from BEM2D_PRECISION=fp64|mixed).
 pMatrix SolveSystem(Matrix& m, Matrix& rhs);
-// All eigenvalues of a Hermitian / general matrix (not available in this
-// build: UnsupportedError).
+// All eigenvalues of the Hermitian matrix the upper triangle of k defines,
+// ascending (GPU Householder tridiagonalisation and bisection).
 void HermitianEigenvalues(const Matrix& k, pdvector& evalues);
+// All eigenvalues of a general matrix (not available in this build:
+// UnsupportedError).
 void Eigenvalues(const Matrix& k, pcvector& evalues);
 void Eigenvalues(const Matrix& k, pcvector& evalues, pMatrix& evectors);
 // U^{-H} k U^{-1} with m = U^H U (m block diagonal per element, as mass

@@ -98,11 +98,19 @@ void L2NormCond(const Matrix& stiff, double& norm, double& cond) {
                 "L2NormCond");
 }
 
-void SingularValues(const Matrix&, pdvector&) {
-  throw UnsupportedError("SingularValues (full SVD) is not available in this build; use L2NormCond");
+void SingularValues(const Matrix& stiff, pdvector& singvals) {
+  if (stiff.dim[0] != stiff.dim[1]) throw ArrayMismatch();
+  const int n = stiff.dim[0];
+  singvals = pdvector(new dvector(n));
+  detail::check(bem2d_singular_values(detail::ctx(), n, &(*stiff.data)[0], n, &(*singvals)[0]),
+                "SingularValues");
 }
-void HermitianEigenvalues(const Matrix&, pdvector&) {
-  throw UnsupportedError("HermitianEigenvalues (full spectrum) is not available in this build");
+void HermitianEigenvalues(const Matrix& k, pdvector& evalues) {
+  if (k.dim[0] != k.dim[1]) throw ArrayMismatch();
+  const int n = k.dim[0];
+  evalues = pdvector(new dvector(n));
+  detail::check(bem2d_hermitian_eigenvalues(detail::ctx(), n, &(*k.data)[0], n, &(*evalues)[0]),
+                "HermitianEigenvalues");
 }
 void Eigenvalues(const Matrix&, pcvector&) {
   throw UnsupportedError("Eigenvalues (zgeev) is not available in this build");

@@ -217,6 +217,27 @@ int bem2d_change_basis(bem2d_ctx* ctx, int n, const void* K, int64_t ldk, const 
 int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
                        double* norm, double* cond);
 
+/* Largest order bem2d_hermitian_eigenvalues accepts (its workspace holds an
+ * n x n complex128 matrix: 4.3 GB at the limit); bem2d_singular_values
+ * accepts half of it. */
+#define BEM2D_SPECTRA_MAX_N 16384
+
+/* w[0..n-1] = eigenvalues, ascending, of the Hermitian matrix whose upper
+ * triangle A holds (the diagonal's real part is used): replaces
+ * HermitianEigenvalues (lib/bem2d_mathroutines.cpp:353-433, zheev with
+ * jobz 'N', uplo 'U').  Householder reduction to real tridiagonal form on
+ * the GPU (four kernels per column), then bisection on Sturm counts, one
+ * thread per eigenvalue; absolute accuracy ~ n eps ||A||.  A: host or
+ * device; w: host or device. */
+int bem2d_hermitian_eigenvalues(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double* w);
+
+/* s[0..n-1] = singular values of A, descending: replaces SingularValues
+ * (lib/bem2d_mathroutines.cpp:268-320, zgesvd without vectors).  They are
+ * the n largest eigenvalues of the Hermitian [0 A; A^H 0], computed as in
+ * bem2d_hermitian_eigenvalues (absolute accuracy ~ n eps ||A||).
+ * n <= BEM2D_SPECTRA_MAX_N / 2. */
+int bem2d_singular_values(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double* s);
+
 /* lmax[j] = largest eigenvalue of (e^{i th_j} A + e^{-i th_j} A^H) / 2 for
  * nang angles th_j: the eigenvalue step of NumRange
  * (lib/bem2d_mathroutines.cpp:590-653, zheev per angle; the smallest

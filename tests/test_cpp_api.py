@@ -1,7 +1,8 @@
 """The reference-compatible C++ API (bem2d_gb300/lib).
 
-CPU: the reference's own driver programs (examples/, normcomps/) compile and
-link unchanged against it (needs the reference checkout; skipped without).
+CPU: the reference's own driver programs (examples/, normcomps/,
+numrangecomps/, resonances/) compile and link unchanged against it (needs
+the reference checkout; skipped without).
 GPU: a program written against the API reproduces the reference's disk
 results (tests/golden/disk160.npz)."""
 import os
@@ -32,7 +33,7 @@ def link(objs, out):
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "examples")),
                     reason="reference checkout not present")
-@pytest.mark.parametrize("sub", ["examples", "normcomps"])
+@pytest.mark.parametrize("sub", ["examples", "normcomps", "numrangecomps", "resonances"])
 def test_reference_drivers_compile_and_link_unchanged(built, tmp_path, sub):
     """Each driver #includes "../lib/bem2d.h": a sibling lib/ directory that is
     this build's API makes them compile as they are."""

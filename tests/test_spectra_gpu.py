@@ -1,0 +1,126 @@
+"""Dense spectra on the GPU: SingularValues (lib/bem2d_mathroutines.cpp:268-320,
+zgesvd) and HermitianEigenvalues (:353-433, zheev 'N', 'U') through the C ABI.
+
+Bars: singular values within 1e-12 sigma_max of LAPACK's (numpy) and of the
+reference's own output (tests/golden/square_numrange.npz: SingularValues of
+ChangeBasis(A, Id)); Hermitian eigenvalues within 1e-12 ||H||_2 of LAPACK's
+eigvalsh on the matrix the upper triangle defines.  Householder reduction
+and bisection are backward stable: absolute errors ~ n eps ||A||.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from golden.cases import CASES, QUAD
+
+pytestmark = pytest.mark.gpu
+
+
+def _load(name):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    return z, json.loads(str(z["meta"]))
+
+
+def blocks_of(g):
+    ue = g.arrays()["unk_elem"]
+    starts = [0] + [i for i in range(1, len(ue)) if ue[i] != ue[i - 1]] + [len(ue)]
+    return np.array(starts, dtype=np.int32)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from bem2d_gb300 import capi
+    c = capi.Context(0)
+    yield c
+    c.close()
+
+
+def crandn(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 130, 301])
+def test_singular_values_random(ctx, n):
+    rng = np.random.default_rng(n)
+    A = crandn(rng, n, n)
+    s = ctx.singular_values(A)
+    ref = np.linalg.svd(A, compute_uv=False)
+    assert np.all(np.diff(s) <= 0)
+    assert np.abs(s - ref).max() <= 1e-12 * ref[0]
+
+
+def test_singular_values_graded_spectrum(ctx):
+    """Singular values spread over 10 decades: small ones to absolute accuracy."""
+    rng = np.random.default_rng(3)
+    n = 96
+    U, _ = np.linalg.qr(crandn(rng, n, n))
+    V, _ = np.linalg.qr(crandn(rng, n, n))
+    sig = np.logspace(0, -10, n)
+    A = (U * sig) @ V.conj().T
+    s = ctx.singular_values(A)
+    assert np.abs(s - sig).max() <= 1e-13
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 257])
+def test_hermitian_eigenvalues_random(ctx, n):
+    rng = np.random.default_rng(100 + n)
+    A = crandn(rng, n, n)  # lower triangle and the diagonal's imaginary part are ignored
+    H = np.triu(A, 1) + np.triu(A, 1).conj().T + np.diag(A.diagonal().real)
+    w = ctx.hermitian_eigenvalues(A)
+    ref = np.linalg.eigvalsh(H)
+    assert np.all(np.diff(w) >= 0)
+    assert np.abs(w - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_singular_values_match_reference(ctx):
+    """SingularValues(ChangeBasis(A, Id)) as the reference computed it."""
+    z, _ = _load("square_numrange")
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    s = ctx.singular_values(B)
+    ref = z["singvals"]
+    assert np.abs(s - ref).max() <= 1e-12 * ref[0]
+
+
+def test_resonance_scan_quantity(ctx):
+    """The resonance scan (resonances/trapresonance.cpp) reads 1 / sigma_min of
+    ChangeBasis(A, Id) at complex k: here k = 6 - i on the trapping domain,
+    against the reference's norm and condition number of the same matrix."""
+    z, _ = _load("trap_ck")
+    spec = CASES["trap_ck"]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", complex(spec["k"], spec["kim"]), spec["eta"], QUAD,
+                            alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    s = ctx.singular_values(B)
+    ref_n, ref_c = z["normcond"]
+    assert abs(s[0] - ref_n) <= 1e-11 * ref_n
+    assert abs(s[-1] - ref_n / ref_c) <= 1e-11 * ref_n
+
+
+def test_device_buffers(ctx):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(8)
+    n = 50
+    A = crandn(rng, n, n)
+    # column-major view of a row-major torch tensor: store A^T row-major
+    dAt = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    from bem2d_gb300 import capi
+    out = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ctx._check(ctx.lib.bem2d_singular_values(ctx.h, n, capi._ptr(dAt), n, capi._ptr(out)))
+    ref = np.linalg.svd(A, compute_uv=False)
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-12 * ref[0]
+
+
+def test_rejects_bad_arguments(ctx):
+    from bem2d_gb300 import capi
+    with pytest.raises(capi.Bem2dError):
+        ctx._check(ctx.lib.bem2d_singular_values(ctx.h, 0, None, 1, None))
+    A = np.zeros((4, 4), dtype=np.complex128, order="F")
+    out = np.zeros(4)
+    with pytest.raises(capi.Bem2dError):  # lda < n
+        ctx._check(ctx.lib.bem2d_hermitian_eigenvalues(ctx.h, 4, capi._ptr(A), 3, capi._ptr(out)))
