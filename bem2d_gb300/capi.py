@@ -32,7 +32,8 @@ EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer",
            "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_num_range",
            "bem2d_eval_kernel", "bem2d_solve_system_noalloc",
-           "bem2d_sweep_solve", "bem2d_hermitian_eigenvalues", "bem2d_singular_values"]
+           "bem2d_sweep_solve", "bem2d_hermitian_eigenvalues", "bem2d_singular_values",
+           "bem2d_eigenvalues"]
 
 NOALLOC_MAX_N = 1024  # BEM2D_NOALLOC_MAX_N
 
@@ -106,6 +107,7 @@ def load():
         lib.bem2d_eval_kernel.argtypes = [vp, vp, vp, i32, d, d, d, vp, i32, vp, vp]
         lib.bem2d_hermitian_eigenvalues.argtypes = [vp, i32, vp, i64, vp]
         lib.bem2d_singular_values.argtypes = [vp, i32, vp, i64, vp]
+        lib.bem2d_eigenvalues.argtypes = [vp, i32, vp, i64, vp]
         lib.bem2d_ctx_enable_timers.argtypes = [vp, i32]
         lib.bem2d_ctx_timer.argtypes = [vp, i32, ctypes.POINTER(d), ctypes.POINTER(i64)]
         _LIB = lib
@@ -348,6 +350,15 @@ class Context:
             A = np.asfortranarray(A, dtype=np.complex128)
         out = np.zeros(n)
         self._check(self.lib.bem2d_singular_values(self.h, n, _ptr(A), _ld(A, n), _ptr(out)))
+        return out
+
+    def eigenvalues(self, A):
+        """Eigenvalues of the general complex A (Eigenvalues, zgeev)."""
+        n = A.shape[0]
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
+        out = np.zeros(n, dtype=np.complex128)
+        self._check(self.lib.bem2d_eigenvalues(self.h, n, _ptr(A), _ld(A, n), _ptr(out)))
         return out
 
     def potential(self, g, coeffs, points, kernel="single", k=10.0, eta=0.0, q=(3, 5, 0.15)):

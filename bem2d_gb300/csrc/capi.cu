@@ -1695,6 +1695,43 @@ int bem2d_singular_values(bem2d_ctx* c, int n, const void* A, int64_t lda, doubl
   return spectra_run(c, M, N, n, 1, s);
 }
 
+int bem2d_eigenvalues(bem2d_ctx* c, int n, const void* A, int64_t lda, void* w) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !w || lda < n) return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (n > BEM2D_EIG_MAX_N)
+    return fail(c, BEM2D_ERR_ARG, "order %d above BEM2D_EIG_MAX_N = %d", n, BEM2D_EIG_MAX_N);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "eig_in", &la, &rc);
+  if (!dA) return rc;
+  double2* H = static_cast<double2*>(ws(c, "eig_H", sizeof(double2) * (size_t)n * n, &rc));
+  void* work = ws(c, "eig_work", eig_work_bytes(n), &rc);
+  if (!H || !work) return rc;
+  const bool odev = is_device_ptr(w);
+  double2* dw = odev ? static_cast<double2*>(w)
+                     : static_cast<double2*>(ws(c, "eig_w", sizeof(double2) * n, &rc));
+  if (!dw) return rc;
+  CUDA_TRY(c, cudaMemcpy2DAsync(H, sizeof(double2) * n, dA, sizeof(double2) * la,
+                                sizeof(double2) * n, n, cudaMemcpyDeviceToDevice, c->stream));
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      sms < 1)
+    sms = 1;
+  c->launches += launch_eigenvalues(H, n, work, dw, sms, c->stream);
+  CHECK_LAUNCH(c);
+  int status = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&status, eig_status_ptr(work, n), sizeof(int),
+                              cudaMemcpyDeviceToHost, c->stream));
+  if (!odev)
+    CUDA_TRY(c, cudaMemcpyAsync(w, dw, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (status)
+    return fail(c, BEM2D_ERR_NOCONV, "QR iteration: %d eigenvalues not found within the limit",
+                status);
+  return BEM2D_OK;
+}
+
 int bem2d_eval_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
                       int kernel, double k_re, double k_im, double eta, const void* coeffs,
                       int npts, const double* points, void* out) {

@@ -491,4 +491,14 @@ void launch_jordan_wielandt(const double2* A, long long lda, int n, double2* M, 
 long long launch_tridiag_eigs(double2* M, int N, int count, int descending, void* work,
                               double* out, int sms, cudaStream_t s);
 
+// ---- launch interfaces (eig.cu) --------------------------------------------
+// Work bytes of launch_eigenvalues for order n.
+size_t eig_work_bytes(int n);
+// Eigenvalues of the general A (n x n, ld n, overwritten by its Hessenberg
+// form and the QR iterates) into w (device, n complex128).  Returns the
+// number of kernels launched; eig_status_ptr(work, n) then holds 0 or the
+// number of eigenvalues not found within the iteration limit.
+long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms, cudaStream_t s);
+int* eig_status_ptr(void* work, int n);
+
 }  // namespace bem2d_gpu

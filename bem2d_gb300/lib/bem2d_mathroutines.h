@@ -53,8 +53,9 @@ pMatrix SolveSystem(Matrix& m, Matrix& rhs);
 // All eigenvalues of the Hermitian matrix the upper triangle of k defines,
 // ascending (GPU Householder tridiagonalisation and bisection).
 void HermitianEigenvalues(const Matrix& k, pdvector& evalues);
-// All eigenvalues of a general matrix (not available in this build:
-// UnsupportedError).
+// All eigenvalues of a general matrix (GPU Hessenberg reduction and
+// shifted QR); the variant with eigenvectors is not available in this build
+// (UnsupportedError).
 void Eigenvalues(const Matrix& k, pcvector& evalues);
 void Eigenvalues(const Matrix& k, pcvector& evalues, pMatrix& evectors);
 // U^{-H} k U^{-1} with m = U^H U (m block diagonal per element, as mass

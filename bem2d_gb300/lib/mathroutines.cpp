@@ -112,11 +112,15 @@ void HermitianEigenvalues(const Matrix& k, pdvector& evalues) {
   detail::check(bem2d_hermitian_eigenvalues(detail::ctx(), n, &(*k.data)[0], n, &(*evalues)[0]),
                 "HermitianEigenvalues");
 }
-void Eigenvalues(const Matrix&, pcvector&) {
-  throw UnsupportedError("Eigenvalues (zgeev) is not available in this build");
+void Eigenvalues(const Matrix& k, pcvector& evalues) {
+  if (k.dim[0] != k.dim[1]) throw ArrayMismatch();
+  const int n = k.dim[0];
+  evalues = pcvector(new cvector(n));
+  detail::check(bem2d_eigenvalues(detail::ctx(), n, &(*k.data)[0], n, &(*evalues)[0]),
+                "Eigenvalues");
 }
 void Eigenvalues(const Matrix&, pcvector&, pMatrix&) {
-  throw UnsupportedError("Eigenvalues (zgeev) is not available in this build");
+  throw UnsupportedError("Eigenvalues with eigenvectors (zgeev 'V') is not available in this build");
 }
 
 Matrix ChangeBasis(const Matrix& k, const Matrix& m) {

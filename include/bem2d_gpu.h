@@ -238,6 +238,21 @@ int bem2d_hermitian_eigenvalues(bem2d_ctx* ctx, int n, const void* A, int64_t ld
  * n <= BEM2D_SPECTRA_MAX_N / 2. */
 int bem2d_singular_values(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double* s);
 
+/* Largest order bem2d_eigenvalues accepts: its QR iteration runs on one
+ * CTA, about n^2 dependent rotation steps of a few microseconds each. */
+#define BEM2D_EIG_MAX_N 4096
+
+/* w[0..n-1] (complex128) = eigenvalues of the general complex A: replaces
+ * Eigenvalues(const Matrix&, pcvector&) (lib/bem2d_mathroutines.cpp:437-466,
+ * zgeev without eigenvectors).  Householder reduction to upper Hessenberg
+ * form on the GPU (six kernels per column), then implicitly shifted QR
+ * (Wilkinson shifts, exceptional shifts, closed-form 2 x 2 blocks) in one
+ * CTA; no balancing.  Eigenvalues come in the order they deflate (bottom of
+ * the matrix first), as in LAPACK's QR.  BEM2D_ERR_NOCONV if the iteration
+ * limit 30 max(10, n) is reached.  A: host or device (not modified);
+ * w: host or device. */
+int bem2d_eigenvalues(bem2d_ctx* ctx, int n, const void* A, int64_t lda, void* w);
+
 /* lmax[j] = largest eigenvalue of (e^{i th_j} A + e^{-i th_j} A^H) / 2 for
  * nang angles th_j: the eigenvalue step of NumRange
  * (lib/bem2d_mathroutines.cpp:590-653, zheev per angle; the smallest

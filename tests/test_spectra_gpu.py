@@ -1,11 +1,16 @@
 """Dense spectra on the GPU: SingularValues (lib/bem2d_mathroutines.cpp:268-320,
-zgesvd) and HermitianEigenvalues (:353-433, zheev 'N', 'U') through the C ABI.
+zgesvd), HermitianEigenvalues (:353-433, zheev 'N', 'U') and Eigenvalues
+(:437-466, zgeev 'N', 'N') through the C ABI.
 
 Bars: singular values within 1e-12 sigma_max of LAPACK's (numpy) and of the
 reference's own output (tests/golden/square_numrange.npz: SingularValues of
 ChangeBasis(A, Id)); Hermitian eigenvalues within 1e-12 ||H||_2 of LAPACK's
-eigvalsh on the matrix the upper triangle defines.  Householder reduction
-and bisection are backward stable: absolute errors ~ n eps ||A||.
+eigvalsh on the matrix the upper triangle defines; general eigenvalues
+within 1e-12 max|lambda| of known eigenvalues of normal matrices and within
+1e-11 ||A||_2 of LAPACK's zgeev (numpy) for random and boundary-element
+matrices, matched as sets.  Householder reduction, bisection and shifted QR
+are backward stable: absolute errors ~ n eps ||A|| times the eigenvalues'
+condition numbers.
 """
 import json
 import os
@@ -124,3 +129,48 @@ def test_rejects_bad_arguments(ctx):
     out = np.zeros(4)
     with pytest.raises(capi.Bem2dError):  # lda < n
         ctx._check(ctx.lib.bem2d_hermitian_eigenvalues(ctx.h, 4, capi._ptr(A), 3, capi._ptr(out)))
+
+
+def match_err(a, b):
+    """Largest distance between the eigenvalue sets a and b under the best
+    one-to-one pairing."""
+    from scipy.optimize import linear_sum_assignment
+    C = np.abs(a[:, None] - b[None, :])
+    r, c = linear_sum_assignment(C)
+    return C[r, c].max()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 10, 64, 200])
+def test_eigenvalues_random(ctx, n):
+    rng = np.random.default_rng(200 + n)
+    A = crandn(rng, n, n)
+    w = ctx.eigenvalues(A)
+    assert match_err(w, np.linalg.eigvals(A)) <= 1e-11 * np.linalg.norm(A, 2)
+
+
+def test_eigenvalues_normal_known(ctx):
+    rng = np.random.default_rng(17)
+    n = 120
+    Q, _ = np.linalg.qr(crandn(rng, n, n))
+    lam = crandn(rng, n)
+    A = (Q * lam) @ Q.conj().T
+    w = ctx.eigenvalues(A)
+    assert match_err(w, lam) <= 1e-12 * np.abs(lam).max() * 10
+
+
+def test_eigenvalues_structured(ctx):
+    rng = np.random.default_rng(4)
+    T = np.triu(crandn(rng, 40, 40))
+    assert match_err(ctx.eigenvalues(T), np.diag(T)) <= 1e-13 * np.abs(T).max()
+    assert np.abs(ctx.eigenvalues(np.eye(7, dtype=np.complex128)) - 1).max() <= 1e-15
+    assert np.abs(ctx.eigenvalues(np.zeros((5, 5), dtype=np.complex128))).max() == 0
+
+
+def test_eigenvalues_boundary_element_matrix(ctx):
+    """The numrangecomps drivers' call: Eigenvalues(ChangeBasis(A, Id))."""
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    w = ctx.eigenvalues(B)
+    assert match_err(w, np.linalg.eigvals(B)) <= 1e-11 * np.linalg.norm(B, 2)
