@@ -13,6 +13,8 @@
  *   kernels S, D, D', combined     lib/bem2d_kernel.cpp:15-112
  *   Hankel H0/H1 (real argument)   lib/bem2d_mathroutines.cpp:20-42, with
  *                                  POSIX j0/j1/y0/y1 standing in for GSL
+ *   Hankel H0/H1 (complex argument, lib/bem2d_mathroutines.cpp:44-75, AMOS
+ *   zbesh): binary128 series / asymptotic expansion (hankel_q.h)
  *   Integrate / IntegrateIdent     lib/bem2d_quadrature.h:37-109
  *   DiscreteKernel                 lib/bem2d_quadrature.h:231-294
  *   EvalIdent                      lib/bem2d_quadrature.cpp:79-127
@@ -21,6 +23,7 @@
  */
 #define _DEFAULT_SOURCE 1 /* POSIX j0/j1/y0/y1 */
 #include "bem2d_oracle.h"
+#include "hankel_q.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -322,10 +325,40 @@ static double basis_eval(const orc_geometry* g, int u, double t) {
 }
 
 /* ---- kernels ----------------------------------------------------------- */
-static cplx kernel_eval(int kernel, double k, double eta, double xx, double xy,
+/* Complex wavenumber k + i ki (lib/bem2d_kernel.cpp:15-112, k.im != 0
+ * branches): S = i/4 H0(kd), D / D' = -i k/4 H1(kd)/d (n.w), combined
+ * D' - i eta S with eta real. */
+static cplx kernel_eval_c(int kernel, double k, double ki, double eta, double xx, double xy,
+                          double yx, double yy, double n1x, double n1y, double n2x,
+                          double n2y) {
+  double wx = xx - yx, wy = xy - yy;
+  double d = plength(wx, wy);
+  double h0r, h0i, h1r, h1i;
+  orc_hankel01_q(k * d, ki * d, &h0r, &h0i, &h1r, &h1i);
+  cplx r;
+  if (kernel == K_SINGLE) {
+    r.re = -h0i / 4.0;
+    r.im = h0r / 4.0;
+    return r;
+  }
+  double dot = kernel == K_DOUBLE ? -(n2x * wx + n2y * wy) : (n1x * wx + n1y * wy);
+  /* p = k H1 dot / d; -i p / 4 */
+  double pr = (k * h1r - ki * h1i) * dot / d, pi = (k * h1i + ki * h1r) * dot / d;
+  r.re = pi / 4.0;
+  r.im = -pr / 4.0;
+  if (kernel == K_COMBINED) {
+    r.re += eta * (h0r / 4.0);
+    r.im += eta * (h0i / 4.0);
+  }
+  return r;
+}
+
+static cplx kernel_eval(int kernel, double k, double ki, double eta, double xx, double xy,
                         double yx, double yy, double n1x, double n1y,
                         double n2x, double n2y) {
   cplx r;
+  if (ki != 0.0)
+    return kernel_eval_c(kernel, k, ki, eta, xx, xy, yx, yy, n1x, n1y, n2x, n2y);
   if (kernel == K_SINGLE) {
     double d = plength(xx - yx, xy - yy);
     double kd = k * d;
@@ -358,7 +391,7 @@ static cplx kernel_eval(int kernel, double k, double eta, double xx, double xy,
 
 /* Integrate<kernel,T>, lib/bem2d_quadrature.h:37-65 */
 static cplx integrate(const orc_geometry* g, int ui, int uj, int kernel,
-                      double k, double eta, const rule2d* r) {
+                      double k, double ki, double eta, const rule2d* r) {
   int e1 = g->unk_elem[ui], e2 = g->unk_elem[uj];
   cplx acc = {0, 0};
   for (int q = 0; q < r->n; ++q) {
@@ -369,7 +402,7 @@ static cplx integrate(const orc_geometry* g, int ui, int uj, int kernel,
     normal_of(&p2, &n2x, &n2y);
     double f1 = basis_eval(g, ui, r->x[q]);
     double f2 = basis_eval(g, uj, r->y[q]);
-    cplx v = kernel_eval(kernel, k, eta, p1.mx, p1.my, p2.mx, p2.my, n1x, n1y,
+    cplx v = kernel_eval(kernel, k, ki, eta, p1.mx, p1.my, p2.mx, p2.my, n1x, n1y,
                          n2x, n2y);
     double s1 = plength(p1.dx, p1.dy), s2 = plength(p2.dx, p2.dy);
     v = cscale(v, f1 * f2);
@@ -385,7 +418,7 @@ static cplx integrate(const orc_geometry* g, int ui, int uj, int kernel,
 /* IntegrateIdent, lib/bem2d_quadrature.h:67-109 (Duffy split of the
  * self-element square into two triangles). */
 static cplx integrate_ident(const orc_geometry* g, int ui, int uj, int kernel,
-                            double k, double eta, const rule2d* r) {
+                            double k, double ki, double eta, const rule2d* r) {
   int e1 = g->unk_elem[ui], e2 = g->unk_elem[uj];
   cplx acc = {0, 0};
   for (int q = 0; q < r->n; ++q) {
@@ -400,7 +433,7 @@ static cplx integrate_ident(const orc_geometry* g, int ui, int uj, int kernel,
       normal_of(&p2, &n2x, &n2y);
       double f1 = basis_eval(g, ui, s[h]);
       double f2 = basis_eval(g, uj, t[h]);
-      cplx v = kernel_eval(kernel, k, eta, p1.mx, p1.my, p2.mx, p2.my, n1x,
+      cplx v = kernel_eval(kernel, k, ki, eta, p1.mx, p1.my, p2.mx, p2.my, n1x,
                            n1y, n2x, n2y);
       double s1 = plength(p1.dx, p1.dy), s2 = plength(p2.dx, p2.dy);
       v = cscale(v, x);
@@ -452,15 +485,15 @@ static void rules_free(rules_t* r) {
 /* One entry of beta*Id + alpha*K, with DiscreteKernel's rule selection
  * (lib/bem2d_quadrature.h:264-289). */
 static cplx entry(const orc_geometry* g, const rules_t* r, int N, int i, int j,
-                  int kernel, double k, double eta, double alpha, double beta) {
+                  int kernel, double k, double ki, double eta, double alpha, double beta) {
   int ei = g->unk_elem[i], ej = g->unk_elem[j];
   int64_t indi = g->index[ei], indj = g->index[ej];
   cplx v;
   int same = indi == indj;
-  if (same) v = integrate_ident(g, i, j, kernel, k, eta, &r->g1);
-  else if (g->next[ei] == indj) v = integrate(g, i, j, kernel, k, eta, &r->g3);
-  else if (g->prev[ei] == indj) v = integrate(g, i, j, kernel, k, eta, &r->g2);
-  else v = integrate(g, i, j, kernel, k, eta, &r->g0);
+  if (same) v = integrate_ident(g, i, j, kernel, k, ki, eta, &r->g1);
+  else if (g->next[ei] == indj) v = integrate(g, i, j, kernel, k, ki, eta, &r->g3);
+  else if (g->prev[ei] == indj) v = integrate(g, i, j, kernel, k, ki, eta, &r->g2);
+  else v = integrate(g, i, j, kernel, k, ki, eta, &r->g0);
   cplx o = {alpha * v.re, alpha * v.im};
   if (beta != 0.0 && same) {
     cplx m = ident_entry(g, i, j, N, r->xt, r->wt);
@@ -473,6 +506,12 @@ static cplx entry(const orc_geometry* g, const rules_t* r, int N, int i, int j,
 int orc_discrete_kernel(const orc_geometry* g, int L, int N, double sigma,
                         int kernel, double k, double eta, double alpha,
                         double beta, double* out, int nthreads) {
+  return orc_discrete_kernel_c(g, L, N, sigma, kernel, k, 0.0, eta, alpha, beta, out, nthreads);
+}
+
+int orc_discrete_kernel_c(const orc_geometry* g, int L, int N, double sigma,
+                          int kernel, double k, double ki, double eta, double alpha,
+                          double beta, double* out, int nthreads) {
   rules_t r;
   int rc = rules_make(&r, L, N, sigma);
   if (rc) return rc;
@@ -483,7 +522,7 @@ int orc_discrete_kernel(const orc_geometry* g, int L, int N, double sigma,
 #endif
   for (int j = 0; j < n; ++j) {
     for (int i = 0; i < n; ++i) {
-      cplx v = entry(g, &r, N, i, j, kernel, k, eta, alpha, beta);
+      cplx v = entry(g, &r, N, i, j, kernel, k, ki, eta, alpha, beta);
       out[2 * ((size_t)i + (size_t)n * j)] = v.re;
       out[2 * ((size_t)i + (size_t)n * j) + 1] = v.im;
     }
@@ -506,7 +545,7 @@ int orc_discrete_kernel_rows(const orc_geometry* g, int L, int N, double sigma,
 #endif
   for (int q = 0; q < nrows; ++q) {
     for (int j = 0; j < n; ++j) {
-      cplx v = entry(g, &r, N, rows[q], j, kernel, k, eta, alpha, beta);
+      cplx v = entry(g, &r, N, rows[q], j, kernel, k, 0.0, eta, alpha, beta);
       out[2 * ((size_t)q * n + j)] = v.re;
       out[2 * ((size_t)q * n + j) + 1] = v.im;
     }
@@ -533,6 +572,12 @@ int orc_eval_ident(const orc_geometry* g, int N, double* out) {
 
 int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
             double dy, double eta, double scale, double* out) {
+  return orc_rhs_c(g, N, fun, k, 0.0, dx, dy, eta, scale, out);
+}
+
+/* Complex wavenumber k + i ki: f = exp(i (k + i ki) d.x) (lib/bem2d_fun.h:14-93). */
+int orc_rhs_c(const orc_geometry* g, int N, int fun, double k, double ki, double dx,
+              double dy, double eta, double scale, double* out) {
   double xt[64], wt[64];
   if (N < 1 || N > 64) return -1;
   if (orc_gauss(N, xt, wt)) return -2;
@@ -543,14 +588,17 @@ int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
       elem_pt p = elem_eval(g, e, xt[q]);
       double nx, ny;
       normal_of(&p, &nx, &ny);
-      double ph = k * (dx * p.mx + dy * p.my);
-      cplx f = {cos(ph), sin(ph)};
+      double dd = dx * p.mx + dy * p.my;
+      double ph = k * dd;
+      double amp = ki != 0.0 ? exp(-ki * dd) : 1.0;
+      cplx f = {amp * cos(ph), amp * sin(ph)};
       cplx v;
       if (fun == 0) {
         v = f;
       } else {
         double nd = nx * dx + ny * dy;
-        cplx ikf = {-k * f.im, k * f.re}; /* i k f */
+        /* i (k + i ki) f */
+        cplx ikf = {-k * f.im - ki * f.re, k * f.re - ki * f.im};
         v = cscale(ikf, nd);
         if (fun == 2) {
           /* - i eta f */
@@ -575,6 +623,11 @@ int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
  * K(p_j, y_uq) |J| phi_u(y_uq) w_q, both normals set to the source normal. */
 int orc_potential(const orc_geometry* g, int N, int kernel, double k, double eta,
                   const double* coeffs, int npts, const double* pts, double* out) {
+  return orc_potential_c(g, N, kernel, k, 0.0, eta, coeffs, npts, pts, out);
+}
+
+int orc_potential_c(const orc_geometry* g, int N, int kernel, double k, double ki, double eta,
+                    const double* coeffs, int npts, const double* pts, double* out) {
   double xt[64], wt[64];
   if (N < 1 || N > 64) return -1;
   if (orc_gauss(N, xt, wt)) return -2;
@@ -589,8 +642,8 @@ int orc_potential(const orc_geometry* g, int N, int kernel, double k, double eta
         elem_pt p = elem_eval(g, e, xt[q]);
         double nx, ny;
         normal_of(&p, &nx, &ny);
-        cplx v = kernel_eval(kernel, k, eta, pts[2 * j], pts[2 * j + 1], p.mx, p.my, nx, ny,
-                             nx, ny);
+        cplx v = kernel_eval(kernel, k, ki, eta, pts[2 * j], pts[2 * j + 1], p.mx, p.my, nx,
+                             ny, nx, ny);
         const double w = plength(p.dx, p.dy) * basis_eval(g, u, xt[q]) * wt[q];
         const double cr = coeffs[2 * u], ci = coeffs[2 * u + 1];
         ar += (cr * v.re - ci * v.im) * w;

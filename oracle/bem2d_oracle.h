@@ -37,6 +37,11 @@ int orc_discrete_kernel(const orc_geometry* g, int L, int N, double sigma,
                         int kernel, double k, double eta, double alpha,
                         double beta, double* out, int nthreads);
 
+/* orc_discrete_kernel with a complex wavenumber k + i ki. */
+int orc_discrete_kernel_c(const orc_geometry* g, int L, int N, double sigma,
+                          int kernel, double k, double ki, double eta, double alpha,
+                          double beta, double* out, int nthreads);
+
 /* rows of beta*Id + alpha*K: out[q*n_unk + j] = entry (rows[q], j). */
 int orc_discrete_kernel_rows(const orc_geometry* g, int L, int N, double sigma,
                              int kernel, double k, double eta, double alpha,
@@ -51,10 +56,18 @@ int orc_eval_ident(const orc_geometry* g, int N, double* out);
 int orc_rhs(const orc_geometry* g, int N, int fun, double k, double dx,
             double dy, double eta, double scale, double* out);
 
+/* orc_rhs with a complex wavenumber k + i ki. */
+int orc_rhs_c(const orc_geometry* g, int N, int fun, double k, double ki, double dx,
+              double dy, double eta, double scale, double* out);
+
 /* potential of the density coeffs (complex128[n_unk]) at npts points
  * (x0 y0 x1 y1 ...): EvalKernel. */
 int orc_potential(const orc_geometry* g, int N, int kernel, double k, double eta,
                   const double* coeffs, int npts, const double* pts, double* out);
+
+/* orc_potential with a complex wavenumber k + i ki. */
+int orc_potential_c(const orc_geometry* g, int N, int kernel, double k, double ki, double eta,
+                    const double* coeffs, int npts, const double* pts, double* out);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,13 @@ _LIB = None
 KERNELS = {"single": 0, "double": 1, "conjdouble": 2, "combined": 3}
 
 
+def _k(k, eta):
+    """(Re k, Im k, eta): a complex k selects the oracle's binary128 Hankel
+    functions (the reference's AMOS branch); eta defaults to Re k."""
+    kc = complex(k)
+    return kc.real, kc.imag, (kc.real if eta is None else float(eta))
+
+
 class _Geom(ctypes.Structure):
     _fields_ = [("n_elem", ctypes.c_int32),
                 ("kind", ctypes.c_void_p), ("param", ctypes.c_void_p),
@@ -63,15 +70,17 @@ def gauss(n):
 
 def discrete_kernel(g, kernel="combined", k=10.0, eta=None, quad=(3, 5, 0.15),
                     alpha=1.0, beta=0.0, threads=0):
-    """beta*Id + alpha*DiscreteKernel(g, quad, kernel) as complex128 (n x n)."""
+    """beta*Id + alpha*DiscreteKernel(g, quad, kernel) as complex128 (n x n);
+    k real or complex."""
     s, keep = _geom(g)
     n = s.n_unk
     out = np.zeros((n, n), dtype=np.complex128, order="F")
-    eta = float(k) if eta is None else float(eta)
+    kr, ki, eta = _k(k, eta)
     L, N, sigma = quad
-    rc = lib().orc_discrete_kernel(
+    rc = lib().orc_discrete_kernel_c(
         ctypes.byref(s), ctypes.c_int(L), ctypes.c_int(N), ctypes.c_double(sigma),
-        ctypes.c_int(KERNELS[kernel]), ctypes.c_double(k), ctypes.c_double(eta),
+        ctypes.c_int(KERNELS[kernel]), ctypes.c_double(kr), ctypes.c_double(ki),
+        ctypes.c_double(eta),
         ctypes.c_double(alpha), ctypes.c_double(beta),
         out.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(threads))
     assert rc == 0, rc
@@ -107,12 +116,13 @@ def eval_ident(g, N=5):
 
 
 def rhs(g, k, direction, eta=None, N=5, fun=2, scale=2.0):
-    """scale * DotProdBasFuns(g, quad, CombinedPlaneWave(direction, k, eta))."""
+    """scale * DotProdBasFuns(g, quad, CombinedPlaneWave(direction, k, eta));
+    k real or complex."""
     s, keep = _geom(g)
     out = np.zeros(s.n_unk, dtype=np.complex128)
-    eta = float(k) if eta is None else float(eta)
-    rc = lib().orc_rhs(ctypes.byref(s), ctypes.c_int(N), ctypes.c_int(fun),
-                       ctypes.c_double(k), ctypes.c_double(direction[0]),
+    kr, ki, eta = _k(k, eta)
+    rc = lib().orc_rhs_c(ctypes.byref(s), ctypes.c_int(N), ctypes.c_int(fun),
+                       ctypes.c_double(kr), ctypes.c_double(ki), ctypes.c_double(direction[0]),
                        ctypes.c_double(direction[1]), ctypes.c_double(eta),
                        ctypes.c_double(scale), out.ctypes.data_as(ctypes.c_void_p))
     assert rc == 0
@@ -160,13 +170,15 @@ def numrange_lmax(A, thetas):
 
 
 def potential(g, coeffs, points, kernel="single", k=10.0, eta=0.0, N=5):
-    """EvalKernel: sum_u c_u int K(p, y) phi_u(y) ds(y) at the points."""
+    """EvalKernel: sum_u c_u int K(p, y) phi_u(y) ds(y) at the points; k real
+    or complex."""
     s, keep = _geom(g)
     c = np.ascontiguousarray(coeffs, dtype=np.complex128)
     pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
     out = np.zeros(len(pts), dtype=np.complex128)
-    rc = lib().orc_potential(ctypes.byref(s), ctypes.c_int(N), ctypes.c_int(KERNELS[kernel]),
-                             ctypes.c_double(k), ctypes.c_double(eta),
+    kr, ki, eta = _k(k, eta)
+    rc = lib().orc_potential_c(ctypes.byref(s), ctypes.c_int(N), ctypes.c_int(KERNELS[kernel]),
+                             ctypes.c_double(kr), ctypes.c_double(ki), ctypes.c_double(eta),
                              c.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(len(pts)),
                              pts.ctypes.data_as(ctypes.c_void_p),
                              out.ctypes.data_as(ctypes.c_void_p))

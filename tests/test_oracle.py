@@ -38,15 +38,15 @@ def built():
     _build.build_oracle(with_reference=False)
 
 
-# The restatement covers real wavenumbers; the complex-k cases are pinned
-# directly against the reference's outputs by the GPU tests.
-@pytest.mark.parametrize("name", sorted(n for n in CASES if not CASES[n].get("kim")))
+# Real and complex wavenumbers (the *_ck cases: the reference's AMOS branch,
+# its zbesh served by the binary128 evaluator of oracle/hankel_q.h).
+@pytest.mark.parametrize("name", sorted(CASES))
 def test_port_matches_reference(name):
     z, meta = load(name)
     spec = CASES[name]
     g = spec["geom"]()
     assert g.n_unknowns == meta["n"]
-    k, eta, d = spec["k"], spec["eta"], spec["direction"]
+    k, eta, d = complex(spec["k"], spec.get("kim", 0.0)), spec["eta"], spec["direction"]
     M = O.eval_ident(g, QUAD[1])
     assert np.abs(np.diag(M) - z["ident_diag"]).max() <= 1e-15 * np.abs(z["ident_diag"]).max()
     if "rhs" in z:
@@ -60,11 +60,23 @@ def test_port_matches_reference(name):
             assert rel(A[z["sample_i"], z["sample_j"]], z["sample"]) < TOL_MAT
             assert rel(np.diag(A), z["diag"]) < TOL_MAT
         x = O.solve(A, b)
-        # the graded L-shape is ill-conditioned (element sizes down to 0.15^8)
-        assert rel(x, z["x"]) < (1e-8 if name == "lshape_graded" else 1e-11)
+        # the graded L-shape is ill-conditioned (element sizes down to 0.15^8);
+        # with Im k < 0 the kernel grows and cond(A) reaches 7e4 (kite_ck):
+        # solutions and sigma_min then move by about cond(A) times the
+        # matrix difference
+        dA = rel(A, z["A"]) if "A" in z else 1e-15
+        tol = max(1e-8 if name == "lshape_graded" else 1e-11,
+                  10 * np.linalg.cond(z["A"]) * dA if "A" in z else 0.0)
+        assert rel(x, z["x"]) < tol
         nrm, cond = O.norm_cond(O.change_basis(A, M))
         assert abs(nrm - z["normcond"][0]) < 1e-12 * nrm
-        assert abs(cond - z["normcond"][1]) < (1e-8 if name == "lshape_graded" else 1e-11) * cond
+        assert abs(cond - z["normcond"][1]) < tol * cond
+        if "evalsol" in z:
+            # EvalSol: u = u_inc - S x at the field points
+            pts = z["evalsol_points"]
+            u = np.exp(1j * k * (d[0] * pts[:, 0] + d[1] * pts[:, 1])) - O.potential(
+                g, z["x"], pts, "single", k)
+            assert rel(u, z["evalsol"]) < 1e-12
     for kn in spec.get("kernels", ()):
         K = O.discrete_kernel(g, kn, k, eta, QUAD)
         R = z["K_" + kn]
