@@ -70,3 +70,26 @@ def test_api_program_matches_reference(built, tmp_path):
     assert np.linalg.norm(u - z["evalsol"]) < 1e-11 * np.linalg.norm(z["evalsol"])
     a00 = complex(float(vals[6][0]), float(vals[6][1]))
     assert abs(a00 - z["A"][0, 0]) < 1e-13 * abs(z["A"][0, 0])
+
+
+def test_api_complex_hankel_host(built, tmp_path):
+    """BesselH0 / BesselH1 of a complex argument and SingleLayer at a complex
+    wavenumber, evaluated on the host by the C++ API, against the reference's
+    own values (tests/golden/hankel_ck.npz)."""
+    exe = str(tmp_path / "api_hankel")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I" + LIB,
+                    os.path.join(ROOT, "tests", "native", "api_hankel.cpp"), "-o", exe,
+                    os.path.join(LIB, "bem2d.a"), GPU_SO, "-Wl,-rpath," + os.path.dirname(GPU_SO)],
+                   check=True)
+    z = np.load(os.path.join(ROOT, "tests", "golden", "hankel_ck.npz"))
+    pts = z["z"]
+    inp = "".join("%.17g %.17g\n" % (p.real, p.imag) for p in pts)
+    out = subprocess.run([exe], input=inp, check=True, capture_output=True, text=True).stdout
+    v = np.array([[float(t) for t in l.split()] for l in out.splitlines()])
+    h0 = v[:, 0] + 1j * v[:, 1]
+    h1 = v[:, 2] + 1j * v[:, 3]
+    sl = v[:, 4] + 1j * v[:, 5]
+    scale = 1 + np.abs(pts) / 50
+    assert (np.abs(h0 - z["h0"]) / np.abs(z["h0"]) / scale).max() < 4e-15
+    assert (np.abs(h1 - z["h1"]) / np.abs(z["h1"]) / scale).max() < 4e-15
+    assert (np.abs(sl - 0.25j * z["h0"]) / np.abs(z["h0"]) / scale).max() < 4e-15
