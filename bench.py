@@ -44,7 +44,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 QUAD = (3, 5, 0.15)
-# numerical range (config 5b): both arms stop each angle at the same error
+# numerical range scan: both arms stop each angle at the same error
 # estimate, 1e-11 of |H| (ten times below the 1e-10 accuracy bar)
 NR_TOL = 1e-11
 SWEEP_WORKERS = 16
@@ -206,7 +206,8 @@ AUX = {
 
 
 def run_aux(args):
-    """Norm / condition (BASELINE config 3) and numerical range (config 5b):
+    """Norm / condition (graded square, N = 8192, k = 200) and numerical range
+    (unit square, N = 2048, k = 50, 360 angles):
     one step = mixed assembly + ChangeBasis(A, Id) + the study, through the C
     ABI.  The results are checked once, untimed, against dense cuSOLVER
     spectra (torch.linalg)."""
@@ -418,8 +419,8 @@ def run_ours(args):
                              precision="fp64", out=x_fp64[big])
 
     # -- headline: mixed path, device-resident results ------------------------
-    clk_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                            else "_build", "bench_clocks_%d.csv" % rank)
+    clk_path = os.path.join(os.environ.get("BEM2D_CLOCKS_DIR", os.path.join(ROOT, "_build")),
+                            "bench_clocks_%d.csv" % rank)
     os.makedirs(os.path.dirname(clk_path), exist_ok=True)
     cp, cf = clocks_start(clk_path)
     l0 = ctx.launches

@@ -41,7 +41,7 @@ def _two_squares():
 
 # name -> dict(geom=callable, k, direction, eta, quad, full, kernels, extra)
 CASES = {
-    # BASELINE config 1: unit disk, 160 equal-arc elements, k = 10, d = (1,0)
+    # unit disk, 160 equal-arc elements, k = 10, d = (1,0)
     "disk160": dict(geom=lambda: G.curve_equispaced(G.CIRCLE, 160).add_poly_basis(0),
                     k=10.0, direction=(1.0, 0.0), eta=10.0, full=True,
                     kernels=("single", "double", "conjdouble"),
