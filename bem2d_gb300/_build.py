@@ -96,12 +96,12 @@ def build_cpp(force=False):
 
 def build_oracle(with_reference=None):
     """The CPU oracle (test infrastructure): the C restatement always, the
-    reference library itself when its sources are present."""
+    reference library itself when BEM2D_REFERENCE names its checkout."""
     oracle = os.path.join(ROOT, "oracle")
     _run(["make", "-C", oracle, "port"])
-    ref = os.environ.get("BEM2D_REFERENCE", "/root/reference")
+    ref = os.environ.get("BEM2D_REFERENCE", "")
     if with_reference is None:
-        with_reference = os.path.isdir(os.path.join(ref, "lib"))
+        with_reference = bool(ref) and os.path.isdir(os.path.join(ref, "lib"))
     if with_reference:
         _run(["make", "-C", oracle, "-j8", "ref", "REF=" + ref])
 

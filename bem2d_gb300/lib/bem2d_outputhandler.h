@@ -31,7 +31,8 @@ class OutputHandler {
 
 typedef std::shared_ptr<OutputHandler> pOutputHandler;
 
-// gnuplot data + script files <name>_<field>_{real,imag}
+// gnuplot data + script files <name>inc, <name>scatt, <name>full (and
+// their _gplot scripts): real or imaginary parts on the mesh
 class GplotOutput : public OutputHandler {
  public:
   GplotOutput(int xpts, int ypts, double ax, double bx, double ay, double by, std::string name);
@@ -42,7 +43,6 @@ class GplotOutput : public OutputHandler {
                 const cvector& valsfull);
 
  private:
-  void Write(const std::string& field, const cvector& vals);
   std::string name_;
   int xpts_, ypts_;
 };

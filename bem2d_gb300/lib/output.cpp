@@ -1,77 +1,122 @@
 // bem2d C++ API (GB300 build): text output (plot grids, matrices, densities).
 #include <fstream>
+#include <map>
 
 #include "bem2d_outputhandler.h"
 #include "bem2d_outputroutines.h"
 
 namespace bem2d {
 
+// The text formats below are the reference library's
+// (lib/bem2d_outputroutines.cpp): same file names, point order, sampling and
+// column layout, default stream formatting, so drivers write the same files.
+
 void Abrange(dvector& xx, double a, double b, int n) {
   xx.resize(n);
-  for (int i = 0; i < n; ++i) xx[i] = n > 1 ? a + (b - a) * i / (n - 1) : a;
+  const double h = 1.0 / (n - 1);
+  for (int i = 0; i < n; ++i) xx[i] = a + h * i * (b - a);
 }
 
+// x outer, y inner: point (i, j) at index i * ypts + j
 std::shared_ptr<std::vector<Point> > MeshGrid(double ax, double bx, double ay, double by, int xpts,
                                               int ypts) {
   dvector xs, ys;
   Abrange(xs, ax, bx, xpts);
   Abrange(ys, ay, by, ypts);
   std::shared_ptr<std::vector<Point> > p(new std::vector<Point>);
-  for (int j = 0; j < ypts; ++j)
-    for (int i = 0; i < xpts; ++i) p->push_back(Point(xs[i], ys[j]));
+  p->reserve((std::size_t)xpts * ypts);
+  for (int i = 0; i < xpts; ++i)
+    for (int j = 0; j < ypts; ++j) p->push_back(Point(xs[i], ys[j]));
   return p;
 }
 
-void GplotOut(std::string name, const std::vector<Point>& points, const dvector& z, int xpts, int ypts) {
-  std::ofstream d((name + ".dat").c_str());
-  for (int j = 0; j < ypts; ++j) {
+// data file `name` (a blank line after each x column) and gnuplot script
+// `name`_gplot
+void GplotOut(std::string name, const std::vector<Point>& points, const dvector& z, int xpts,
+              int ypts) {
+  {
+    std::ofstream d(name.c_str());
     for (int i = 0; i < xpts; ++i) {
-      const std::size_t k = (std::size_t)j * xpts + i;
-      d << points[k].x << " " << points[k].y << " " << z[k] << "\n";
+      for (int j = 0; j < ypts; ++j) {
+        const std::size_t k = (std::size_t)i * ypts + j;
+        d << points[k].x << " " << points[k].y << " " << z[k] << "\n";
+      }
+      d << "\n";
     }
-    d << "\n";
   }
-  std::ofstream s((name + ".gnuplot").c_str());
-  s << "set pm3d map\nset size ratio -1\nsplot '" << name << ".dat' with pm3d notitle\n";
+  std::ofstream s((name + "_gplot").c_str());
+  s << "set pm3d map\n"
+    << "set hidden3d\n"
+    << "set datafile missing \"nan\"\n"
+    << "set palette rgbformulae 33,13,10\n"
+    << "set size ratio -1\n"
+    << "set size square\n"
+    << "set cbrange [-1:1]\n"
+    << "splot '" << name << "'\n"
+    << "pause -1\n";
 }
 
+// `fname`_real and `fname`_imag: row i holds entries (i, j) of the leading
+// dim[0] x dim[0] block, each followed by a space
 void WriteMatrix(std::string fname, const Matrix m) {
-  std::ofstream out(fname.c_str());
-  out.precision(16);
-  for (int i = 0; i < m.dim[0]; ++i) {
-    for (int j = 0; j < m.dim[1]; ++j) {
-      const complex v = (*m.data)[i + (size_t)m.dim[0] * j];
-      out << std::real(v) << " " << std::imag(v) << " ";
+  std::ofstream re((fname + "_real").c_str());
+  std::ofstream im((fname + "_imag").c_str());
+  const int n = m.dim[0];
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) {
+      const complex v = (*m.data)[(std::size_t)j * n + i];
+      re << std::real(v) << " ";
+      im << std::imag(v) << " ";
     }
-    out << "\n";
+    re << std::endl;
+    im << std::endl;
   }
 }
 
+// Per element (geometry order), npoints samples at t = j / npoints: the point
+// Map(t), then for every column of m the real parts, then the imaginary
+// parts, of sum_u m(u, col) phi_u.  The basis argument is the integer
+// quotient j / npoints (0 for every sample), as in the reference's
+// (*base)(j/npoints).
 void WriteDensity(std::string name, const Matrix& m, pGeometry pgeom, int npoints) {
+  std::vector<pElement> el = pgeom->elements();
   std::shared_ptr<Geometry::flat_basis_map> fm = pgeom->FlatMap();
+  std::map<std::size_t, std::size_t> pos;  // element index() -> position
+  for (std::size_t e = 0; e < el.size(); ++e) pos[el[e]->index()] = e;
+  const int ncol = m.dim[1];
+  std::vector<std::vector<Point> > pts(el.size());
+  std::vector<std::vector<cvector> > val(el.size());
+  for (std::size_t u = 0; u < fm->size(); ++u) {
+    const pElement& elem = (*fm)[u].first;
+    const pBasis& base = (*fm)[u].second;
+    const std::size_t e = pos[elem->index()];
+    if (pts[e].empty()) {
+      for (int j = 0; j < npoints; ++j) pts[e].push_back(elem->Map((1.0 * j) / npoints));
+      val[e].assign(npoints, cvector(ncol));
+    }
+    for (int j = 0; j < npoints; ++j)
+      for (int c = 0; c < ncol; ++c)
+        val[e][j][c] += (*base)(j / npoints) * (*m.data)[(std::size_t)c * m.dim[0] + u];
+  }
   std::ofstream out(name.c_str());
-  out.precision(16);
-  std::vector<pElement>& el = pgeom->elements();
   for (std::size_t e = 0; e < el.size(); ++e)
-    for (int q = 0; q < npoints; ++q) {
-      const double t = npoints > 1 ? (double)q / (npoints - 1) : 0.5;
-      complex v = 0;
-      for (std::size_t u = 0; u < fm->size(); ++u)
-        if ((*fm)[u].first == el[e]) v += (*m.data)[u] * (*(*fm)[u].second)(t);
-      const Point p = el[e]->Map(t);
-      out << p.x << " " << p.y << " " << std::real(v) << " " << std::imag(v) << "\n";
+    for (int j = 0; j < npoints; ++j) {
+      out << pts[e][j].x << " " << pts[e][j].y << " ";
+      for (int c = 0; c < ncol; ++c) out << std::real(val[e][j][c]) << " ";
+      for (int c = 0; c < ncol; ++c) out << std::imag(val[e][j][c]) << " ";
+      out << std::endl;
     }
 }
 
+// Map(j / npoints), j < npoints, for every element in geometry order
 void WriteDomain(std::string name, pGeometry pgeom, int npoints) {
+  std::vector<pElement> el = pgeom->elements();
   std::ofstream out(name.c_str());
-  for (const pElement& e : pgeom->elements()) {
-    for (int q = 0; q < npoints; ++q) {
-      const Point p = e->Map(npoints > 1 ? (double)q / (npoints - 1) : 0.5);
-      out << p.x << " " << p.y << "\n";
+  for (std::size_t e = 0; e < el.size(); ++e)
+    for (int j = 0; j < npoints; ++j) {
+      const Point p = el[e]->Map((1.0 * j) / npoints);
+      out << p.x << " " << p.y << std::endl;
     }
-    out << "\n";
-  }
 }
 
 pdvector OutputHandler::RealData(const cvector& vals) {
@@ -88,16 +133,22 @@ pdvector OutputHandler::TurnToRealImag(const cvector& vals) { return real_ ? Rea
 
 GplotOutput::GplotOutput(int xpts, int ypts, double ax, double bx, double ay, double by, std::string name)
     : name_(name), xpts_(xpts), ypts_(ypts) {
+  set_real(true);
+  isroot_ = true;
   mesh_ = *MeshGrid(ax, bx, ay, by, xpts, ypts);
 }
 
-void GplotOutput::Write(const std::string& field, const cvector& vals) {
-  GplotOut(name_ + "_" + field + "_real", mesh_, *RealData(vals), xpts_, ypts_);
-  GplotOut(name_ + "_" + field + "_imag", mesh_, *ImagData(vals), xpts_, ypts_);
+// <name>inc, <name>scatt, <name>full: the real (set_real(true), the default)
+// or imaginary parts on the mesh
+void GplotOutput::WriteIncident(const cvector& vals) {
+  GplotOut(name_ + "inc", mesh_, *TurnToRealImag(vals), xpts_, ypts_);
 }
-void GplotOutput::WriteIncident(const cvector& vals) { Write("incident", vals); }
-void GplotOutput::WriteScattered(const cvector& vals) { Write("scattered", vals); }
-void GplotOutput::WriteFull(const cvector& vals) { Write("full", vals); }
+void GplotOutput::WriteScattered(const cvector& vals) {
+  GplotOut(name_ + "scatt", mesh_, *TurnToRealImag(vals), xpts_, ypts_);
+}
+void GplotOutput::WriteFull(const cvector& vals) {
+  GplotOut(name_ + "full", mesh_, *TurnToRealImag(vals), xpts_, ypts_);
+}
 void GplotOutput::WriteAll(const cvector& a, const cvector& b, const cvector& c) {
   WriteIncident(a);
   WriteScattered(b);

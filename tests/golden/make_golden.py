@@ -8,7 +8,11 @@ Small cases keep full matrices.  Larger ones keep size-independent probes:
 A @ v and A^H @ w for seeded vectors, the diagonal, 4096 seeded entries, the
 right-hand side, the solution and the norm / condition number.
 
-Run from the repository root:  python tests/golden/make_golden.py
+The text output formats: oracle/_ref/ref_output (tests/native/api_output.cpp
+linked to the reference library) writes its files into tests/golden/output.
+
+Run from the repository root, with the reference checkout named:
+    BEM2D_REFERENCE=<checkout> python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -27,6 +31,18 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 from golden.cases import CASES, QUAD  # noqa: E402
 
 REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+REF_OUTPUT = os.path.join(ROOT, "oracle", "_ref", "ref_output")
+
+
+def output_files():
+    """The reference library's text output files (api_output.cpp) into
+    tests/golden/output, replacing what is there."""
+    out = os.path.join(ROOT, "tests", "golden", "output")
+    os.makedirs(out, exist_ok=True)
+    for f in os.listdir(out):
+        os.remove(os.path.join(out, f))
+    subprocess.run([REF_OUTPUT], check=True, cwd=out)
+    return sorted(os.listdir(out))
 
 
 def probes(A, seed):
@@ -129,10 +145,16 @@ def hankel_fixture():
 
 def main():
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref"],
+    ref = os.environ.get("BEM2D_REFERENCE", "")
+    if not ref:
+        raise SystemExit("set BEM2D_REFERENCE to the reference checkout")
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j8", "ref", "REF=" + ref],
                    check=True, stdout=subprocess.DEVNULL)
-    names = sys.argv[1:] or (list(CASES) + ["hankel_ck"])
+    names = sys.argv[1:] or (list(CASES) + ["hankel_ck", "output"])
     for name in names:
+        if name == "output":
+            print("output files:", " ".join(output_files()))
+            continue
         if name == "hankel_ck":
             path = os.path.join(ROOT, "tests", "golden", "hankel_ck.npz")
             np.savez_compressed(path, **hankel_fixture())

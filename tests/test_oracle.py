@@ -60,13 +60,25 @@ def test_port_matches_reference(name):
             assert rel(A[z["sample_i"], z["sample_j"]], z["sample"]) < TOL_MAT
             assert rel(np.diag(A), z["diag"]) < TOL_MAT
         x = O.solve(A, b)
-        # the graded L-shape is ill-conditioned (element sizes down to 0.15^8);
-        # with Im k < 0 the kernel grows and cond(A) reaches 7e4 (kite_ck):
-        # solutions and sigma_min then move by about cond(A) times the
-        # matrix difference
-        dA = rel(A, z["A"]) if "A" in z else 1e-15
-        tol = max(1e-8 if name == "lshape_graded" else 1e-11,
-                  10 * np.linalg.cond(z["A"]) * dA if "A" in z else 0.0)
+        # Both solutions are LAPACK's, of slightly different systems: the
+        # difference is bounded by 2 cond(A) (eA + eb + be + be_ref) (first
+        # order; the graded L-shape has element sizes down to 0.15^8 and cond
+        # ~1e6, kite_ck's kernel grows with Im k < 0, cond 7e4).  eA is the
+        # 2-norm-relative matrix difference, from the full reference matrix
+        # where the fixture holds it, else estimated from the probe product
+        # (|dA v| ~ |dA|_F |v| / sqrt(n) for a random v, times 10).
+        s = np.linalg.svd(A, compute_uv=False)
+        n = A.shape[0]
+        if "A" in z:
+            eA = np.linalg.norm(A - z["A"]) / s[0]
+        else:
+            pv = z["probe_v"]
+            eA = 10 * np.sqrt(n) * np.linalg.norm(A @ pv - z["Av"]) / (np.linalg.norm(pv) * s[0])
+        nb = np.linalg.norm(b)
+        eb = np.linalg.norm(b - z["rhs"]) / nb
+        be = np.linalg.norm(b - A @ x) / (s[0] * np.linalg.norm(x) + nb)
+        be_ref = np.linalg.norm(b - A @ z["x"]) / (s[0] * np.linalg.norm(z["x"]) + nb)
+        tol = 2 * (s[0] / s[-1]) * (eA + eb + be + be_ref) + 1e-15
         assert rel(x, z["x"]) < tol
         nrm, cond = O.norm_cond(O.change_basis(A, M))
         assert abs(nrm - z["normcond"][0]) < 1e-12 * nrm
