@@ -30,10 +30,12 @@ EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",
            "bem2d_eval_ident",
            "bem2d_dot_prod_basfuns", "bem2d_solve_system", "bem2d_scattering_solve",
            "bem2d_fma_peak", "bem2d_ctx_enable_timers", "bem2d_ctx_timer",
-           "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_num_range",
+           "bem2d_change_basis", "bem2d_l2_norm_cond", "bem2d_l2_norm_cond_prec",
+           "bem2d_num_range",
            "bem2d_eval_kernel", "bem2d_solve_system_noalloc",
            "bem2d_sweep_solve", "bem2d_hermitian_eigenvalues", "bem2d_singular_values",
-           "bem2d_eigenvalues"]
+           "bem2d_eigenvalues", "bem2d_debug_panel_timeout", "bem2d_noalloc_scratch_fits",
+           "bem2d_debug_tc_update", "bem2d_matmul", "bem2d_eigenvectors"]
 
 NOALLOC_MAX_N = 1024  # BEM2D_NOALLOC_MAX_N
 
@@ -108,6 +110,13 @@ def load():
         lib.bem2d_hermitian_eigenvalues.argtypes = [vp, i32, vp, i64, vp]
         lib.bem2d_singular_values.argtypes = [vp, i32, vp, i64, vp]
         lib.bem2d_eigenvalues.argtypes = [vp, i32, vp, i64, vp]
+        lib.bem2d_l2_norm_cond_prec.argtypes = [vp, i32, vp, i64, d, i32, ctypes.POINTER(d),
+                                                ctypes.POINTER(d)]
+        lib.bem2d_debug_panel_timeout.argtypes = [vp, i32, i32]
+        lib.bem2d_noalloc_scratch_fits.argtypes = [ctypes.POINTER(i64), ctypes.POINTER(i64)]
+        lib.bem2d_debug_tc_update.argtypes = [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64]
+        lib.bem2d_matmul.argtypes = [vp, i32, i32, i32, vp, i64, vp, i64, vp, i64]
+        lib.bem2d_eigenvectors.argtypes = [vp, i32, vp, i64, vp, vp, i64]
         lib.bem2d_ctx_enable_timers.argtypes = [vp, i32]
         lib.bem2d_ctx_timer.argtypes = [vp, i32, ctypes.POINTER(d), ctypes.POINTER(i64)]
         _LIB = lib
@@ -120,6 +129,19 @@ def _ld(a, n):
     if hasattr(a, "stride"):
         return a.stride(1) if a.stride(0) == 1 else a.stride(0)
     return n
+
+
+def _sync_producers(*objs):
+    """The library orders its work on the context's stream.  torch CUDA
+    tensors handed to it (inputs, or outputs torch has just allocated and
+    filled) are written on torch's stream: wait for that stream first."""
+    for o in objs:
+        if isinstance(o, (list, tuple)):
+            o = o[0] if o else None
+        if getattr(o, "is_cuda", False):
+            import torch
+            torch.cuda.current_stream().synchronize()
+            return
 
 
 def _ptr(a):
@@ -206,6 +228,7 @@ class Context:
     # -- assembly ----------------------------------------------------------
     def discrete_kernel(self, g, kernel="combined", k=10.0, eta=None, q=(3, 5, 0.15),
                         alpha=1.0, beta=0.0, out=None):
+        _sync_producers(out)
         gh = _GeomHold(g)
         n = gh.n
         if out is None:
@@ -224,6 +247,7 @@ class Context:
                               alpha=1.0, beta=0.0, out=None, out32=None):
         """Mixed-precision assembly: (complex128, complex64) matrices (host
         numpy by default, or the given torch CUDA tensors)."""
+        _sync_producers(out, out32)
         gh = _GeomHold(g)
         n = gh.n
         if out is None:
@@ -239,6 +263,7 @@ class Context:
         return out, out32
 
     def eval_ident(self, g, q=(3, 5, 0.15), out=None):
+        _sync_producers(out)
         gh = _GeomHold(g)
         n = gh.n
         if out is None:
@@ -250,6 +275,7 @@ class Context:
 
     def rhs(self, g, k, direction, eta=None, q=(3, 5, 0.15), fun="combinedplanewave",
             scale=2.0, out=None):
+        _sync_producers(out)
         gh = _GeomHold(g)
         if out is None:
             out = np.zeros(gh.n, dtype=np.complex128)
@@ -262,6 +288,7 @@ class Context:
 
     # -- solve -------------------------------------------------------------
     def solve(self, A, b, precision="fp64", tol=0.0, out=None):
+        _sync_producers(A, b, out)
         n = A.shape[0]
         if out is None:
             out = np.zeros(n, dtype=np.complex128)
@@ -280,6 +307,7 @@ class Context:
     def solve_noalloc(self, A, b, out=None):
         """FP64 solve through bem2d_solve_system_noalloc (no device allocation,
         n <= NOALLOC_MAX_N)."""
+        _sync_producers(A, b, out)
         n = A.shape[0]
         if out is None:
             out = np.zeros(n, dtype=np.complex128)
@@ -295,9 +323,43 @@ class Context:
         self.last_info = (info.info, info.iterations, info.residual)
         return out
 
+    def debug_panel_timeout(self, n=512, polls=64):
+        """Return code of bem2d_debug_panel_timeout (BEM2D_ERR_TIMEOUT = -6
+        expected) and the context's message."""
+        rc = self.lib.bem2d_debug_panel_timeout(self.h, int(n), int(polls))
+        return rc, self.lib.bem2d_ctx_last_error(self.h).decode()
+
+    def matmul(self, A, B, out=None):
+        """A @ B (complex128) through bem2d_matmul; numpy in, numpy out, or
+        column-major torch CUDA views."""
+        _sync_producers(A, B, out)
+        m, k = A.shape
+        n = B.shape[1]
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
+        if isinstance(B, np.ndarray):
+            B = np.asfortranarray(B, dtype=np.complex128)
+        if out is None:
+            out = np.zeros((m, n), dtype=np.complex128, order="F")
+        self._check(self.lib.bem2d_matmul(self.h, m, n, k, _ptr(A), _ld(A, m), _ptr(B), _ld(B, k),
+                                          _ptr(out), _ld(out, m)))
+        return out
+
+    def tc_update(self, C, A, B):
+        """C -= A B in place on complex64 torch CUDA tensors holding
+        column-major matrices (column-major views, as x.t() of a row-major
+        tensor) through bem2d_debug_tc_update."""
+        _sync_producers(C, A, B)
+        M, N = C.shape
+        K = A.shape[1]
+        self._check(self.lib.bem2d_debug_tc_update(self.h, M, N, K, _ptr(C), _ld(C, M), _ptr(A),
+                                                   _ld(A, M), _ptr(B), _ld(B, K)))
+        return C
+
     # -- dense operators ---------------------------------------------------
     def change_basis(self, K, M, bstart, out=None):
         """U^{-H} K U^{-1} with M = U^H U block diagonal (blocks at bstart)."""
+        _sync_producers(K, M, out)
         n = K.shape[0]
         if isinstance(K, np.ndarray):
             K = np.asfortranarray(K, dtype=np.complex128)
@@ -311,18 +373,27 @@ class Context:
                                                 _ld(out, n)))
         return out
 
-    def norm_cond(self, A, tol=0.0):
-        """(sigma_max, sigma_max / sigma_min) of A."""
+    def norm_cond(self, A, tol=0.0, precision=None):
+        """(sigma_max, sigma_max / sigma_min) of A; precision None:
+        bem2d_l2_norm_cond, else bem2d_l2_norm_cond_prec with "fp64" or
+        "mixed" (complex64 LU + FP64 refinement for sigma_min)."""
+        _sync_producers(A)
         n = A.shape[0]
         if isinstance(A, np.ndarray):
             A = np.asfortranarray(A, dtype=np.complex128)
         nrm, cond = ctypes.c_double(), ctypes.c_double()
-        self._check(self.lib.bem2d_l2_norm_cond(self.h, n, _ptr(A), _ld(A, n), float(tol),
-                                                ctypes.byref(nrm), ctypes.byref(cond)))
+        if precision is None:
+            self._check(self.lib.bem2d_l2_norm_cond(self.h, n, _ptr(A), _ld(A, n), float(tol),
+                                                    ctypes.byref(nrm), ctypes.byref(cond)))
+        else:
+            self._check(self.lib.bem2d_l2_norm_cond_prec(
+                self.h, n, _ptr(A), _ld(A, n), float(tol), PREC[precision],
+                ctypes.byref(nrm), ctypes.byref(cond)))
         return nrm.value, cond.value
 
     def num_range_lmax(self, A, thetas, tol=0.0, precision="fp64"):
         """lambda_max of (e^{i th} A + e^{-i th} A^H)/2 for each angle."""
+        _sync_producers(A)
         n = A.shape[0]
         if isinstance(A, np.ndarray):
             A = np.asfortranarray(A, dtype=np.complex128)
@@ -335,6 +406,7 @@ class Context:
     def hermitian_eigenvalues(self, A):
         """Eigenvalues (ascending) of the Hermitian matrix A's upper triangle
         defines (HermitianEigenvalues)."""
+        _sync_producers(A)
         n = A.shape[0]
         if isinstance(A, np.ndarray):
             A = np.asfortranarray(A, dtype=np.complex128)
@@ -345,6 +417,7 @@ class Context:
 
     def singular_values(self, A):
         """Singular values of A, descending (SingularValues)."""
+        _sync_producers(A)
         n = A.shape[0]
         if isinstance(A, np.ndarray):
             A = np.asfortranarray(A, dtype=np.complex128)
@@ -354,12 +427,26 @@ class Context:
 
     def eigenvalues(self, A):
         """Eigenvalues of the general complex A (Eigenvalues, zgeev)."""
+        _sync_producers(A)
         n = A.shape[0]
         if isinstance(A, np.ndarray):
             A = np.asfortranarray(A, dtype=np.complex128)
         out = np.zeros(n, dtype=np.complex128)
         self._check(self.lib.bem2d_eigenvalues(self.h, n, _ptr(A), _ld(A, n), _ptr(out)))
         return out
+
+    def eigenvectors(self, A):
+        """(eigenvalues, right eigenvectors as columns) of the general complex
+        A (Eigenvalues with eigenvectors, zgeev 'V')."""
+        _sync_producers(A)
+        n = A.shape[0]
+        if isinstance(A, np.ndarray):
+            A = np.asfortranarray(A, dtype=np.complex128)
+        w = np.zeros(n, dtype=np.complex128)
+        V = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._check(self.lib.bem2d_eigenvectors(self.h, n, _ptr(A), _ld(A, n), _ptr(w), _ptr(V),
+                                                n))
+        return w, V
 
     def potential(self, g, coeffs, points, kernel="single", k=10.0, eta=0.0, q=(3, 5, 0.15)):
         """sum_u c_u int K(p, y) phi_u(y) ds(y) at the points (EvalKernel)."""
@@ -376,6 +463,7 @@ class Context:
 
     def scattering_solve(self, g, k, direction, eta=None, q=(3, 5, 0.15), precision="fp64",
                          tol=0.0, out=None):
+        _sync_producers(out)
         gh = _GeomHold(g)
         if out is None:
             out = np.zeros(gh.n, dtype=np.complex128)
@@ -393,6 +481,7 @@ class Context:
                     tol=0.0, nworkers=0, outs=None):
         """Batched bem2d_sweep_solve over (geoms[i], ks[i]); returns the list of
         solutions (numpy, or the given `outs`, which may be CUDA tensors)."""
+        _sync_producers(outs)
         nk = len(geoms)
         holds = [g if isinstance(g, _GeomHold) else _GeomHold(g) for g in geoms]
         garr = (Geometry_c * max(nk, 1))(*[h.c for h in holds])
@@ -420,6 +509,14 @@ def gauss(n):
     if rc:
         raise Bem2dError(rc, "bem2d_gauss")
     return x, w
+
+
+def noalloc_scratch_fits():
+    """(fits, bytes needed at BEM2D_NOALLOC_MAX_N, bytes of the static array)."""
+    lib = load()
+    t, cap = ctypes.c_int64(), ctypes.c_int64()
+    ok = lib.bem2d_noalloc_scratch_fits(ctypes.byref(t), ctypes.byref(cap))
+    return bool(ok), t.value, cap.value
 
 
 def fma_peak(precision="fp64"):

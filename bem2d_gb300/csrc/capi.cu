@@ -12,6 +12,7 @@
 #include <map>
 #include <string>
 #include <unordered_map>
+#include <functional>
 #include <vector>
 
 #include "common.cuh"
@@ -571,6 +572,37 @@ static int with_matrix_out(bem2d_ctx* c, void* out, long long ld, int n, F fill)
   return BEM2D_OK;
 }
 
+// Non-finite guard of the assembly: nf_clear() before an assembly, nf_scan()
+// of each output, nf_check() after a synchronisation of the stream.
+static int* nf_flag(bem2d_ctx* c, int* rc) {
+  return static_cast<int*>(ws(c, "nf_flag", 256, rc));
+}
+static int nf_clear(bem2d_ctx* c) {
+  int rc = 0;
+  int* f = nf_flag(c, &rc);
+  if (!f) return rc;
+  CUDA_TRY(c, cudaMemsetAsync(f, 0, sizeof(int), c->stream));
+  return BEM2D_OK;
+}
+static int nf_scan(bem2d_ctx* c, const double2* A, long long ld, int rows, int cols) {
+  int rc = 0;
+  int* f = nf_flag(c, &rc);
+  if (!f) return rc;
+  launch_nonfinite_scan(A, ld, rows, cols, f, c->stream);
+  ++c->launches;
+  return BEM2D_OK;
+}
+static int nf_check(bem2d_ctx* c, const char* what) {
+  int rc = 0;
+  int* f = nf_flag(c, &rc);
+  if (!f) return rc;
+  int h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, f, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h) return fail(c, BEM2D_ERR_NONFINITE, "non-finite entry in the assembled %s", what);
+  return BEM2D_OK;
+}
+
 }  // namespace bem2d_gpu
 
 using namespace bem2d_gpu;
@@ -667,9 +699,12 @@ int bem2d_discrete_kernel(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_
   cudaSetDevice(c->device);
   Staged st;
   if ((rc = stage(c, geom, quad, true, true, &st))) return rc;
-  return with_matrix_out(c, out, ld, geom->n_unk, [&](double2* A, long long lda) {
-    return assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, lda, k_im);
+  if ((rc = nf_clear(c))) return rc;
+  rc = with_matrix_out(c, out, ld, geom->n_unk, [&](double2* A, long long lda) {
+    int r = assemble_dev(c, st, kernel, k_re, eta, alpha, beta, A, lda, k_im);
+    return r ? r : nf_scan(c, A, lda, geom->n_unk, geom->n_unk);
   });
+  return rc ? rc : nf_check(c, "matrix");
 }
 
 int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
@@ -696,6 +731,7 @@ int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
                   : static_cast<float2*>(ws(c, "out32", sizeof(float2) * (size_t)n * n, &rc));
   if (!B) return rc;
   const long long la = d64 ? ld : n, lb = d32 ? ld32 : n;
+  if ((rc = nf_clear(c))) return rc;
   if (k_im != 0.0) {
     // complex wavenumber: FP64 assembly (complex-argument Hankel functions),
     // then its complex64 rounding
@@ -706,6 +742,7 @@ int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
   } else if ((rc = assemble_mixed_dev(c, st, kernel, k_re, eta, alpha, beta, A, la, B, lb))) {
     return rc;
   }
+  if ((rc = nf_scan(c, A, la, n, n))) return rc;
   if (!d64)
     CUDA_TRY(c, cudaMemcpy2DAsync(out, sizeof(double2) * ld, A, sizeof(double2) * n,
                                   sizeof(double2) * n, n, cudaMemcpyDeviceToHost, c->stream));
@@ -714,7 +751,7 @@ int bem2d_discrete_kernel_mixed(bem2d_ctx* c, const bem2d_geometry* geom,
                                   sizeof(float2) * n, n, cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   resolve_timers(c);
-  return BEM2D_OK;
+  return nf_check(c, "matrix");
 }
 
 int bem2d_eval_ident(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d_quad* quad,
@@ -1003,6 +1040,7 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   const bool mixed = precision == BEM2D_PREC_MIXED;
   // complex wavenumbers: FP64 assembly; the mixed solver converts A itself
   const bool mixed_asm = mixed && k_im == 0.0;
+  if ((rc = nf_clear(c))) return rc;
   if (mixed_asm) {
     float2* A32 = static_cast<float2*>(ws(c, "lu32", sizeof(float2) * (size_t)n * n, &rc));
     if (!A32) return rc;
@@ -1015,6 +1053,9 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
              c->stream, k_im);
   ++c->launches;
   CHECK_LAUNCH(c);
+  // NaN or Inf in A or b (a degenerate element, say) would otherwise reach
+  // the caller as a zero pivot or a non-finite solution
+  if ((rc = nf_scan(c, A, n, n, n)) || (rc = nf_scan(c, b, n, n, 1))) return rc;
   const bool xdev = is_device_ptr(x);
   double2* dx = xdev ? static_cast<double2*>(x)
                      : static_cast<double2*>(ws(c, "out_x", sizeof(double2) * n, &rc));
@@ -1024,7 +1065,11 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   // assembly grids; the next call's assembly waits for this phase.
   PhaseStream ps(c);
   if ((rc = ps.begin())) return rc;
-  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info, mixed_asm))) return rc;
+  if ((rc = solve_dev(c, n, A, n, b, dx, precision, tol, info, mixed_asm))) {
+    const int nf = nf_check(c, "matrix or right-hand side");
+    return nf ? nf : rc;
+  }
+  if ((rc = nf_check(c, "matrix or right-hand side"))) return rc;
   if (!xdev) {
     CUDA_TRY(c, cudaMemcpyAsync(x, dx, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1334,9 +1379,14 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
 // Largest singular value of an operator given y = op(x) and y = op^H(x), by
 // Golub-Kahan-Lanczos bidiagonalisation with two-pass Gram-Schmidt
 // reorthogonalisation of both bases.
+// sigma_max of the operator `op` (adjoint `oph`) by Golub-Kahan-Lanczos
+// with full reorthogonalisation, until the estimate changes by less than
+// tol (relative) twice.  v0: start vector (device, need not be normalised;
+// null: the deterministic default); ritz: if not null, receives the unit
+// right Ritz vector of the final estimate (device, n entries).
 template <typename Op, typename OpH>
 static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const char* tag,
-                        double* sigma) {
+                        double* sigma, const double2* v0 = nullptr, double2* ritz = nullptr) {
   int rc = 0;
   const int mmax = std::min(n, 300);
   double2* V = static_cast<double2*>(ws(c, (std::string(tag) + "V").c_str(),
@@ -1346,8 +1396,13 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
   double2* h = static_cast<double2*>(ws(c, "gk_h", sizeof(double2) * (mmax + 2), &rc));
   double* nrm = static_cast<double*>(ws(c, "gk_nrm", sizeof(double) * 4, &rc));
   if (!V || !U || !h || !nrm) return rc;
-  const std::vector<std::complex<double>> v0 = start_vector(n);
-  CUDA_TRY(c, cudaMemcpyAsync(V, v0.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+  if (v0) {
+    CUDA_TRY(c, cudaMemcpyAsync(V, v0, sizeof(double2) * n, cudaMemcpyDeviceToDevice, c->stream));
+  } else {
+    const std::vector<std::complex<double>> sv = start_vector(n);
+    CUDA_TRY(c, cudaMemcpyAsync(V, sv.data(), sizeof(double2) * n, cudaMemcpyHostToDevice,
+                                c->stream));
+  }
   std::vector<double> alpha, beta;
   auto norm_of = [&](double2* w, double* out) -> int {
     launch_batched_norm2(n, w, n, nrm, 1, c->stream);
@@ -1368,6 +1423,12 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
     launch_batched_scale(n, w, 0, nrm + 2, w, 0, 1, c->stream);
     return BEM2D_OK;
   };
+  if (v0) {  // normalise the given start vector
+    double a0 = 0;
+    if ((rc = norm_of(V, &a0))) return rc;
+    if (!(a0 > 0) || !std::isfinite(a0)) return fail(c, BEM2D_ERR_NONFINITE, "bad start vector");
+    if ((rc = normalize(V, a0))) return rc;
+  }
   // u_0 = op(v_0) / alpha_0
   if ((rc = op(V, U))) return rc;
   double a = 0;
@@ -1417,6 +1478,30 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
     prev = sig;
   }
   *sigma = sig;
+  if (ritz) {
+    // right Ritz vector V y, y the top eigenvector of B^T B (the
+    // tridiagonal of the last step), over the k vectors v_0 .. v_{k-1}
+    const int k = (int)alpha.size();
+    std::vector<double> d(k), e(k > 1 ? k - 1 : 0);
+    for (int i = 0; i < k; ++i) {
+      d[i] = alpha[i] * alpha[i] + (i > 0 ? beta[i - 1] * beta[i - 1] : 0.0);
+      if (i + 1 < k) e[i] = alpha[i] * beta[i];
+    }
+    const std::vector<double> y = tridiag_eigenvector(d, e, sig * sig);
+    std::vector<std::complex<double>> yc(k);
+    for (int i = 0; i < k; ++i) yc[i] = y[i];
+    double2* yd = static_cast<double2*>(ws(c, "gk_y", sizeof(double2) * (mmax + 2), &rc));
+    if (!yd) return rc;
+    CUDA_TRY(c, cudaMemcpyAsync(yd, yc.data(), sizeof(double2) * k, cudaMemcpyHostToDevice,
+                                c->stream));
+    launch_zgemm_rect(V, n, n, k, yd, k, 1, ritz, n, c->stream);
+    ++c->launches;
+    double rn = 0;
+    if ((rc = norm_of(ritz, &rn))) return rc;
+    if (!(rn > 0)) return fail(c, BEM2D_ERR_NONFINITE, "zero Ritz vector");
+    if ((rc = normalize(ritz, rn))) return rc;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // host vectors above are freed on return
+  }
   return BEM2D_OK;
 }
 
@@ -1508,8 +1593,15 @@ int bem2d_change_basis(bem2d_ctx* c, int n, const void* K, int64_t ldk, const vo
 
 int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double tol, double* norm,
                        double* cond) {
+  return bem2d_l2_norm_cond_prec(c, n, A, lda, tol, BEM2D_PREC_FP64, norm, cond);
+}
+
+int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, double tol,
+                            int precision, double* norm, double* cond) {
   if (!c) return BEM2D_ERR_ARG;
   if (n < 1 || !A || !norm || !cond || lda < n) return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (precision != BEM2D_PREC_FP64 && precision != BEM2D_PREC_MIXED)
+    return fail(c, BEM2D_ERR_ARG, "unknown precision %d", precision);
   if (!(tol > 0)) tol = 1e-13;
   cudaSetDevice(c->device);
   int rc = 0;
@@ -1530,7 +1622,10 @@ int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double t
   };
   double smax = 0, inv_smin = 0;
   if ((rc = gk_sigma_max(c, n, op, oph, tol, "gka", &smax))) return rc;
-  // sigma_min = 1 / sigma_max(A^{-1}) through a complex128 LU
+  // sigma_min = 1 / sigma_max(A^{-1}): complex128 LU, or complex64 LU with
+  // FP64 refinement of every product with A^{-1} / A^{-H}
+  const bool mixed = precision == BEM2D_PREC_MIXED;
+  const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
   LuWork w;
   int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
   if (!ints) return rc;
@@ -1539,15 +1634,24 @@ int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double t
   w.status = ints + 1;
   w.scratch_bytes = lu_scratch_bytes(n);
   w.scratch = ws(c, "lu_scratch", w.scratch_bytes, &rc);
-  char* aux = static_cast<char*>(ws(c, "lu_aux", lu_aux_bytes(n, sizeof(double2)), &rc));
-  double2* LU = static_cast<double2*>(ws(c, "lu64", sizeof(double2) * (size_t)n * n, &rc));
+  char* aux = static_cast<char*>(ws(c, "lu_aux", lu_aux_bytes(n, esz), &rc));
+  void* LU = ws(c, mixed ? "lu32" : "lu64", esz * (size_t)n * n, &rc);
   if (!w.scratch || !aux || !LU) return rc;
   w.dinv = aux;
-  w.perm = reinterpret_cast<int*>(aux + (lu_aux_bytes(n, sizeof(double2)) - 256 - sizeof(int) * (size_t)n));
-  CUDA_TRY(c, cudaMemcpy2DAsync(LU, sizeof(double2) * n, dA, sizeof(double2) * la, sizeof(double2) * n,
-                                n, cudaMemcpyDeviceToDevice, c->stream));
-  if ((rc = lu_factor<double2>(LU, n, n, w, c->stream, &c->launches)))
-    return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+  w.perm = reinterpret_cast<int*>(aux + (lu_aux_bytes(n, esz) - 256 - sizeof(int) * (size_t)n));
+  if (mixed) {
+    w.pack_bytes = lu_pack_bytes(n);
+    w.pack = ws(c, "lu_pack", w.pack_bytes, &rc);
+    if (!w.pack) return rc;
+    launch_to_c64(dA, la, static_cast<float2*>(LU), n, n, n, c->stream);
+    ++c->launches;
+    rc = lu_factor<float2>(static_cast<float2*>(LU), n, n, w, c->stream, &c->launches);
+  } else {
+    CUDA_TRY(c, cudaMemcpy2DAsync(LU, sizeof(double2) * n, dA, sizeof(double2) * la,
+                                  sizeof(double2) * n, n, cudaMemcpyDeviceToDevice, c->stream));
+    rc = lu_factor<double2>(static_cast<double2*>(LU), n, n, w, c->stream, &c->launches);
+  }
+  if (rc) return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
   int hinfo[2];
   CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
@@ -1560,17 +1664,190 @@ int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double t
   }
   double2* tmp = static_cast<double2*>(ws(c, "nc_tmp", sizeof(double2) * n, &rc));
   if (!tmp) return rc;
-  auto iop = [&](const double2* x, double2* y) -> int {
-    int r = lu_solve<double2>(LU, n, n, w, x, y, c->stream, &c->launches);
-    return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+  if (!mixed) {
+    double2* LU64 = static_cast<double2*>(LU);
+    auto iop = [&, LU64](const double2* x, double2* y) -> int {
+      int r = lu_solve<double2>(LU64, n, n, w, x, y, c->stream, &c->launches);
+      return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+    };
+    auto ioph = [&, LU64](const double2* x, double2* y) -> int {
+      int r = lu_solve_h<double2>(LU64, n, n, w, x, y, c->stream, &c->launches);
+      return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+    };
+    if ((rc = gk_sigma_max(c, n, iop, ioph, tol, "gkb", &inv_smin))) return rc;
+    *norm = smax;
+    *cond = smax * inv_smin;
+    return BEM2D_OK;
+  }
+  float2* LU32 = static_cast<float2*>(LU);
+  double2* r = static_cast<double2*>(ws(c, "nc_r", sizeof(double2) * n, &rc));
+  float2* d = static_cast<float2*>(ws(c, "nc_d", 2 * sizeof(float2) * n, &rc));
+  double2* rpart = static_cast<double2*>(ws(c, "ir_part", residual_part_bytes(n), &rc));
+  double* red = static_cast<double*>(ws(c, "ir_red", sumsq_part_bytes() + 64, &rc));
+  double2* v1 = static_cast<double2*>(ws(c, "nc_v1", sizeof(double2) * n, &rc));
+  if (!r || !d || !rpart || !red || !v1) return rc;
+  double* scal = red + sumsq_part_bytes() / sizeof(double);  // [0] |A|^2 [1] |x|^2 [2] |r|^2 [3] |y|^2
+  launch_sumsq(dA, la, n, n, red, scal, c->stream);
+  c->launches += 2;
+  double hA = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&hA, scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const double normA = std::sqrt(hA);
+  // y = op(A)^{-1} x: corrections from the complex64 factor, residuals
+  // x - op(A) y in FP64, until the backward error
+  // ||x - op(A) y|| / (||A||_F ||y|| + ||x||) is at FP64 roundoff (2e-16)
+  // or stops halving; at most 10 corrections
+  auto refine = [&](bool herm, const double2* x, double2* y) -> int {
+    CUDA_TRY(c, cudaMemsetAsync(y, 0, sizeof(double2) * n, c->stream));
+    CUDA_TRY(c, cudaMemcpyAsync(r, x, sizeof(double2) * n, cudaMemcpyDeviceToDevice, c->stream));
+    launch_sumsq(x, n, n, 1, red, scal + 1, c->stream);
+    c->launches += 2;
+    double hs[4];
+    CUDA_TRY(c, cudaMemcpyAsync(hs + 1, scal + 1, sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const double xnorm = std::sqrt(hs[1]);
+    double rnorm = xnorm, ynorm = 0.0, best = INFINITY;
+    for (int it = 0; it < 10; ++it) {
+      if (rnorm == 0.0 || rnorm <= 2.2e-16 * (normA * ynorm + xnorm)) break;
+      if (!(rnorm < 0.5 * best)) break;
+      best = rnorm;
+      launch_scale_to_c64(n, r, 1.0 / rnorm, d, c->stream);
+      int e = herm ? lu_solve_h<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches)
+                   : lu_solve<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches);
+      if (e) return fail(c, e, "triangular solve launch failed");
+      launch_axpy_c64(n, rnorm, d + n, y, c->stream);
+      if (herm) {
+        launch_mvh(dA, la, n, y, tmp, c->stream);
+        CUDA_TRY(c, cudaMemcpyAsync(r, x, sizeof(double2) * n, cudaMemcpyDeviceToDevice,
+                                    c->stream));
+        launch_axpy_real(n, 1.0, tmp, r, c->stream);
+      } else {
+        launch_residual(dA, la, n, y, x, r, rpart, c->stream);
+      }
+      launch_sumsq(r, n, n, 1, red, scal + 2, c->stream);
+      launch_sumsq(y, n, n, 1, red, scal + 3, c->stream);
+      c->launches += 8;
+      CUDA_TRY(c, cudaMemcpyAsync(hs + 2, scal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+      CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                                  c->stream));
+      CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+      if (hinfo[1]) return fail(c, BEM2D_ERR_TIMEOUT, "triangular solve wait timed out");
+      rnorm = std::sqrt(hs[2]);
+      ynorm = std::sqrt(hs[3]);
+      if (!std::isfinite(rnorm))
+        return fail(c, BEM2D_ERR_NONFINITE, "non-finite residual in a refined solve");
+    }
+    return BEM2D_OK;
   };
-  auto ioph = [&](const double2* x, double2* y) -> int {
-    int r = lu_solve_h<double2>(LU, n, n, w, x, y, c->stream, &c->launches);
-    return r ? fail(c, r, "triangular solve launch failed") : BEM2D_OK;
+  // phase 1: the same iteration with unrefined complex64 solves (an
+  // operator accurate to ~1e-7), until its estimate settles to 1e-10: its
+  // Ritz vector starts the refined phase, which then needs only a few steps
+  auto op32 = [&](bool herm, const double2* x, double2* y) -> int {
+    launch_scale_to_c64(n, x, 1.0, d, c->stream);
+    int e = herm ? lu_solve_h<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches)
+                 : lu_solve<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches);
+    if (e) return fail(c, e, "triangular solve launch failed");
+    launch_widen(n, d + n, n, y, n, 1, c->stream);
+    c->launches += 2;
+    return BEM2D_OK;
   };
-  if ((rc = gk_sigma_max(c, n, iop, ioph, tol, "gkb", &inv_smin))) return rc;
+  double s32 = 0;
+  if ((rc = gk_sigma_max(
+           c, n, [&](const double2* x, double2* y) { return op32(false, x, y); },
+           [&](const double2* x, double2* y) { return op32(true, x, y); }, 1e-10, "gkb", &s32,
+           nullptr, v1)))
+    return rc;
+  if ((rc = gk_sigma_max(
+           c, n, [&](const double2* x, double2* y) { return refine(false, x, y); },
+           [&](const double2* x, double2* y) { return refine(true, x, y); }, tol, "gkb",
+           &inv_smin, v1)))
+    return rc;
   *norm = smax;
   *cond = smax * inv_smin;
+  return BEM2D_OK;
+}
+
+int bem2d_matmul(bem2d_ctx* c, int m, int n, int k, const void* A, int64_t lda, const void* B,
+                 int64_t ldb, void* C, int64_t ldc) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (m < 1 || n < 1 || k < 1 || !A || !B || !C || lda < m || ldb < k || ldc < m)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments (m=%d n=%d k=%d)", m, n, k);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0, lb = 0;
+  const double2* dA = dev_in(c, A, m, k, lda, "mm_A", &la, &rc);
+  if (!dA) return rc;
+  const double2* dB = dev_in(c, B, k, n, ldb, "mm_B", &lb, &rc);
+  if (!dB) return rc;
+  const bool cdev = is_device_ptr(C);
+  double2* dC = cdev ? static_cast<double2*>(C)
+                     : static_cast<double2*>(ws(c, "mm_C", sizeof(double2) * (size_t)m * n, &rc));
+  if (!dC) return rc;
+  const long long lc = cdev ? ldc : m;
+  launch_zgemm_rect(dA, la, m, k, dB, lb, n, dC, lc, c->stream);
+  ++c->launches;
+  CHECK_LAUNCH(c);
+  if (!cdev)
+    CUDA_TRY(c, cudaMemcpy2DAsync(C, sizeof(double2) * ldc, dC, sizeof(double2) * m,
+                                  sizeof(double2) * m, n, cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return BEM2D_OK;
+}
+
+int bem2d_debug_panel_timeout(bem2d_ctx* c, int n, int polls) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 256 || n > 4096 || polls < 1)
+    return fail(c, BEM2D_ERR_ARG, "timeout probe: n in [256, 4096], polls >= 1");
+  cudaSetDevice(c->device);
+  int rc = 0;
+  int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
+  if (!ints) return rc;
+  LuWork w;
+  w.ipiv = ints + 8;
+  w.info = ints;
+  w.status = ints + 1;
+  w.scratch_bytes = lu_scratch_bytes(n);
+  w.scratch = ws(c, "lu_scratch", w.scratch_bytes, &rc);
+  float2* P = static_cast<float2*>(ws(c, "probe_panel", sizeof(float2) * (size_t)n * 64, &rc));
+  if (!w.scratch || !P) return rc;
+  CUDA_TRY(c, cudaMemsetAsync(P, 0, sizeof(float2) * (size_t)n * 64, c->stream));
+  if ((rc = lu_panel_timeout_probe(P, n, n, w, (unsigned)polls, c->stream)))
+    return fail(c, rc, "timeout probe launch: %s", cudaGetErrorString(cudaGetLastError()));
+  ++c->launches;
+  int h[2] = {0, 0};
+  CUDA_TRY(c, cudaMemcpyAsync(h, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h[1])
+    return fail(c, BEM2D_ERR_TIMEOUT, "panel wait gave up after %d polls on a slot never posted",
+                polls);
+  return BEM2D_OK;
+}
+
+int bem2d_debug_tc_update(bem2d_ctx* c, int M, int N, int K, void* C, int64_t ldc,
+                          const void* A, int64_t lda, const void* B, int64_t ldb) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (M < 1 || N < 1 || K < 1 || !C || !A || !B || ldc < M || lda < M || ldb < K)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (!is_device_ptr(C) || !is_device_ptr(A) || !is_device_ptr(B))
+    return fail(c, BEM2D_ERR_ARG, "the tensor-core update takes device pointers");
+  cudaSetDevice(c->device);
+  int rc = 0;
+  const size_t pb = tc_pack_bytes(M, N, K);
+  void* pack = ws(c, "dbg_pack", pb, &rc);
+  int* st = static_cast<int*>(ws(c, "dbg_status", 256, &rc));
+  if (!pack || !st) return rc;
+  CUDA_TRY(c, cudaMemsetAsync(st, 0, sizeof(int), c->stream));
+  if ((rc = launch_tc_cgemm_sub(static_cast<float2*>(C), ldc, static_cast<const float2*>(A), lda,
+                                static_cast<const float2*>(B), ldb, M, N, K, pack, pb, st,
+                                c->stream)))
+    return fail(c, rc, "tensor-core update launch: %s", cudaGetErrorString(cudaGetLastError()));
+  c->launches += 3;
+  int h = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, st, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h) return fail(c, BEM2D_ERR_TIMEOUT, "tensor-core update wait timed out");
   return BEM2D_OK;
 }
 
@@ -1729,6 +2006,55 @@ int bem2d_eigenvalues(bem2d_ctx* c, int n, const void* A, int64_t lda, void* w) 
   if (status)
     return fail(c, BEM2D_ERR_NOCONV, "QR iteration: %d eigenvalues not found within the limit",
                 status);
+  return BEM2D_OK;
+}
+
+int bem2d_eigenvectors(bem2d_ctx* c, int n, const void* A, int64_t lda, void* w, void* vr,
+                       int64_t ldvr) {
+  if (!c) return BEM2D_ERR_ARG;
+  if (n < 1 || !A || !w || !vr || lda < n || ldvr < n)
+    return fail(c, BEM2D_ERR_ARG, "bad arguments");
+  if (n > BEM2D_EIG_MAX_N)
+    return fail(c, BEM2D_ERR_ARG, "order %d above BEM2D_EIG_MAX_N = %d", n, BEM2D_EIG_MAX_N);
+  cudaSetDevice(c->device);
+  int rc = 0;
+  long long la = 0;
+  const double2* dA = dev_in(c, A, n, n, lda, "eig_in", &la, &rc);
+  if (!dA) return rc;
+  const size_t nn = sizeof(double2) * (size_t)n * n;
+  double2* H = static_cast<double2*>(ws(c, "eig_H", nn, &rc));
+  double2* Z = static_cast<double2*>(ws(c, "eig_Z", nn, &rc));
+  double2* Y = static_cast<double2*>(ws(c, "eig_Y", nn, &rc));
+  void* work = ws(c, "eig_work", eig_work_bytes(n), &rc);
+  if (!H || !Z || !Y || !work) return rc;
+  const bool wdev = is_device_ptr(w), vdev = is_device_ptr(vr) && ldvr == n;
+  double2* dw = wdev ? static_cast<double2*>(w)
+                     : static_cast<double2*>(ws(c, "eig_w", sizeof(double2) * n, &rc));
+  double2* X = vdev ? static_cast<double2*>(vr) : static_cast<double2*>(ws(c, "eig_X", nn, &rc));
+  if (!dw || !X) return rc;
+  CUDA_TRY(c, cudaMemcpy2DAsync(H, sizeof(double2) * n, dA, sizeof(double2) * la,
+                                sizeof(double2) * n, n, cudaMemcpyDeviceToDevice, c->stream));
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess ||
+      sms < 1)
+    sms = 1;
+  c->launches += launch_eigenvalues(H, n, work, dw, sms, c->stream, Z);
+  CHECK_LAUNCH(c);
+  int status = 0;
+  CUDA_TRY(c, cudaMemcpyAsync(&status, eig_status_ptr(work, n), sizeof(int),
+                              cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (status)
+    return fail(c, BEM2D_ERR_NOCONV, "QR iteration: %d eigenvalues not found within the limit",
+                status);
+  c->launches += launch_eigenvectors(H, Z, n, Y, X, c->stream);
+  CHECK_LAUNCH(c);
+  if (!wdev)
+    CUDA_TRY(c, cudaMemcpyAsync(w, dw, sizeof(double2) * n, cudaMemcpyDeviceToHost, c->stream));
+  if (!vdev)
+    CUDA_TRY(c, cudaMemcpy2DAsync(vr, sizeof(double2) * ldvr, X, sizeof(double2) * n,
+                                  sizeof(double2) * n, n, cudaMemcpyDefault, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return BEM2D_OK;
 }
 

@@ -445,6 +445,10 @@ size_t lu_pack_bytes(int n);
 template <typename T>
 int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
               long long* launches);
+// Bounded-wait check of the grid panel (lu.cu): one complex64 panel whose
+// waits never complete; gives up after `polls` polls and sets *w.status.
+int lu_panel_timeout_probe(float2* A, long long lda, int n, const LuWork& w, unsigned polls,
+                           cudaStream_t s);
 // x = A^{-1} b with the factor of lu_factor (b and x may alias).
 template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
@@ -476,6 +480,10 @@ void launch_axpy_c64(int n, double scale, const float2* d, double2* x, cudaStrea
 void launch_sumsq(const double2* A, long long ld, int rows, int cols, double* part,
                   double* out, cudaStream_t s);
 size_t sumsq_part_bytes();
+// *flag |= 1 if the rows x cols column-major block holds a NaN or an
+// infinity (the flag is not cleared here)
+void launch_nonfinite_scan(const double2* A, long long ld, int rows, int cols, int* flag,
+                           cudaStream_t s);
 
 // ---- launch interfaces (spectra.cu) ---------------------------------------
 // Work bytes of launch_tridiag_eigs for order N.
@@ -498,7 +506,14 @@ size_t eig_work_bytes(int n);
 // form and the QR iterates) into w (device, n complex128).  Returns the
 // number of kernels launched; eig_status_ptr(work, n) then holds 0 or the
 // number of eigenvalues not found within the iteration limit.
-long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms, cudaStream_t s);
+// Z (n x n, optional): if given, receives the Schur vectors (A on exit holds
+// the triangular Schur factor T).
+long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms, cudaStream_t s,
+                             double2* Z = nullptr);
+// Right eigenvectors X (n x n) from the Schur factor T and the Schur
+// vectors Z (Y: n x n scratch), normalised as zgeev does.
+long long launch_eigenvectors(const double2* T, const double2* Z, int n, double2* Y, double2* X,
+                              cudaStream_t s);
 int* eig_status_ptr(void* work, int n);
 
 }  // namespace bem2d_gpu

@@ -146,10 +146,12 @@ void launch_mvh(const double2* A, long long lda, int n, const double2* x, double
 // C + z * cz and zgemm_reduce_kernel adds the partials in a fixed order
 // (deterministic), so that narrow products (few Lanczos vectors) still
 // fill the GPU.  T = double2 (complex128) or float2 (complex64).
+// `rows` is the row count of op(A) and C (n for the square products).
 template <typename T, bool HERM, int BN>
 __global__ void __launch_bounds__(256)
 zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict__ B,
-             long long ldb, int m, T* __restrict__ C, long long ldc, int kchunk, long long cz) {
+             long long ldb, int m, T* __restrict__ C, long long ldc, int kchunk, long long cz,
+             int rows) {
   constexpr int TY = BN >= 16 ? 16 : BN, TX = 256 / TY, RA = 64 / TX, RB = BN / TY;
   __shared__ T As[16][64 + 1];
   __shared__ T Bs[16][BN + 1];
@@ -168,7 +170,7 @@ zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict_
       const int kk = v / 64, ii = v - kk * 64;
       const int i = i0 + ii, k = k0 + kk;
       T a = zero;
-      if (i < n && k < ke) {
+      if (i < rows && k < ke) {
         if (HERM) {
           const T t = A[(size_t)i * lda + k];  // (A^H)_{ik} = conj(A_{ki})
           a = CTraits<T>::make(t.x, -t.y);
@@ -205,7 +207,7 @@ zgemm_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict_
 #pragma unroll
     for (int a = 0; a < RA; ++a) {
       const int i = i0 + tx + TX * a;
-      if (i < n) Cz[(size_t)j * ldc + i] = acc[a][b];
+      if (i < rows) Cz[(size_t)j * ldc + i] = acc[a][b];
     }
   }
 }
@@ -236,6 +238,21 @@ static int zgemm_splits(int n, int m, int bn) {
 
 static int zgemm_bn(int m) { return m <= 4 ? 4 : (m <= 16 ? 16 : 64); }
 
+// C (rows x m) = A (rows x k) B (k x m), complex128, no K split
+void launch_zgemm_rect(const double2* A, long long lda, int rows, int k, const double2* B,
+                       long long ldb, int m, double2* C, long long ldc, cudaStream_t s) {
+  if (rows <= 0 || m <= 0) return;
+  const int bn = zgemm_bn(m);
+  const int kchunk = (k + 15) / 16 * 16;
+  dim3 g((rows + 63) / 64, (m + bn - 1) / bn, 1);
+  if (bn == 4)
+    zgemm_kernel<double2, false, 4><<<g, 256, 0, s>>>(A, lda, k, B, ldb, m, C, ldc, kchunk, 0, rows);
+  else if (bn == 16)
+    zgemm_kernel<double2, false, 16><<<g, 256, 0, s>>>(A, lda, k, B, ldb, m, C, ldc, kchunk, 0, rows);
+  else
+    zgemm_kernel<double2, false, 64><<<g, 256, 0, s>>>(A, lda, k, B, ldb, m, C, ldc, kchunk, 0, rows);
+}
+
 size_t zgemm_work_bytes(int n, int m, size_t elem) {
   const int z = zgemm_splits(n, m, zgemm_bn(m));
   return z > 1 ? elem * (size_t)z * n * m : 0;
@@ -249,9 +266,9 @@ static void zgemm_bn_t(bool herm, const T* A, long long lda, int n, const T* B, 
   T* out = z > 1 ? P : C;
   const long long lo = z > 1 ? n : ldc, cz = z > 1 ? (long long)n * m : 0;
   if (herm)
-    zgemm_kernel<T, true, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz);
+    zgemm_kernel<T, true, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz, n);
   else
-    zgemm_kernel<T, false, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz);
+    zgemm_kernel<T, false, BN><<<g, 256, 0, s>>>(A, lda, n, B, ldb, m, out, lo, kchunk, cz, n);
   if (z > 1)
     zgemm_reduce_kernel<T><<<dim3((n + 255) / 256, m), 256, 0, s>>>(P, cz, z, n, m, C, ldc);
 }

@@ -25,6 +25,9 @@ void launch_zgemm(bool herm, const float2* A, long long lda, int n, const float2
                   long long ldb, int m, float2* C, long long ldc, void* work,
                   size_t work_bytes, cudaStream_t s);
 size_t zgemm_work_bytes(int n, int m, size_t elem);
+// C (rows x m, ldc) = A (rows x k, lda) B (k x m, ldb), complex128
+void launch_zgemm_rect(const double2* A, long long lda, int rows, int k, const double2* B,
+                       long long ldb, int m, double2* C, long long ldc, cudaStream_t s);
 #define BEM2D_BATCHED_DECLS(T)                                                                \
   void launch_batched_dots(const T* Q, long long qstride, int n, int j, const T* W,           \
                            long long wstride, T* h, int ldh, int nb, cudaStream_t s);         \

@@ -1,6 +1,6 @@
-// Eigenvalues of a general complex matrix on sm_103a: the eigenvalue-only
-// path of Eigenvalues (lib/bem2d_mathroutines.cpp:437-466, LAPACK zgeev
-// with jobvl = jobvr = 'N').
+// Eigenvalues (and right eigenvectors) of a general complex matrix on
+// sm_103a: Eigenvalues (lib/bem2d_mathroutines.cpp:437-528, LAPACK zgeev
+// with jobvl = 'N', jobvr = 'N' or 'V').
 //
 // 1. Householder reduction to upper Hessenberg form (the unblocked
 //    reduction of Golub & Van Loan, sec. 7.4.3), step j = 0..n-3 with
@@ -21,6 +21,11 @@
 //    the active block.  Every loop bound and decision is broadcast through
 //    shared memory before the threads use it, so all threads meet every
 //    barrier.
+// 3. Eigenvectors (jobvr = 'V'): the reduction's reflectors and the QR
+//    rotations are accumulated into Z and the QR runs on the whole matrix
+//    (the Schur form A = Z T Z^H, T upper triangular), then back
+//    substitution on T (ztrevc's scheme, one CTA per vector), X = Z Y on the
+//    FP64 pipe, and zgeev's normalisation (unit norm, largest entry real).
 // No balancing (zgebal) is applied; the boundary-element matrices this
 // library produces are well scaled.
 #include <float.h>
@@ -29,6 +34,7 @@
 
 #include "common.cuh"
 #include "cplx.cuh"
+#include "dense.cuh"
 
 namespace bem2d_gpu {
 
@@ -202,12 +208,19 @@ __device__ void eig2(double2 a, double2 b, double2 c, double2 d, double2* l1, do
 // Shifted QR on the upper Hessenberg H (n x n, ld); eigenvalues into w as
 // they deflate (bottom up).  status[0] = 0, or the number of eigenvalues
 // not found when the iteration limit was reached.
+// VEC: the Schur form as well (zlahqr with wantt = wantz = true): every
+// rotation is applied to the whole rows (columns to n - 1) and the whole
+// columns (rows from 0) of H and to the columns of Z (n x n, ld, the
+// accumulated Hessenberg reduction on entry), and a deflated 2 x 2 block is
+// made upper triangular by one more rotation, so that on exit H holds the
+// upper triangular T with A = Z T Z^H and w[i] = T(i, i).
+template <bool VEC>
 __global__ void __launch_bounds__(kQrThreads)
 hess_qr_kernel(double2* __restrict__ H, long long ld, int n, double2* __restrict__ w,
-               int* __restrict__ status) {
+               int* __restrict__ status, double2* __restrict__ Z) {
   __shared__ int s_lo, s_hi, s_mode, s_defl;
   __shared__ double s_c;
-  __shared__ double2 s_s;
+  __shared__ double2 s_s, s_g0, s_g1;
   const int tid = threadIdx.x;
   auto at = [&](int i, int j) -> double2& { return H[(size_t)j * ld + i]; };
   int its = 0, total = 0;
@@ -244,10 +257,28 @@ hess_qr_kernel(double2* __restrict__ H, long long ld, int n, double2* __restrict
       } else if (lo == hi - 1) {
         double2 l1, l2;
         eig2(at(hi - 1, hi - 1), at(hi - 1, hi), at(hi, hi - 1), at(hi, hi), &l1, &l2);
-        w[hi - 1] = l1;
-        w[hi] = l2;
-        s_hi = hi - 2;
-        s_mode = 0;
+        if (VEC) {
+          // rotation whose first column is the unit eigenvector of the block
+          // for l1: (b, l1 - a) or (l1 - d, c), the better scaled one
+          const double2 a = at(hi - 1, hi - 1), b = at(hi - 1, hi), cc = at(hi, hi - 1),
+                        d = at(hi, hi);
+          double2 x = b, y = make_double2(l1.x - a.x, l1.y - a.y);
+          const double2 x2 = make_double2(l1.x - d.x, l1.y - d.y), y2 = cc;
+          if (cabs1d(x2) + cabs1d(y2) > cabs1d(x) + cabs1d(y)) {
+            x = x2;
+            y = y2;
+          }
+          const double r = hypot(hypot(x.x, x.y), hypot(y.x, y.y));
+          // G = [x -conj(y); y conj(x)] / r: G^H [a b; c d] G is upper triangular
+          s_g0 = r > 0 ? make_double2(x.x / r, x.y / r) : make_double2(1.0, 0.0);
+          s_g1 = r > 0 ? make_double2(y.x / r, y.y / r) : make_double2(0.0, 0.0);
+          s_mode = 2;
+        } else {
+          w[hi - 1] = l1;
+          w[hi] = l2;
+          s_hi = hi - 2;
+          s_mode = 0;
+        }
         its = 0;
       } else if (++total > itmax) {
         status[0] = hi + 1;
@@ -277,6 +308,40 @@ hess_qr_kernel(double2* __restrict__ H, long long ld, int n, double2* __restrict
     }
     __syncthreads();
     if (s_mode == 0) continue;  // uniform: every thread read the same flag
+    if (VEC && s_mode == 2) {
+      // triangularise the deflated 2 x 2 block at rows / columns hi-1, hi
+      // with G = [g0 -conj(g1); g1 conj(g0)]: rows (all columns from hi-1)
+      // by G^H, columns (rows 0..hi) and Z's columns by G
+      const double2 g0 = s_g0, g1 = s_g1;
+      const int p = hi - 1;
+      for (int jc = p + tid; jc < n; jc += kQrThreads) {
+        const double2 h1 = at(p, jc), h2 = at(hi, jc);
+        at(p, jc) = cfma(cconjd(g1), h2, cmul(cconjd(g0), h1));
+        at(hi, jc) = cfms(cmul(g0, h2), g1, h1);
+      }
+      __syncthreads();
+      for (int i = tid; i <= hi; i += kQrThreads) {
+        const double2 h1 = at(i, p), h2 = at(i, hi);
+        at(i, p) = cfma(h2, g1, cmul(h1, g0));
+        at(i, hi) = cfms(cmul(h2, cconjd(g0)), h1, cconjd(g1));
+      }
+      for (int i = tid; i < n; i += kQrThreads) {
+        double2* z1 = Z + (size_t)p * ld + i;
+        double2* z2 = Z + (size_t)hi * ld + i;
+        const double2 a1 = *z1, a2 = *z2;
+        *z1 = cfma(a2, g1, cmul(a1, g0));
+        *z2 = cfms(cmul(a2, cconjd(g0)), a1, cconjd(g1));
+      }
+      __syncthreads();
+      if (tid == 0) {
+        at(hi, p) = make_double2(0.0, 0.0);
+        w[p] = at(p, p);
+        w[hi] = at(hi, hi);
+        s_hi = hi - 2;
+      }
+      __syncthreads();
+      continue;
+    }
     const int lo = s_lo;
     const double2 mu = s_s;
     __syncthreads();  // all threads have read mu before s_s is reused
@@ -315,8 +380,10 @@ hess_qr_kernel(double2* __restrict__ H, long long ld, int n, double2* __restrict
       const double c = s_c;
       const double2 s = s_s;
       const double2 sc = cconjd(s);
-      // rows k, k+1, columns max(lo, k-1)..hi: (h1, h2) <- (c h1 + s h2, -conj(s) h1 + c h2)
-      for (int jc = max(lo, k - 1) + tid; jc <= hi; jc += kQrThreads) {
+      // rows k, k+1, columns max(lo, k-1)..hi (..n-1 with VEC):
+      // (h1, h2) <- (c h1 + s h2, -conj(s) h1 + c h2)
+      const int jend = VEC ? n - 1 : hi;
+      for (int jc = max(lo, k - 1) + tid; jc <= jend; jc += kQrThreads) {
         const double2 h1 = at(k, jc), h2 = at(k + 1, jc);
         const double2 n1 = cfma(s, h2, make_double2(c * h1.x, c * h1.y));
         const double2 n2 = cfms(make_double2(c * h2.x, c * h2.y), sc, h1);
@@ -325,18 +392,125 @@ hess_qr_kernel(double2* __restrict__ H, long long ld, int n, double2* __restrict
       }
       __syncthreads();
       if (tid == 0 && k > lo) at(k + 1, k - 1) = make_double2(0.0, 0.0);
-      // columns k, k+1, rows lo..min(k+2, hi): (h1, h2) <- (c h1 + conj(s) h2, -s h1 + c h2)
+      // columns k, k+1, rows lo..min(k+2, hi) (from 0 with VEC):
+      // (h1, h2) <- (c h1 + conj(s) h2, -s h1 + c h2)
       const int i1 = min(k + 2, hi);
-      for (int i = lo + tid; i <= i1; i += kQrThreads) {
+      for (int i = (VEC ? 0 : lo) + tid; i <= i1; i += kQrThreads) {
         const double2 h1 = at(i, k), h2 = at(i, k + 1);
         const double2 n1 = cfma(sc, h2, make_double2(c * h1.x, c * h1.y));
         const double2 n2 = cfms(make_double2(c * h2.x, c * h2.y), s, h1);
         at(i, k) = n1;
         at(i, k + 1) = n2;
       }
+      if (VEC) {  // the Schur vectors: columns k, k+1 of Z, the same rotation
+        for (int i = tid; i < n; i += kQrThreads) {
+          double2* z1 = Z + (size_t)k * ld + i;
+          double2* z2 = Z + (size_t)(k + 1) * ld + i;
+          const double2 h1 = *z1, h2 = *z2;
+          *z1 = cfma(sc, h2, make_double2(c * h1.x, c * h1.y));
+          *z2 = cfms(make_double2(c * h2.x, c * h2.y), s, h1);
+        }
+      }
       __syncthreads();
     }
   }
+}
+
+// Eigenvectors of the upper triangular T (n x n, ld): column j of Y (ld)
+// solves (T - T(j,j) I) y = 0 with y_j = 1, y_i = 0 below (ztrevc's back
+// substitution, column oriented: after y_k is known, r[0..k-1] -= T[0..k-1, k]
+// y_k; divisors below smin = max(eps |T(j,j)|, DBL_MIN) are raised to smin).
+// One CTA per eigenvector; r lives in Y's column.
+__global__ void __launch_bounds__(256)
+trevc_kernel(const double2* __restrict__ T, long long ld, int n, double2* __restrict__ Y) {
+  const int j = blockIdx.x;
+  double2* y = Y + (size_t)j * ld;
+  const double2 lam = T[(size_t)j * ld + j];
+  const double smin = fmax(DBL_EPSILON * cabs1d(lam), DBL_MIN);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (i < j) {
+      const double2 t = T[(size_t)j * ld + i];
+      y[i] = make_double2(-t.x, -t.y);  // r = -T[0..j-1, j]
+    } else {
+      y[i] = i == j ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+    }
+  }
+  __shared__ double2 s_yk;
+  __syncthreads();
+  for (int k = j - 1; k >= 0; --k) {
+    if (threadIdx.x == 0) {
+      double2 d = T[(size_t)k * ld + k];
+      d = make_double2(d.x - lam.x, d.y - lam.y);
+      if (cabs1d(d) < smin) d = make_double2(smin, 0.0);
+      const double2 yk = cmul(y[k], crcp(d));
+      y[k] = yk;
+      s_yk = yk;
+    }
+    __syncthreads();
+    const double2 yk = s_yk;
+    const double2* tk = T + (size_t)k * ld;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) y[i] = cfms(y[i], tk[i], yk);
+    __syncthreads();
+  }
+}
+
+// zgeev's normalisation of each column of X (n x n, ld): unit 2-norm, then
+// the entry of largest |re|^2 + |im|^2 (the first such) made real and
+// positive.  One CTA per column.
+__global__ void __launch_bounds__(256)
+normalize_vectors_kernel(double2* __restrict__ X, long long ld, int n) {
+  __shared__ double s_v[256];
+  __shared__ int s_i[256];
+  double2* x = X + (size_t)blockIdx.x * ld;
+  double ss = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) ss = fma(x[i].x, x[i].x, fma(x[i].y, x[i].y, ss));
+  s_v[threadIdx.x] = ss;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) s_v[threadIdx.x] += s_v[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double inv = s_v[0] > 0 ? 1.0 / sqrt(s_v[0]) : 1.0;
+  __syncthreads();
+  double best = -1.0;
+  int bi = n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 v = make_double2(x[i].x * inv, x[i].y * inv);
+    x[i] = v;
+    const double m = v.x * v.x + v.y * v.y;
+    if (m > best) {
+      best = m;
+      bi = i;
+    }
+  }
+  s_v[threadIdx.x] = best;
+  s_i[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      const double v2 = s_v[threadIdx.x + o];
+      const int i2 = s_i[threadIdx.x + o];
+      if (v2 > s_v[threadIdx.x] || (v2 == s_v[threadIdx.x] && i2 < s_i[threadIdx.x])) {
+        s_v[threadIdx.x] = v2;
+        s_i[threadIdx.x] = i2;
+      }
+    }
+    __syncthreads();
+  }
+  const int k = s_i[0];
+  if (k >= n || !(s_v[0] > 0)) return;
+  const double2 vk = x[k];
+  const double a = sqrt(s_v[0]);
+  const double2 f = make_double2(vk.x / a, -vk.y / a);  // conj(v_k) / |v_k|
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    x[i] = i == k ? make_double2(a, 0.0) : cmul(x[i], f);
+}
+
+// Z = I (n x n, ld)
+__global__ void identity_kernel(double2* __restrict__ Z, long long ld, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i < n) Z[(size_t)j * ld + i] = make_double2(i == j ? 1.0 : 0.0, 0.0);
 }
 
 }  // namespace
@@ -349,7 +523,7 @@ size_t eig_work_bytes(int n) {
 }
 
 long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms,
-                             cudaStream_t s) {
+                             cudaStream_t s, double2* Z) {
   auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* p = static_cast<char*>(work);
   double2* v = reinterpret_cast<double2*>(p);
@@ -365,6 +539,10 @@ long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms,
   int* status = reinterpret_cast<int*>(p);
   const long long ld = n;
   long long launches = 0;
+  if (Z) {
+    identity_kernel<<<dim3((n + 255) / 256, n), 256, 0, s>>>(Z, ld, n);
+    ++launches;
+  }
   for (int j = 0; j + 2 < n; ++j) {
     const int m = n - j - 1;
     double2* Bt = A + (size_t)(j + 1) * ld;  // columns j+1.., all rows
@@ -384,9 +562,28 @@ long long launch_eigenvalues(double2* A, int n, void* work, double2* w, int sms,
     rank1_left_kernel<<<dim3((m + 31) / 32, (m + 31) / 32), dim3(32, 8), 0, s>>>(Bl, ld, m, v,
                                                                                  wl, S);
     launches += 6;
+    if (Z) {  // Z <- Z H_j: the same right update on Z's columns j+1..
+      double2* Zt = Z + (size_t)(j + 1) * ld;
+      gemv_part_kernel<<<dim3(nb, ns), kGvRows, 0, s>>>(Zt, ld, n, m, v, chunk, P);
+      reduce_u_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, ns, P, S, u);
+      rank1_right_kernel<<<dim3((n + 31) / 32, (m + 31) / 32), dim3(32, 8), 0, s>>>(Zt, ld, n, m,
+                                                                                     u, v);
+      launches += 3;
+    }
   }
-  hess_qr_kernel<<<1, kQrThreads, 0, s>>>(A, ld, n, w, status);
+  if (Z)
+    hess_qr_kernel<true><<<1, kQrThreads, 0, s>>>(A, ld, n, w, status, Z);
+  else
+    hess_qr_kernel<false><<<1, kQrThreads, 0, s>>>(A, ld, n, w, status, nullptr);
   return launches + 1;
+}
+
+long long launch_eigenvectors(const double2* T, const double2* Z, int n, double2* Y, double2* X,
+                              cudaStream_t s) {
+  trevc_kernel<<<n, 256, 0, s>>>(T, n, n, Y);
+  launch_zgemm_rect(Z, n, n, n, Y, n, n, X, n, s);
+  normalize_vectors_kernel<<<n, 256, 0, s>>>(X, n, n);
+  return 3;
 }
 
 int* eig_status_ptr(void* work, int n) {

@@ -101,12 +101,14 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Wait (bounded) until *seq == want (acquire); returns false on timeout.
-// Spins without sleeping first: the expected wait is one L2 round trip.
-__device__ __forceinline__ bool wait_seq(const int* seq, int want, int* status) {
+// Wait (bounded: `limit` polls) until *seq == want (acquire); returns false
+// on timeout.  Spins without sleeping first: the expected wait is one L2
+// round trip.
+__device__ __forceinline__ bool wait_seq(const int* seq, int want, int* status,
+                                         unsigned limit = kSpinLimit) {
   unsigned it = 0;
   while (ld_acquire(seq) != want) {
-    if (++it > kSpinLimit || (it > 1024 && *(volatile int*)status != 0)) {
+    if (++it > limit || (it > 1024 && *(volatile int*)status != 0)) {
       atomicExch(status, 1);
       return false;
     }
@@ -128,7 +130,8 @@ __device__ __forceinline__ void block_publish(int* flag, int epoch) {
 template <typename T>
 __global__ void __launch_bounds__(kPanelThreads)
 panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
-             int* __restrict__ ipiv, int* info, int* status, PanelSlots<T> sl) {
+             int* __restrict__ ipiv, int* info, int* status, PanelSlots<T> sl, int nwait,
+             unsigned spin) {
   typedef typename CTraits<T>::R R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* P = reinterpret_cast<T*>(smem_raw);  // [rpb][kNB] block's panel rows
@@ -179,12 +182,14 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
       st_release(reinterpret_cast<int*>(my), epoch);
       if (own_k) st_release(reinterpret_cast<int*>(kr), epoch);
     }
-    // (c) wait for every block's candidate, agree on the pivot
+    // (c) wait for every block's candidate (nwait = the grid size; a larger
+    // value waits for slots nobody posts: the timeout check), agree on the
+    // pivot
     R v = -1;
     int i = INT_MAX;
-    if ((int)threadIdx.x < nblk) {
+    if ((int)threadIdx.x < nwait) {
       const char* q = sl.slot(par, threadIdx.x);
-      if (!wait_seq(reinterpret_cast<const int*>(q), epoch, status)) {
+      if (!wait_seq(reinterpret_cast<const int*>(q), epoch, status, spin)) {
         s_ok = 0;
       } else {
         i = __ldcg(reinterpret_cast<const int*>(q) + 1);
@@ -213,7 +218,7 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
       if (zero && *info == 0) *info = kc + 1;
     }
     if (!zero && p != kc && p >= r0 && p < r1) {
-      if (threadIdx.x == 0 && !wait_seq(reinterpret_cast<const int*>(kr), epoch, status))
+      if (threadIdx.x == 0 && !wait_seq(reinterpret_cast<const int*>(kr), epoch, status, spin))
         s_ok = 0;
       __syncthreads();
       if (!s_ok) return;
@@ -1249,8 +1254,10 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
       nblk = (H + rpb - 1) / rpb;
       const size_t smem = sizeof(T) * ((size_t)rpb * kNB + kNB + rpb);
       if (smem > 200 * 1024) return BEM2D_ERR_ARG;
-      void* args[] = {(void*)&A, (void*)&lda, (void*)&n, (void*)&k0, (void*)&nb, (void*)&rpb,
-                      (void*)&w.ipiv, (void*)&w.info, (void*)&w.status, (void*)&sl};
+      unsigned spin = kSpinLimit;
+      void* args[] = {(void*)&A,      (void*)&lda,    (void*)&n,      (void*)&k0,
+                      (void*)&nb,     (void*)&rpb,    (void*)&w.ipiv, (void*)&w.info,
+                      (void*)&w.status, (void*)&sl,   (void*)&nblk,   (void*)&spin};
       cudaError_t e = cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(nblk),
                                                   dim3(kPanelThreads), args, smem, s);
       if (e != cudaSuccess) return BEM2D_ERR_CUDA;
@@ -1301,12 +1308,14 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
 // the forward sweep: the owner of block k forms y_k = L_kk^{-1} b_k from the
 // stored inverse; one cluster barrier; every CTA reads y_k over DSMEM and
 // updates its rows below the block.  The backward sweep is the mirror with
-// U_kk^{-1}.  One cluster barrier per block step.
+// U_kk^{-1}.  One cluster barrier per block step.  bin and xout may be the
+// same vector (every read of bin precedes the first write of xout), so
+// neither is declared __restrict__.
 template <typename T>
 __global__ void __launch_bounds__(256)
 trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
                         const int* __restrict__ perm, const T* __restrict__ dinv,
-                        const T* __restrict__ bin, T* __restrict__ xout, int rpb) {
+                        const T* bin, T* xout, int rpb) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1381,83 +1390,184 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
   for (int i = threadIdx.x; i < nr; i += blockDim.x) xout[r0 + i] = bc[i];
 }
 
-// ---- grid-wide triangular solves (large n) -----------------------------------
-// One launch per 64-row block step.  Every CTA forms y = D^{-1} x_k from the
-// stored inverse of the diagonal block (64 x 64, redundantly: 4096 complex
-// multiply-adds) and subtracts L[rows, k] y (U[rows, k] y going back) from
-// its own 256 rows; CTA 0 also writes y to the output.  The trailing rows
-// are spread over all SMs, so the factor streams at full memory bandwidth;
-// the kernel boundary orders the steps.
-constexpr int kGridSolveThreads = 256;
-constexpr int kGridSolveMinN = 8192;  // below: the single-cluster solve (fewer launches)
-
-template <typename T>
-__global__ void perm_gather_kernel(int n, const int* __restrict__ perm, const T* __restrict__ b,
-                                   T* __restrict__ u) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < n) u[r] = b[perm[r]];
-}
+// ---- wavefront triangular solves (large n) -----------------------------------
+// One cooperative launch per triangle.  The 64-row blocks are dealt to the G
+// CTAs round-robin (block b to CTA b % G); each CTA keeps its blocks' entries
+// of the right-hand side in shared memory.  Step k (ascending going forward,
+// descending going back): the owner of block k, which has already applied
+// every earlier step to that block, forms y_k = D_k^{-1} x_k from the stored
+// inverse of the diagonal block, writes y_k to the output and to a slot in
+// global memory and posts the slot's flag (release); every other CTA that
+// still has blocks beyond k waits for the flag (acquire, bounded), reads y_k
+// and subtracts L[rows, k] y_k (U[rows, k] y_k going back) from those blocks.
+// There is no grid-wide barrier: a CTA waits only for the block it needs
+// next, and it loads the factor entries of that step and, if it owns the
+// next block, that block's inverse before it waits, so the chain of owners
+// costs about one L2 round trip and two 64 x 64 products per step.  The
+// factor streams through every SM at once.
+constexpr int kWaveThreads = 256;
+constexpr int kWaveMinN = 8192;  // below: the single-cluster solve (fewer launches)
 
 template <typename T, bool FWD>
-__global__ void __launch_bounds__(kGridSolveThreads)
-trisolve_step_kernel(const T* __restrict__ LU, long long lda, int n, const T* __restrict__ dinv,
-                     int kb, T* __restrict__ work, T* __restrict__ out) {
-  __shared__ T y[kNB];
-  __shared__ T xk[kNB];
-  const int k0 = kb * kNB, nb = min(kNB, n - k0);
+__global__ void __launch_bounds__(kWaveThreads)
+trisolve_wave_kernel(const T* __restrict__ LU, long long lda, int n, const T* __restrict__ dinv,
+                     const int* __restrict__ perm, const T* bin, T* xout, T* ybuf, int* flags,
+                     int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const T zero = CTraits<T>::make(0, 0);
-  if ((int)threadIdx.x < nb) xk[threadIdx.x] = work[k0 + threadIdx.x];
-  __syncthreads();
-  if ((int)threadIdx.x < nb) {
-    const T* Di = dinv + (size_t)(2 * kb + (FWD ? 0 : 1)) * kNB * kNB;
-    const int i = threadIdx.x;
-    T acc = zero;
-    for (int j = 0; j < nb; ++j) acc = cfma(Di[j * kNB + i], xk[j], acc);
-    y[i] = acc;
-    if (blockIdx.x == 0) out[k0 + i] = acc;
+  const int G = gridDim.x, g = blockIdx.x;
+  const int nk = (n + kNB - 1) / kNB;
+  const int nown = (nk - g + G - 1) / G;  // this CTA's blocks: g, g + G, ...
+  T* xs = reinterpret_cast<T*>(smem_raw);  // [nown][kNB]
+  T* ys = xs + (size_t)nown * kNB;          // [kNB] y of the current step
+  T* ps = ys + kNB;                         // [4][kNB] partial sums
+  __shared__ int s_ok;
+  const int r = threadIdx.x & (kNB - 1), q = threadIdx.x >> 6;  // row, 16-column group
+  for (int v = threadIdx.x; v < nown * kNB; v += blockDim.x) {
+    const int row = (g + (v / kNB) * G) * kNB + (v % kNB);
+    xs[v] = row < n ? (FWD ? bin[perm[row]] : bin[row]) : zero;
   }
+  if (threadIdx.x == 0) s_ok = 1;
   __syncthreads();
-  // rows below the block (forward) or above it (backward)
-  const int lo = FWD ? k0 + nb : 0, hi = FWD ? n : k0;
-  const int r = lo + blockIdx.x * kGridSolveThreads + threadIdx.x;
-  if (r >= hi) return;
-  const T* col = LU + (size_t)k0 * lda + r;
-  T acc = zero;
-#pragma unroll 16
-  for (int j = 0; j < nb; ++j) acc = cfma(col[(size_t)j * lda], y[j], acc);
-  T v = work[r];
-  v.x -= acc.x;
-  v.y -= acc.y;
-  work[r] = v;
+  if (nown == 0) return;
+  const int first = g, last = g + (nown - 1) * G;  // owned block range
+  // entries of the diagonal-block inverse of block k for thread (r, q)
+  auto load_dinv = [&](int kb, T* d) {
+    const T* Di = dinv + (size_t)(2 * kb + (FWD ? 0 : 1)) * kNB * kNB;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) d[u] = Di[(q * 16 + u) * kNB + r];
+  };
+  // factor entries of block row `blk` in the columns of block kb
+  auto load_l = [&](int blk, int kb, T* l) {
+    const int row = blk * kNB + r, c0 = kb * kNB + q * 16;
+    const T* col = LU + (size_t)c0 * lda + row;
+#pragma unroll
+    for (int u = 0; u < 16; ++u)
+      l[u] = (row < n && c0 + u < n) ? col[(size_t)u * lda] : zero;
+  };
+  // first owned block strictly beyond kb in the sweep direction, or -1
+  auto next_owned = [&](int kb) -> int {
+    if (FWD) {
+      if (kb >= last) return -1;
+      const int b = kb < first ? first : first + ((kb - first) / G + 1) * G;
+      return b <= last ? b : -1;
+    }
+    if (kb <= first) return -1;
+    const int b = kb > last ? last : first + ((kb - first - 1) / G) * G;
+    return b >= first ? b : -1;
+  };
+  T dpre[16], lpre[16];
+  int kb = FWD ? 0 : nk - 1;
+  if (kb % G == g) load_dinv(kb, dpre);
+  for (int s = 0; s < nk; ++s, kb += FWD ? 1 : -1) {
+    if (FWD ? kb > last : kb < first) break;  // nothing of this CTA left to update
+    const int jb = next_owned(kb);
+    if (jb >= 0) load_l(jb, kb, lpre);
+    const int kn = FWD ? kb + 1 : kb - 1;  // the next step's block
+    if (kb % G == g) {
+      // owner: y = D_k^{-1} x_k, published through ybuf / flags[kb]
+      const T* xk = xs + (size_t)((kb - first) / G) * kNB;
+      T acc = zero;
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc = cfma(dpre[u], xk[q * 16 + u], acc);
+      ps[q * kNB + r] = acc;
+      __syncthreads();
+      if ((int)threadIdx.x < kNB) {
+        const int t = threadIdx.x;
+        T v = ps[t];
+        v.x += ps[kNB + t].x + ps[2 * kNB + t].x + ps[3 * kNB + t].x;
+        v.y += ps[kNB + t].y + ps[2 * kNB + t].y + ps[3 * kNB + t].y;
+        ys[t] = v;
+        if (kb * kNB + t < n) {
+          xout[kb * kNB + t] = v;
+          ybuf[kb * kNB + t] = v;
+        }
+      }
+      block_publish(&flags[kb], 1);
+      if (kn >= 0 && kn < nk && kn % G == g) load_dinv(kn, dpre);
+    } else {
+      if (kn >= 0 && kn < nk && kn % G == g) load_dinv(kn, dpre);  // before the wait
+      if (threadIdx.x == 0 && !wait_seq(&flags[kb], 1, status)) s_ok = 0;
+      __syncthreads();
+      if (!s_ok) return;
+      if ((int)threadIdx.x < kNB)
+        ys[threadIdx.x] = kb * kNB + (int)threadIdx.x < n ? __ldcg(&ybuf[kb * kNB + threadIdx.x])
+                                                          : zero;
+    }
+    __syncthreads();
+    // update the owned blocks beyond kb: the first with the prefetched
+    // entries, the others loading theirs
+    for (int blk = jb; blk >= 0 && blk >= first && blk <= last; blk += FWD ? G : -G) {
+      T l[16];
+      if (blk == jb) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) l[u] = lpre[u];
+      } else {
+        load_l(blk, kb, l);
+      }
+      T acc = zero;
+#pragma unroll
+      for (int u = 0; u < 16; ++u) acc = cfma(l[u], ys[q * 16 + u], acc);
+      ps[q * kNB + r] = acc;
+      __syncthreads();
+      if ((int)threadIdx.x < kNB) {
+        const int t = threadIdx.x;
+        T* xv = xs + (size_t)((blk - first) / G) * kNB + t;
+        T v = *xv;
+        v.x -= ps[t].x + ps[kNB + t].x + ps[2 * kNB + t].x + ps[3 * kNB + t].x;
+        v.y -= ps[t].y + ps[kNB + t].y + ps[2 * kNB + t].y + ps[3 * kNB + t].y;
+        *xv = v;
+      }
+      __syncthreads();
+    }
+  }
 }
 
 template <typename T>
-static int lu_solve_grid(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+static int lu_solve_wave(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
                          cudaStream_t s, long long* launches) {
-  if (w.scratch_bytes < sizeof(T) * 2 * (size_t)n) return BEM2D_ERR_ARG;
-  T* u = static_cast<T*>(w.scratch);  // permuted right-hand side, updated in place
-  T* v = u + n;                       // forward result, updated in place going back
   const int nk = (n + kNB - 1) / kNB;
-  perm_gather_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(n, w.perm, b, u);
+  // scratch: forward result v [n], y slots [nk * kNB], flags [2 * nk]
+  const size_t need = sizeof(T) * ((size_t)n + (size_t)nk * kNB) + sizeof(int) * 2 * nk;
+  if (w.scratch_bytes < need) return BEM2D_ERR_ARG;
+  T* v = static_cast<T*>(w.scratch);
+  T* ybuf = v + n;
+  int* flags = reinterpret_cast<int*>(ybuf + (size_t)nk * kNB);
+  static const int nsm = [] {
+    int dev = 0, c = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(c, 1);
+  }();
+  const int G = std::min(nk, nsm);
+  const size_t smem = sizeof(T) * ((size_t)((nk + G - 1) / G) * kNB + 5 * kNB);
+  if (smem > 48 * 1024) return BEM2D_ERR_ARG;
+  cudaMemsetAsync(flags, 0, sizeof(int) * 2 * nk, s);
   const T* dinv = reinterpret_cast<const T*>(w.dinv);
-  for (int kb = 0; kb < nk; ++kb) {
-    const int rows = n - std::min(n, (kb + 1) * kNB);
-    const int g = std::max(1, (rows + kGridSolveThreads - 1) / kGridSolveThreads);
-    trisolve_step_kernel<T, true><<<g, kGridSolveThreads, 0, s>>>(LU, lda, n, dinv, kb, u, v);
-  }
-  for (int kb = nk - 1; kb >= 0; --kb) {
-    const int rows = kb * kNB;
-    const int g = std::max(1, (rows + kGridSolveThreads - 1) / kGridSolveThreads);
-    trisolve_step_kernel<T, false><<<g, kGridSolveThreads, 0, s>>>(LU, lda, n, dinv, kb, v, x);
-  }
-  *launches += 1 + 2 * nk;
+  const int* perm = w.perm;
+  int* fl = flags;
+  int* status = w.status;
+  T* vo = v;
+  void* af[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&dinv, (void*)&perm, (void*)&b,
+                (void*)&vo, (void*)&ybuf, (void*)&fl, (void*)&status};
+  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, true>, dim3(G),
+                                  dim3(kWaveThreads), af, smem, s) != cudaSuccess)
+    return BEM2D_ERR_CUDA;
+  const T* vin = v;
+  int* fb = flags + nk;
+  void* ab[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&dinv, (void*)&perm, (void*)&vin,
+                (void*)&x, (void*)&ybuf, (void*)&fb, (void*)&status};
+  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, false>, dim3(G),
+                                  dim3(kWaveThreads), ab, smem, s) != cudaSuccess)
+    return BEM2D_ERR_CUDA;
+  *launches += 2;
   return BEM2D_OK;
 }
 
 template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
              cudaStream_t s, long long* launches) {
-  if (n >= kGridSolveMinN) return lu_solve_grid(LU, lda, n, w, b, x, s, launches);
+  if (n >= kWaveMinN) return lu_solve_wave(LU, lda, n, w, b, x, s, launches);
   static std::atomic<int> cmax{kMaxCluster};
   static std::once_flag attr;
   std::call_once(attr, [] {
@@ -1601,6 +1711,39 @@ template int lu_solve_h<double2>(const double2*, long long, int, const LuWork&, 
 template int lu_solve_h<float2>(const float2*, long long, int, const LuWork&, const float2*,
                                 float2*, cudaStream_t, long long*);
 
+// Timeout check of the grid panel's bounded waits: one panel of the
+// complex64 matrix A (n x 64, n >= 256, lda) on two cooperative blocks whose
+// waits expect three candidates, so each waits for a slot that is never
+// posted; every wait gives up after `polls` polls, sets *w.status and the
+// kernel returns.  The caller reads *w.status after synchronising.
+int lu_panel_timeout_probe(float2* A, long long lda, int n, const LuWork& w, unsigned polls,
+                           cudaStream_t s) {
+  if (n < 256 || lda < n || polls < 1) return BEM2D_ERR_ARG;
+  PanelSlots<float2> sl;
+  sl.base = static_cast<char*>(w.scratch);
+  cudaMemsetAsync(w.info, 0, sizeof(int), s);
+  cudaMemsetAsync(w.status, 0, sizeof(int), s);
+  cudaMemsetAsync(sl.base, 0, slots_bytes(sizeof(float2)), s);
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    cudaFuncSetAttribute(panel_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+  });
+  int nblk = 2, k0 = 0, nb = kNB;
+  int rpb = (n + nblk - 1) / nblk;
+  const size_t smem = sizeof(float2) * ((size_t)rpb * kNB + kNB + rpb);
+  if (smem > 200 * 1024) return BEM2D_ERR_ARG;
+  int nwait = nblk + 1;
+  unsigned spin = polls;
+  void* args[] = {(void*)&A,      (void*)&lda,    (void*)&n,      (void*)&k0,
+                  (void*)&nb,     (void*)&rpb,    (void*)&w.ipiv, (void*)&w.info,
+                  (void*)&w.status, (void*)&sl,   (void*)&nwait,  (void*)&spin};
+  return cudaLaunchCooperativeKernel((void*)panel_kernel<float2>, dim3(nblk),
+                                     dim3(kPanelThreads), args, smem, s) == cudaSuccess
+             ? BEM2D_OK
+             : BEM2D_ERR_CUDA;
+}
+
 template int lu_factor<double2>(double2*, long long, int, const LuWork&, cudaStream_t, long long*);
 template int lu_factor<float2>(float2*, long long, int, const LuWork&, cudaStream_t, long long*);
 template int lu_solve<double2>(const double2*, long long, int, const LuWork&, const double2*,
@@ -1731,5 +1874,26 @@ void launch_sumsq(const double2* A, long long ld, int rows, int cols, double* pa
   sum_kernel<<<1, 256, 0, s>>>(kSumsqBlocks, part, out);
 }
 size_t sumsq_part_bytes() { return sizeof(double) * kSumsqBlocks; }
+
+// *flag |= 1 if any entry of the rows x cols column-major block is NaN or
+// infinite: one coalesced pass (rows fastest), one atomic per warp that saw
+// a non-finite value.
+__global__ void nonfinite_kernel(const double2* __restrict__ A, long long ld, int rows, int cols,
+                                 int* flag) {
+  bool bad = false;
+  for (int j = blockIdx.y; j < cols; j += gridDim.y)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+      const double2 a = A[(size_t)j * ld + i];
+      bad |= !(isfinite(a.x) && isfinite(a.y));
+    }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+void launch_nonfinite_scan(const double2* A, long long ld, int rows, int cols, int* flag,
+                           cudaStream_t s) {
+  const int bx = std::min(8, (rows + 255) / 256);
+  const int by = std::min(cols, 1024);
+  nonfinite_kernel<<<dim3(bx, by), 256, 0, s>>>(A, ld, rows, cols, flag);
+}
 
 }  // namespace bem2d_gpu

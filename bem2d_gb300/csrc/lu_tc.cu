@@ -2,15 +2,16 @@
 // C -= A B (complex64, column-major, arbitrary leading dimensions), as
 // tcgen05.mma kind::tf32 with FP32 accumulators in tensor memory.
 //
-// Complex arithmetic as two real products.  The complex M x K operand A is
+// Complex arithmetic as one real product.  The complex M x K operand A is
 // read as a real (2M) x K matrix A' whose rows 2i and 2i + 1 hold re and im
-// of row i (that is how complex column-major data lies in memory).  With the
-// real and imaginary parts B_r, B_i of B (K x N):
-//   D1 = A' B_r,  D2 = A' B_i,
+// of row i (that is how complex column-major data lies in memory).  The
+// complex K x N operand B becomes the real N' x K operand [B_r; B_i] with
+// N' = 2N (the real parts of the tile's columns, then the imaginary parts),
+// so one MMA of N = 256 gives D = A' [B_r B_i] with
+//   D1 = A' B_r (columns 0..127),  D2 = A' B_i (columns 128..255),
 //   re C_i = D1[2i] - D2[2i+1],   im C_i = D2[2i] + D1[2i+1].
-// One CTA owns a tile of 64 complex rows (128 real rows = the MMA's M) and
-// 64 complex columns (the MMA's N); D1 and D2 take 64 tensor-memory columns
-// each.
+// A tile is 64 complex rows (128 real rows = the MMA's M) by 128 complex
+// columns: 256 tensor-memory columns per accumulator.
 //
 // Accuracy (3xTF32): every FP32 operand x is split into hi = x with its low
 // 13 mantissa bits cleared (exactly a TF32 value) and lo = x - hi; each
@@ -23,16 +24,29 @@
 // the MMA reads them from shared memory - the K-major, non-swizzled
 // canonical layout (core matrices of 8 rows x 16 bytes, 128 bytes from one
 // core matrix to the next along K, 512 bytes from one group of 8 rows to the
-// next).  The update kernel then stages each chunk with two bulk copies
-// (cp.async.bulk, completion counted in bytes on an mbarrier) into one of two
-// shared-memory stages, so the copy of chunk c + 1 overlaps the MMAs of
-// chunk c.  One thread issues the copies and the MMAs; tcgen05.commit
-// signals an mbarrier when a stage's MMAs are done (the stage may then be
-// refilled) and, at the end, that the accumulators are complete.  Every wait
-// is bounded: on timeout the status flag is set and the tile is left
-// unchanged.  The epilogue reads D1/D2 with tcgen05.ld (warp w reads lanes
-// 32w..32w+31 = real rows), combines rows 2i/2i+1 with one shuffle and
-// updates C in place.
+// next).  A chunk is then one contiguous block per operand: 16 KB of A'
+// (hi, lo) and 32 KB of B (hi, lo).
+//
+// The update kernel is persistent (one CTA per SM, tiles in a static
+// round-robin) and warp-specialised:
+//   warp 0      producer: two bulk copies (cp.async.bulk, completion counted
+//               in bytes on the stage's `full` mbarrier) per chunk into a
+//               ring of four 48 KB shared-memory stages;
+//   warp 1      MMA issuer: six MMAs per chunk (two K-steps of 8, 3xTF32);
+//               tcgen05.commit frees the stage (`empty`) once its MMAs have
+//               read it, and marks the tile's accumulator complete (`acc_full`);
+//   warps 2-17  epilogue: tcgen05.ld of the accumulator (warp w reads TMEM
+//               lanes 32 (w % 4) ..., four warps per lane quarter, one per
+//               quarter of the columns), rows 2i / 2i + 1 combined with one
+//               shuffle; each thread loads its 32 C values before it waits
+//               for the tile's accumulator (the loads overlap the tile's
+//               MMAs; the next tile's C is prefetched into L2 meanwhile), C
+//               is written with coalesced 128-byte accesses; then `acc_empty`.
+// The two accumulators alternate between tiles (512 TMEM columns), so the
+// epilogue of one tile overlaps the MMAs of the next.  Every wait is bounded
+// (2 s of device time): on timeout the status flag is set, every role stops,
+// the producer waits (bounded) for its copies in flight and the MMA thread
+// for its MMAs, and the tensor memory is released before the kernel returns.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -40,19 +54,23 @@
 namespace bem2d_gpu {
 namespace {
 
-constexpr int kTcBM = 64;   // complex rows per tile (128 real rows = MMA M)
-constexpr int kTcBN = 64;   // complex columns per tile (MMA N)
-constexpr int kTcBK = 16;   // K per chunk (two MMAs of K = 8)
-constexpr int kTcThreads = 128;
+constexpr int kTcBM = 64;    // complex rows per tile (128 real rows = MMA M)
+constexpr int kTcBN = 128;   // complex columns per tile (MMA N = 256: re, im)
+constexpr int kTcBK = 16;    // K per chunk (two MMAs of K = 8)
+constexpr int kTcStages = 4;
+constexpr int kTcThreads = 576;  // producer warp, MMA warp, 16 epilogue warps
+constexpr int kTcEpiThreads = 512;
 constexpr int kCoreBytes = 128;                   // 8 rows x 16 bytes
 constexpr int kTcSBO = (kTcBK / 4) * kCoreBytes;  // 512
 constexpr int kTcApart = 2 * kTcBM * kTcBK * 4;   // 8 KB: 128 real rows x 16
-constexpr int kTcBpart = kTcBN * kTcBK * 4;       // 4 KB: 64 rows x 16
+constexpr int kTcBpart = 2 * kTcBN * kTcBK * 4;   // 16 KB: 256 rows x 16
 constexpr int kTcChunkA = 2 * kTcApart;           // hi, lo
-constexpr int kTcChunkB = 4 * kTcBpart;           // re hi, re lo, im hi, im lo
-constexpr int kTcStage = kTcChunkA + kTcChunkB;   // 32 KB
-constexpr int kTcSmem = 2 * kTcStage + 64;
-constexpr unsigned kTcSpin = 1u << 24;
+constexpr int kTcChunkB = 2 * kTcBpart;           // hi, lo
+constexpr int kTcStage = kTcChunkA + kTcChunkB;   // 48 KB
+constexpr int kTcBarOff = kTcStages * kTcStage;   // 192 KB
+constexpr int kTcSmem = kTcBarOff + 256;
+constexpr unsigned kTcAcc = 2 * kTcBN;            // TMEM columns per accumulator
+constexpr unsigned long long kTcWaitNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -79,24 +97,51 @@ __device__ __forceinline__ void mma_tf32(unsigned d, unsigned a, unsigned b, uns
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
       "l"(smem_desc(a)), "l"(smem_desc(b)), "r"(idesc), "r"(acc));
 }
+__device__ __forceinline__ void mma_commit(unsigned long long* m) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(m)));
+}
 
-__device__ __forceinline__ void mbar_init(unsigned long long* m) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(m)));
+__device__ __forceinline__ void mbar_init(unsigned long long* m, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* m, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)),
                "r"(bytes));
 }
-// bounded wait for phase `parity` of the mbarrier; false on timeout
-__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity) {
-  unsigned done = 0;
-  for (unsigned it = 0; it < kTcSpin && !done; ++it)
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(smem_u32(m)), "r"(parity));
+__device__ __forceinline__ void mbar_arrive(unsigned long long* m) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* m, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
   return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for phase `parity` of the mbarrier (try_wait suspends the
+// thread for a short while between polls): false after kTcWaitNs of device
+// time, or, if `abort` is given, as soon as another role has given up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* m, unsigned parity,
+                                          const volatile int* abort) {
+  if (mbar_test(m, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (unsigned it = 1;; ++it) {
+    if (mbar_test(m, parity)) return true;
+    if ((it & 15u) == 0u) {
+      if (abort && *abort) return false;
+      if (global_ns() - t0 > kTcWaitNs) return false;
+    }
+  }
 }
 __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned bytes,
                                           unsigned long long* m) {
@@ -137,8 +182,9 @@ __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M
   *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il + 1, kl)) = l;
 }
 
-// B (K x N complex) -> Bpk[nt][kc] = {re hi, re lo, im hi, im lo} chunks.
-// grid: (ceil(N / 64) * 64 x ceil(nkc * 16 / 64)), 64 threads
+// B (K x N complex) -> Bpk[nt][kc] = {hi, lo} chunks of kTcBpart bytes, each
+// with rows 0..127 = re and rows 128..255 = im of the tile's 128 columns.
+// grid: (ceil(N / 128) * 128 x ceil(nkc * 16 / 64)), 64 threads
 __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int nkc,
                               unsigned char* __restrict__ Bpk) {
   const int n = blockIdx.x;                             // complex column
@@ -148,43 +194,50 @@ __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K
   const int kc = k / kTcBK, kl = k - kc * kTcBK;
   const float2 v = (k < K && n < N) ? B[(size_t)n * ldb + k] : make_float2(0.f, 0.f);
   unsigned char* chunk = Bpk + ((size_t)nt * nkc + kc) * kTcChunkB;
-  const int off = kmajor_off(nl, kl);
+  const int ore = kmajor_off(nl, kl), oim = kmajor_off(kTcBN + nl, kl);
   float h, l;
   tf32_split(v.x, h, l);
-  *reinterpret_cast<float*>(chunk + off) = h;
-  *reinterpret_cast<float*>(chunk + kTcBpart + off) = l;
+  *reinterpret_cast<float*>(chunk + ore) = h;
+  *reinterpret_cast<float*>(chunk + kTcBpart + ore) = l;
   tf32_split(v.y, h, l);
-  *reinterpret_cast<float*>(chunk + 2 * kTcBpart + off) = h;
-  *reinterpret_cast<float*>(chunk + 3 * kTcBpart + off) = l;
+  *reinterpret_cast<float*>(chunk + oim) = h;
+  *reinterpret_cast<float*>(chunk + kTcBpart + oim) = l;
 }
 
 // ---- the update --------------------------------------------------------------
-// grid (ceil(M / 64), ceil(N / 64)), 128 threads, kTcSmem bytes of shared memory
-__global__ void __launch_bounds__(kTcThreads, 3)
+// grid: min(tiles, SMs) persistent CTAs, kTcThreads threads, kTcSmem bytes
+// of shared memory (one CTA per SM).  Tile t: mt = t % mtiles, nt = t / mtiles.
+__global__ void __launch_bounds__(kTcThreads, 1)
 tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* __restrict__ Apk,
-                    const unsigned char* __restrict__ Bpk, int M, int N, int nkc, int* status) {
+                    const unsigned char* __restrict__ Bpk, int M, int N, int nkc, int mtiles,
+                    int ntiles, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned long long* full = reinterpret_cast<unsigned long long*>(sm + 2 * kTcStage);
-  unsigned long long* done = full + 2;
-  unsigned* tslot = reinterpret_cast<unsigned*>(done + 2);
-  int* s_ok = reinterpret_cast<int*>(tslot + 1);
-  const int t = threadIdx.x, w = t >> 5;
-  const int mt = blockIdx.x, nt = blockIdx.y;
-  const int i0 = mt * kTcBM, n0 = nt * kTcBN;
-  const unsigned char* asrc = Apk + (size_t)mt * nkc * kTcChunkA;
-  const unsigned char* bsrc = Bpk + (size_t)nt * nkc * kTcChunkB;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(sm + kTcBarOff);
+  unsigned long long* empty = full + kTcStages;
+  unsigned long long* acc_full = empty + kTcStages;
+  unsigned long long* acc_empty = acc_full + 2;
+  unsigned long long* fin = acc_empty + 2;
+  unsigned* tslot = reinterpret_cast<unsigned*>(fin + 1);
+  volatile int* s_abort = reinterpret_cast<volatile int*>(tslot + 1);
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  const int ntl = mtiles * ntiles;
   if (w == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
         smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (t == 0) {
-    mbar_init(&full[0]);
-    mbar_init(&full[1]);
-    mbar_init(&done[0]);
-    mbar_init(&done[1]);
+  if (t == 32) {
+    for (int s = 0; s < kTcStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&acc_full[a], 1);
+      mbar_init(&acc_empty[a], kTcEpiThreads);
+    }
+    mbar_init(fin, 1);
     asm volatile("fence.mbarrier_init.release.cluster;");
-    *s_ok = 1;
+    *s_abort = 0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
@@ -192,95 +245,171 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* 
   const unsigned tmem = *tslot;
   // kind::tf32: D f32 (bits 4-5 = 1), A/B tf32 (bits 7-9, 10-12 = 2), both
   // K-major, N >> 3 at bit 17, M >> 4 at bit 24
-  const unsigned idesc =
-      (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(kTcBN >> 3) << 17) | ((128u >> 4) << 24);
-  if (t == 0) {
-    // chunk c goes to stage c & 1: A (hi, lo) and B (four parts) are each
-    // one contiguous block in the packed operands
-    auto issue = [&](int c) {
-      unsigned char* st = sm + (c & 1) * kTcStage;
-      mbar_expect_tx(&full[c & 1], kTcStage);
-      bulk_copy(st, asrc + (size_t)c * kTcChunkA, kTcChunkA, &full[c & 1]);
-      bulk_copy(st + kTcChunkA, bsrc + (size_t)c * kTcChunkB, kTcChunkB, &full[c & 1]);
+  const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((kTcAcc >> 3) << 17) |
+                         ((128u >> 4) << 24);
+  bool ok = true;
+  if (w == 0) {
+    if (lane == 0) {  // ---- producer
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntl && ok; tile += gridDim.x) {
+        const int mt = tile % mtiles, nt = tile / mtiles;
+        const unsigned char* asrc = Apk + (size_t)mt * nkc * kTcChunkA;
+        const unsigned char* bsrc = Bpk + (size_t)nt * nkc * kTcChunkB;
+        for (int c = 0; c < nkc; ++c, ++it) {
+          const int s = it % kTcStages;
+          const unsigned ph = (unsigned)(it / kTcStages) & 1u;
+          if (!mbar_wait(&empty[s], ph ^ 1u, s_abort)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = sm + s * kTcStage;
+          mbar_expect_tx(&full[s], kTcStage);
+          bulk_copy(st, asrc + (size_t)c * kTcChunkA, kTcChunkA, &full[s]);
+          bulk_copy(st + kTcChunkA, bsrc + (size_t)c * kTcChunkB, kTcChunkB, &full[s]);
+        }
+      }
+      if (!ok) {
+        *s_abort = 1;
+        // let the copies in flight land before the CTA's shared memory goes
+        for (int q = it - 1; q >= 0 && q >= it - kTcStages; --q)
+          mbar_wait(&full[q % kTcStages], (unsigned)(q / kTcStages) & 1u, nullptr);
+      }
+    }
+  } else if (w == 1) {
+    if (lane == 0) {  // ---- MMA issuer
+      int it = 0, j = 0;
+      for (int tile = blockIdx.x; tile < ntl && ok; tile += gridDim.x, ++j) {
+        const int a = j & 1;
+        const unsigned aph = (unsigned)(j >> 1) & 1u;
+        if (!mbar_wait(&acc_empty[a], aph ^ 1u, s_abort)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const unsigned d = tmem + (unsigned)a * kTcAcc;
+        for (int c = 0; c < nkc; ++c, ++it) {
+          const int s = it % kTcStages;
+          const unsigned ph = (unsigned)(it / kTcStages) & 1u;
+          if (!mbar_wait(&full[s], ph, s_abort)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const unsigned base = smem_u32(sm + s * kTcStage);
+          const unsigned ah = base, al = base + kTcApart;
+          const unsigned bh = base + kTcChunkA, bl = bh + kTcBpart;
+#pragma unroll
+          for (int ks = 0; ks < kTcBK / 8; ++ks) {
+            const unsigned o = 256u * ks;  // K = 8 tf32 = two core matrices
+            mma_tf32(d, ah + o, bh + o, idesc, (c == 0 && ks == 0) ? 0u : 1u);
+            mma_tf32(d, ah + o, bl + o, idesc, 1u);
+            mma_tf32(d, al + o, bh + o, idesc, 1u);
+          }
+          mma_commit(&empty[s]);  // the stage may be refilled once these MMAs read it
+        }
+        if (!ok) break;
+        mma_commit(&acc_full[a]);
+      }
+      if (!ok) *s_abort = 1;
+      // every MMA issued has completed before the tensor memory is released
+      mma_commit(fin);
+      if (!mbar_wait(fin, 0u, nullptr)) ok = false;
+    }
+  } else {  // ---- epilogue, warps 2-17
+    // four warps per TMEM lane quarter (warp w may access lanes 32 (w % 4)
+    // ..), one for each quarter of the tile's 128 columns
+    const int ew = w - 2, q = w & 3, part = ew >> 2;
+    const int tl = q * 32 + lane;
+    const int i = tl >> 1, cc = tl & 1;  // real row tl = 2i + cc
+    float* Cf = reinterpret_cast<float*>(C);
+    // the next tile's C columns into L2 while this tile's MMAs run: thread
+    // et covers 128 of the 512 bytes of column et / 4 of the tile
+    auto prefetch = [&](int tile) {
+      if (tile >= ntl) return;
+      const int et = ew * 32 + lane;
+      const int i0 = (tile % mtiles) * kTcBM, n = (tile / mtiles) * kTcBN + (et >> 2);
+      const int l = et & 3;
+      if (n >= N || l * 16 >= M - i0) return;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(Cf + 2 * ((size_t)n * ldc + i0) + 32 * l));
     };
-    issue(0);
-    if (nkc > 1) issue(1);
-    const unsigned d1 = tmem, d2 = tmem + kTcBN;
-    for (int c = 0; c < nkc; ++c) {
-      const int s = c & 1;
-      const unsigned ph = (c >> 1) & 1;
-      if (!mbar_wait(&full[s], ph)) {
-        *s_ok = 0;
+    prefetch(blockIdx.x);
+    int j = 0;
+    for (int tile = blockIdx.x; tile < ntl; tile += gridDim.x, ++j) {
+      prefetch(tile + gridDim.x);
+      const int mt = tile % mtiles, nt = tile / mtiles;
+      const int i0 = mt * kTcBM, n0 = nt * kTcBN + part * (kTcBN / 4);
+      const bool row_ok = i0 + i < M;
+      float* crow = Cf + 2 * ((size_t)i0 + i) + cc;
+      // this thread's 32 C values, loaded while the tile's MMAs still run
+      const int nlim = row_ok ? min(kTcBN / 4, N - n0) : 0;
+      const long long cstep = 2 * ldc;
+      float cv[kTcBN / 4];
+      {
+        const float* pc = crow + (size_t)n0 * cstep;
+        if (nlim == kTcBN / 4) {  // full tile: no per-column predicates
+#pragma unroll
+          for (int u = 0; u < kTcBN / 4; ++u, pc += cstep) cv[u] = *pc;
+        } else {
+#pragma unroll
+          for (int u = 0; u < kTcBN / 4; ++u, pc += cstep) cv[u] = u < nlim ? *pc : 0.f;
+        }
+      }
+      const int a = j & 1;
+      const unsigned aph = (unsigned)(j >> 1) & 1u;
+      if (!mbar_wait(&acc_full[a], aph, s_abort)) {
+        ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const unsigned base = smem_u32(sm + s * kTcStage);
-      const unsigned ah = base, al = base + kTcApart;
-      const unsigned brh = base + kTcChunkA, brl = brh + kTcBpart;
-      const unsigned bih = brh + 2 * kTcBpart, bil = brh + 3 * kTcBpart;
+      const unsigned lanes = tmem + (unsigned)a * kTcAcc + ((unsigned)(q * 32) << 16) +
+                             (unsigned)(part * (kTcBN / 4));
+      float* pw = crow + (size_t)n0 * cstep;
 #pragma unroll
-      for (int ks = 0; ks < kTcBK / 8; ++ks) {
-        const unsigned o = 256u * ks;  // K = 8 tf32 = two core matrices
-        const unsigned acc = (c == 0 && ks == 0) ? 0u : 1u;
-        mma_tf32(d1, ah + o, brh + o, idesc, acc);
-        mma_tf32(d1, ah + o, brl + o, idesc, 1u);
-        mma_tf32(d1, al + o, brh + o, idesc, 1u);
-        mma_tf32(d2, ah + o, bih + o, idesc, acc);
-        mma_tf32(d2, ah + o, bil + o, idesc, 1u);
-        mma_tf32(d2, al + o, bih + o, idesc, 1u);
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&done[s])));
-      if (c + 2 < nkc) {  // refill this stage once its MMAs have read it
-        if (!mbar_wait(&done[s], ph)) {
-          *s_ok = 0;
-          break;
+      for (int h = 0; h < kTcBN / 4; h += 16) {
+        unsigned d1[16], d2[16];
+        TC_LD16(d1, lanes + h);
+        TC_LD16(d2, lanes + kTcBN + h);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        float o[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const float p2 = __shfl_xor_sync(0xffffffffu, __uint_as_float(d2[u]), 1);
+          o[u] = cv[h + u] - (__uint_as_float(d1[u]) + (cc ? p2 : -p2));
         }
-        issue(c + 2);
-      }
-    }
-  }
-  __syncthreads();
-  // the last commit covers every MMA of the tile
-  bool ok = *s_ok != 0;
-  if (ok) ok = mbar_wait(&done[(nkc - 1) & 1], ((nkc - 1) >> 1) & 1);
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (__syncthreads_or(!ok)) {
-    if (t == 0) atomicExch(status, 1);
-  } else {
-    const int i = t >> 1, c = t & 1;  // real row t = 2i + c
-    const unsigned lanes = tmem + ((unsigned)(w * 32) << 16);
-    float* Cf = reinterpret_cast<float*>(C);
-    const bool row_ok = i0 + i < M;
-    for (int j0 = 0; j0 < kTcBN; j0 += 16) {
-      float cv[16];  // the C values first, all loads in flight
+        if (nlim == kTcBN / 4) {
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const int n = n0 + j0 + u;
-        cv[u] = (row_ok && n < N) ? Cf[2 * ((size_t)n * ldc + i0 + i) + c] : 0.f;
-      }
-      unsigned dv1[16], dv2[16];
-      TC_LD16(dv1, lanes + j0);
-      TC_LD16(dv2, lanes + kTcBN + j0);
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
+          for (int u = 0; u < 16; ++u, pw += cstep) *pw = o[u];
+        } else {
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        const float p2 = __shfl_xor_sync(0xffffffffu, __uint_as_float(dv2[u]), 1);
-        const float o = __uint_as_float(dv1[u]) + (c ? p2 : -p2);
-        const int n = n0 + j0 + u;
-        if (row_ok && n < N) Cf[2 * ((size_t)n * ldc + i0 + i) + c] = cv[u] - o;
+          for (int u = 0; u < 16; ++u, pw += cstep)
+            if (h + u < nlim) *pw = o[u];
+        }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mbar_arrive(&acc_empty[a]);
     }
+    if (!ok) *s_abort = 1;
   }
+  if (!ok) atomicExch(status, 1);
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
 }
 
 #undef TC_LD16
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+int num_sms() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
 
 }  // namespace
 
@@ -305,8 +434,9 @@ int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda
   pack_a_kernel<<<dim3((mt * kTcBM + 127) / 128, nkc * kTcBK), 128, 0, s>>>(A, lda, M, K, nkc,
                                                                             Apk);
   pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc, Bpk);
-  tc_cgemm_sub_kernel<<<dim3(mt, nt), kTcThreads, kTcSmem, s>>>(C, ldc, Apk, Bpk, M, N, nkc,
-                                                                status);
+  const int grid = std::min(mt * nt, num_sms());
+  tc_cgemm_sub_kernel<<<grid, kTcThreads, kTcSmem, s>>>(C, ldc, Apk, Bpk, M, N, nkc, mt, nt,
+                                                        status);
   return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
 }
 

@@ -17,7 +17,8 @@
 // kScratchBytes, sized for n <= BEM2D_NOALLOC_MAX_N.  That array is part of
 // this library's device image: the CUDA runtime reserves it when the module
 // is loaded, not this function.  Larger n is rejected with BEM2D_ERR_ARG and
-// a message naming the limit.
+// a message naming the limit; bem2d_noalloc_scratch_fits() reports whether
+// the largest accepted n fits the array (a host-side check for the tests).
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress (which may load this
@@ -44,9 +45,9 @@ namespace {
 
 constexpr size_t kAlign = 256;
 constexpr int kMaxDevices = 64;
-// n = 1024: A 16 MiB + b 16 KiB + pivots 4 KiB + panel slots 2.03 MiB +
-// permutation and diagonal-block inverses 2.0 MiB = 20.06 MiB; 21 MiB leaves
-// room for the 256-byte alignment of each part.
+// n = 1024: A 16 MiB + b 16 KiB + x 16 KiB + pivots 4 KiB + panel slots
+// 2.03 MiB + permutation and diagonal-block inverses 2.0 MiB = 20.07 MiB;
+// 21 MiB leaves room for the 256-byte alignment of each part.
 constexpr size_t kScratchBytes = (size_t)21 << 20;
 
 static_assert(BEM2D_NOALLOC_MAX_N > 0, "BEM2D_NOALLOC_MAX_N must be positive");
@@ -62,14 +63,15 @@ size_t round_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
 // Byte offsets of the parts within the array for n unknowns.
 struct Layout {
-  size_t lu, vec, ints, slots, aux, aux_bytes, total;
+  size_t lu, vec, xv, ints, slots, aux, aux_bytes, total;
 };
 
 Layout layout(int n) {
   Layout L;
   L.lu = 0;
   L.vec = L.lu + round_up(sizeof(double2) * (size_t)n * n);
-  L.ints = L.vec + round_up(sizeof(double2) * (size_t)n);
+  L.xv = L.vec + round_up(sizeof(double2) * (size_t)n);
+  L.ints = L.xv + round_up(sizeof(double2) * (size_t)n);
   L.slots = L.ints + round_up(sizeof(int) * ((size_t)n + 8));
   L.aux = L.slots + round_up(lu_scratch_bytes(n));
   L.aux_bytes = lu_aux_bytes(n, sizeof(double2));
@@ -133,7 +135,8 @@ extern "C" int bem2d_solve_system_noalloc(bem2d_ctx* c, int n, const void* A, in
   const cudaStream_t s = ctx_stream(c);
 
   double2* LU = reinterpret_cast<double2*>(base + L.lu);
-  double2* v = reinterpret_cast<double2*>(base + L.vec);
+  double2* v = reinterpret_cast<double2*>(base + L.vec);   // b
+  double2* xv = reinterpret_cast<double2*>(base + L.xv);   // x
   int* ints = reinterpret_cast<int*>(base + L.ints);
   LuWork w;
   w.info = ints;
@@ -168,14 +171,24 @@ extern "C" int bem2d_solve_system_noalloc(bem2d_ctx* c, int n, const void* A, in
     std::snprintf(msg, sizeof msg, "zero pivot at column %d", hinfo[0]);
     return ctx_fail(c, hinfo[0], msg);
   }
-  if ((rc = lu_solve<double2>(LU, n, n, w, v, v, s, ctx_launches(c))))
+  if ((rc = lu_solve<double2>(LU, n, n, w, v, xv, s, ctx_launches(c))))
     return ctx_fail(c, rc, "triangular solve launch failed");
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, "triangular solve kernels", e);
-  e = cudaMemcpyAsync(x, v, sizeof(double2) * n, cudaMemcpyDefault, s);
+  e = cudaMemcpyAsync(x, xv, sizeof(double2) * n, cudaMemcpyDefault, s);
   if (e != cudaSuccess) return cuda_fail(c, "copy of x out of the scratch array", e);
   e = cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(c, "solve status read", e);
   if (hinfo[1]) return ctx_fail(c, BEM2D_ERR_TIMEOUT, "triangular solve wait timed out");
   return BEM2D_OK;
+}
+
+// Host-side check that the parts for n = BEM2D_NOALLOC_MAX_N fit the array:
+// 1 if they do (their byte total in *total), 0 if not.
+extern "C" int bem2d_noalloc_scratch_fits(int64_t* total, int64_t* capacity) {
+  using namespace bem2d_gpu;
+  const Layout L = layout(BEM2D_NOALLOC_MAX_N);
+  if (total) *total = (int64_t)L.total;
+  if (capacity) *capacity = (int64_t)kScratchBytes;
+  return L.total <= kScratchBytes ? 1 : 0;
 }

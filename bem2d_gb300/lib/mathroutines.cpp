@@ -1,12 +1,14 @@
 // bem2d C++ API (GB300 build): Matrix and the dense linear algebra.  LU solve,
 // norms / condition numbers, change of basis and the numerical range run on
-// the GPU (include/bem2d_gpu.h); the elementwise operators stay on the host
-// where the reference's Matrix lives.
+// the GPU (include/bem2d_gpu.h), and so does the matrix product; the
+// elementwise operators stay on the host where the reference's Matrix lives.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <thread>
+#include <vector>
 
 #include "bem2d_mathroutines.h"
 #include "bem2d_pnpoly.h"
@@ -27,44 +29,73 @@ Matrix::Matrix(const Matrix& m) : data(new cvector(*m.data)), msize(m.msize), ns
   dim[1] = m.dim[1];
 }
 
+// Elementwise operators: host passes over the reference's host-resident
+// Matrix (it calls zaxpy / zscal there), split over the hardware threads.
+template <typename F>
+static void parallel_for(std::size_t n, F f) {
+  const std::size_t grain = (std::size_t)1 << 18;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const std::size_t nt = std::min<std::size_t>(hw, (n + grain - 1) / grain);
+  if (nt <= 1) {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const std::size_t chunk = (n + nt - 1) / nt;
+  for (std::size_t t = 0; t < nt; ++t) {
+    const std::size_t a = t * chunk, b = std::min(n, a + chunk);
+    if (a < b) th.emplace_back(f, a, b);
+  }
+  for (auto& t : th) t.join();
+}
+
 Matrix operator+(const Matrix& lhs, const Matrix& rhs) {
   if (lhs.dim[0] != rhs.dim[0] || lhs.dim[1] != rhs.dim[1]) throw ArrayMismatch();
   Matrix r(rhs);
-  for (std::size_t i = 0; i < r.data->size(); ++i) (*r.data)[i] += (*lhs.data)[i];
+  complex* d = &(*r.data)[0];
+  const complex* a = &(*lhs.data)[0];
+  parallel_for(r.data->size(), [=](std::size_t b, std::size_t e) {
+    for (std::size_t i = b; i < e; ++i) d[i] += a[i];
+  });
   return r;
 }
 Matrix operator-(const Matrix& lhs, const Matrix& rhs) {
   if (lhs.dim[0] != rhs.dim[0] || lhs.dim[1] != rhs.dim[1]) throw ArrayMismatch();
   Matrix r(lhs);
-  for (std::size_t i = 0; i < r.data->size(); ++i) (*r.data)[i] -= (*rhs.data)[i];
+  complex* d = &(*r.data)[0];
+  const complex* a = &(*rhs.data)[0];
+  parallel_for(r.data->size(), [=](std::size_t b, std::size_t e) {
+    for (std::size_t i = b; i < e; ++i) d[i] -= a[i];
+  });
   return r;
 }
 Matrix operator*(const Matrix& lhs, const complex& alpha) {
   Matrix r(lhs);
-  for (auto& v : *r.data) v *= alpha;
+  complex* d = &(*r.data)[0];
+  parallel_for(r.data->size(), [=](std::size_t b, std::size_t e) {
+    for (std::size_t i = b; i < e; ++i) d[i] *= alpha;
+  });
   return r;
 }
 Matrix operator*(const complex& alpha, const Matrix& rhs) { return rhs * alpha; }
 Matrix operator*(const Matrix& lhs, const double& alpha) {
   Matrix r(lhs);
-  for (auto& v : *r.data) v *= alpha;
+  complex* d = &(*r.data)[0];
+  parallel_for(r.data->size(), [=](std::size_t b, std::size_t e) {
+    for (std::size_t i = b; i < e; ++i) d[i] *= alpha;
+  });
   return r;
 }
 Matrix operator*(const double& alpha, const Matrix& rhs) { return rhs * alpha; }
 
+// Matrix product on the GPU (bem2d_matmul): the reference calls cblas_zgemm
 Matrix operator*(const Matrix& lhs, const Matrix& rhs) {
   if (lhs.dim[1] != rhs.dim[0]) throw ArrayMismatch();
   const int m = lhs.dim[0], n = rhs.dim[1], k = lhs.dim[1];
   Matrix r(m, n);
-  const complex* a = &(*lhs.data)[0];
-  const complex* b = &(*rhs.data)[0];
-  complex* c = &(*r.data)[0];
-  for (int j = 0; j < n; ++j)
-    for (int p = 0; p < k; ++p) {
-      const complex bpj = b[p + (size_t)k * j];
-      if (bpj == complex(0)) continue;
-      for (int i = 0; i < m; ++i) c[i + (size_t)m * j] += a[i + (size_t)m * p] * bpj;
-    }
+  detail::check(bem2d_matmul(detail::ctx(), m, n, k, &(*lhs.data)[0], m, &(*rhs.data)[0], k,
+                             &(*r.data)[0], m),
+                "Matrix product");
   return r;
 }
 
@@ -119,8 +150,13 @@ void Eigenvalues(const Matrix& k, pcvector& evalues) {
   detail::check(bem2d_eigenvalues(detail::ctx(), n, &(*k.data)[0], n, &(*evalues)[0]),
                 "Eigenvalues");
 }
-void Eigenvalues(const Matrix&, pcvector&, pMatrix&) {
-  throw UnsupportedError("Eigenvalues with eigenvectors (zgeev 'V') is not available in this build");
+void Eigenvalues(const Matrix& k, pcvector& evalues, pMatrix& evectors) {
+  const int n = k.dim[0];
+  evalues = pcvector(new cvector(n));
+  evectors = pMatrix(new Matrix(n));
+  detail::check(bem2d_eigenvectors(detail::ctx(), n, &(*k.data)[0], n, &(*evalues)[0],
+                                   &(*evectors->data)[0], n),
+                "Eigenvalues");
 }
 
 Matrix ChangeBasis(const Matrix& k, const Matrix& m) {

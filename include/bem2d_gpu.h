@@ -198,6 +198,19 @@ int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
 int bem2d_solve_system_noalloc(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
                                const void* b, void* x, bem2d_solve_info* info);
 
+/* Host-side layout check of bem2d_solve_system_noalloc (no counterpart in
+ * the reference): 1 if every work buffer of the largest accepted order
+ * BEM2D_NOALLOC_MAX_N fits the static array, else 0; *total and *capacity
+ * (may be NULL) receive the bytes needed and the array's size.  No GPU
+ * work. */
+int bem2d_noalloc_scratch_fits(int64_t* total, int64_t* capacity);
+
+/* C = A B (complex128; C m x n, A m x k, B k x n, column-major, host or
+ * device): replaces Matrix * Matrix (lib/bem2d_mathroutines.cpp:190-206,
+ * cblas_zgemm).  FP64 on the CUDA cores (64 x 64 tiles). */
+int bem2d_matmul(bem2d_ctx* ctx, int m, int n, int k, const void* A, int64_t lda, const void* B,
+                 int64_t ldb, void* C, int64_t ldc);
+
 /* ---- norms, change of basis, numerical range, potentials --------------- */
 /* out = U^{-H} K U^{-1} where M = U^H U: replaces ChangeBasis
  * (lib/bem2d_mathroutines.cpp:534-588, zpotrf + two ztrsm).  M must be block
@@ -216,6 +229,19 @@ int bem2d_change_basis(bem2d_ctx* ctx, int n, const void* K, int64_t ldk, const 
  * estimates change by less than tol (tol <= 0 selects 1e-13). */
 int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
                        double* norm, double* cond);
+
+/* bem2d_l2_norm_cond with a choice of arithmetic for sigma_min (the same
+ * routine of the reference, lib/bem2d_mathroutines.cpp:208-266):
+ * BEM2D_PREC_FP64: as bem2d_l2_norm_cond (complex128 LU);
+ * BEM2D_PREC_MIXED: complex64 LU (tensor-core trailing updates); the Lanczos
+ *   iteration on A^{-1} first runs with unrefined complex64 solves until its
+ *   estimate settles, then again from that Ritz vector with every product
+ *   with A^{-1} or A^{-H} refined with FP64 residuals of A until its backward
+ *   error reaches FP64 roundoff or stops halving, so the final iteration sees
+ *   the operator to FP64 accuracy.  The Lanczos arithmetic is FP64 in both
+ *   modes. */
+int bem2d_l2_norm_cond_prec(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
+                            int precision, double* norm, double* cond);
 
 /* Largest order bem2d_hermitian_eigenvalues accepts (its workspace holds an
  * n x n complex128 matrix: 4.3 GB at the limit); bem2d_singular_values
@@ -252,6 +278,19 @@ int bem2d_singular_values(bem2d_ctx* ctx, int n, const void* A, int64_t lda, dou
  * limit 30 max(10, n) is reached.  A: host or device (not modified);
  * w: host or device. */
 int bem2d_eigenvalues(bem2d_ctx* ctx, int n, const void* A, int64_t lda, void* w);
+
+/* w[0..n-1] (complex128) and the right eigenvectors vr (n x n, ldvr,
+ * complex128, column i for w[i]) of the general complex A: replaces
+ * Eigenvalues(const Matrix&, pcvector&, pMatrix&)
+ * (lib/bem2d_mathroutines.cpp:468-528, zgeev with jobvr = 'V').  The
+ * reduction's reflectors and the QR rotations are accumulated into the
+ * Schur vectors Z (A = Z T Z^H, T upper triangular, w[i] = T(i, i)); the
+ * eigenvectors of T by back substitution (ztrevc's scheme), X = Z Y, each
+ * column scaled to unit 2-norm with its largest entry real and positive
+ * (zgeev's normalisation).  Limits and order as bem2d_eigenvalues; A, w, vr
+ * host or device. */
+int bem2d_eigenvectors(bem2d_ctx* ctx, int n, const void* A, int64_t lda, void* w, void* vr,
+                       int64_t ldvr);
 
 /* lmax[j] = largest eigenvalue of (e^{i th_j} A + e^{-i th_j} A^H) / 2 for
  * nang angles th_j: the eigenvalue step of NumRange
@@ -320,6 +359,23 @@ int bem2d_fma_peak(int precision, double* tflops);
 #define BEM2D_PHASE_SOLVE 3
 int bem2d_ctx_enable_timers(bem2d_ctx* ctx, int enable);
 int bem2d_ctx_timer(const bem2d_ctx* ctx, int phase, double* ms, int64_t* count);
+
+/* Failure-detection check of the bounded device waits (no counterpart in
+ * the reference; its LAPACK calls cannot time out).  Runs one complex64 LU
+ * panel of order n (256 <= n <= 4096) on the cooperative-grid panel kernel
+ * with two blocks whose waits expect a third block's candidate, which is
+ * never posted; every wait gives up after `polls` polls and the kernel
+ * returns.  Returns BEM2D_ERR_TIMEOUT when the waits gave up (the expected
+ * outcome), BEM2D_OK if they did not.  The context stays usable: the next
+ * factorisation clears the status word. */
+int bem2d_debug_panel_timeout(bem2d_ctx* ctx, int n, int polls);
+
+/* C -= A B for complex64 column-major device matrices (C M x N, A M x K,
+ * B K x N) through the complex64 LU's tensor-core trailing update
+ * (tcgen05 kind::tf32, 3xTF32 split): the update of zgetrf's right-looking
+ * step (lib/bem2d_mathroutines.cpp:345) exposed for its own parity test. */
+int bem2d_debug_tc_update(bem2d_ctx* ctx, int M, int N, int K, void* C, int64_t ldc,
+                          const void* A, int64_t lda, const void* B, int64_t ldb);
 
 #ifdef __cplusplus
 }

@@ -33,6 +33,15 @@ def test_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == names
 
 
+def test_noalloc_layout_fits_at_the_limit(lib):
+    """The allocation-free solve's work buffers for n = BEM2D_NOALLOC_MAX_N
+    fit its static device array (host-side arithmetic only)."""
+    from bem2d_gb300 import capi
+    fits, need, cap = capi.noalloc_scratch_fits()
+    assert fits, (need, cap)
+    assert 16 * capi.NOALLOC_MAX_N ** 2 < need <= cap
+
+
 def test_gauss_host_rule_matches_oracle(lib):
     from bem2d_gb300 import capi, _build
     from oracle import oracle as O

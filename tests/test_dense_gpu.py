@@ -127,3 +127,17 @@ def test_potential_matches_oracle(ctx, kernel):
     out = ctx.potential(g, c, pts, kernel, 7.0, 3.0)
     ref = O.potential(g, c, pts, kernel, 7.0, 3.0)
     assert rel(out, ref) < 1e-12
+
+
+@pytest.mark.parametrize("m,n,k", [(1, 1, 1), (64, 64, 64), (300, 17, 129), (1000, 700, 1500),
+                                   (2048, 2048, 2048)])
+def test_matmul_matches_numpy(ctx, m, n, k):
+    """Matrix * Matrix (cblas_zgemm in the reference): complex128 product on
+    the GPU within 1e-14 sqrt(k) of numpy's, relative to |A| |B|."""
+    rng = np.random.default_rng(m + 3 * n + 7 * k)
+    A = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    C = ctx.matmul(A, B)
+    R = A @ B
+    scale = np.abs(A) @ np.abs(B)
+    assert (np.abs(C - R) / scale).max() < 1e-14 * max(1, k ** 0.5)

@@ -174,3 +174,69 @@ def test_eigenvalues_boundary_element_matrix(ctx):
     B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
     w = ctx.eigenvalues(B)
     assert match_err(w, np.linalg.eigvals(B)) <= 1e-11 * np.linalg.norm(B, 2)
+
+
+def _zgeev_normalised(V):
+    """zgeev's normalisation of eigenvector columns: unit 2-norm, the first
+    entry of largest modulus real and positive."""
+    V = V / np.linalg.norm(V, axis=0)
+    k = np.argmax(np.abs(V) ** 2, axis=0)
+    ph = V[k, np.arange(V.shape[1])]
+    return V * (np.conj(ph) / np.abs(ph))
+
+
+def _check_eigenvectors(A, w, V, tol_res, tol_vec=None):
+    """Residuals |A v - lambda v| <= tol_res |A|_2 for every pair, unit
+    columns with a real positive largest entry, the eigenvalues as a set
+    against LAPACK's zgeev, and (tol_vec) each vector against LAPACK's for
+    eigenvalues separated from the rest by at least 1e-3 |A|_2."""
+    n = A.shape[0]
+    nrm = np.linalg.norm(A, 2) if n else 1.0
+    R = A @ V - V * w[None, :]
+    assert np.abs(np.linalg.norm(V, axis=0) - 1).max() < 1e-13
+    k = np.argmax(np.abs(V) ** 2, axis=0)
+    top = V[k, np.arange(n)]
+    assert np.abs(top.imag).max() == 0 and (top.real > 0).all()
+    assert (np.linalg.norm(R, axis=0) / max(nrm, 1e-300)).max() <= tol_res
+    wl, Vl = np.linalg.eig(A)
+    assert match_err(w, wl) <= 1e-11 * max(nrm, 1e-300)
+    if tol_vec is not None:
+        Vl = _zgeev_normalised(Vl)
+        for i in range(n):
+            j = int(np.argmin(np.abs(wl - w[i])))
+            gap = np.partition(np.abs(w - w[i]), 1)[1] if n > 1 else np.inf
+            if gap < 1e-3 * nrm:
+                continue
+            assert np.linalg.norm(V[:, i] - Vl[:, j]) <= tol_vec * nrm / gap, (i, gap)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 10, 64, 200])
+def test_eigenvectors_random(ctx, n):
+    rng = np.random.default_rng(300 + n)
+    A = crandn(rng, n, n)
+    w, V = ctx.eigenvectors(A)
+    _check_eigenvectors(A, w, V, 1e-13 * max(1, n) ** 0.5, 1e-12)
+
+
+def test_eigenvectors_triangular_and_diagonal(ctx):
+    rng = np.random.default_rng(9)
+    T = np.triu(crandn(rng, 30, 30))
+    w, V = ctx.eigenvectors(T)
+    _check_eigenvectors(T, w, V, 1e-13)
+    D = np.diag(np.arange(1, 9) + 0.5j)
+    w, V = ctx.eigenvectors(D)
+    P = np.abs(V)  # a permutation: one unit entry per column, matching w
+    assert np.abs(P.max(axis=0) - 1).max() < 1e-15 and np.abs(P.sum(axis=0) - 1).max() < 1e-14
+    assert np.abs(w - np.diag(D)[np.argmax(P, axis=0)]).max() < 1e-15
+
+
+def test_eigenvectors_boundary_element_matrix(ctx):
+    """squaredensity.cpp's call: Eigenvalues(ChangeBasis(A, Id), w, V) on the
+    boundary-element matrix (eigenvalues cluster near 1, a compact
+    perturbation of the identity)."""
+    spec = CASES["square_numrange"]
+    g = spec["geom"]()
+    A = ctx.discrete_kernel(g, "combined", spec["k"], spec["eta"], QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    w, V = ctx.eigenvectors(B)
+    _check_eigenvectors(B, w, V, 1e-13, 1e-11)

@@ -67,6 +67,21 @@ def test_two_calls_match_solve_system(ctx):
     assert rel(x2, g["x"]) < TOL  # the reference's own LAPACK solution
 
 
+def test_largest_order(ctx):
+    """n = BEM2D_NOALLOC_MAX_N, the order whose work buffers come closest to
+    the size of the static array: the host-side layout check says they fit,
+    and the solution matches bem2d_solve_system and LAPACK."""
+    from bem2d_gb300 import capi
+    fits, need, cap = capi.noalloc_scratch_fits()
+    assert fits and need <= cap, (need, cap)
+    n = capi.NOALLOC_MAX_N
+    A, b = rand_system(n, 7)
+    x = ctx.solve_noalloc(A, b)
+    assert ctx.last_info[0] == 0
+    assert rel(x, ctx.solve(A, b, "fp64")) < TOL
+    assert rel(x, np.linalg.solve(A, b)) < TOL
+
+
 def test_rejects_n_above_limit(ctx):
     from bem2d_gb300 import capi
     n = capi.NOALLOC_MAX_N + 1
