@@ -204,18 +204,125 @@ AUX = {
                     "ChangeBasis(A, Id), lambda_max of the Hermitian part at 360 angles",
 }
 
+# DRAM bytes (read + write) per launch of the far-field kernel, from an ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the mixed assembly
+# of the sweep's largest problem (ellipse, N = 3084); the file under
+# profiles/ named traffic_far_ff_kernel_ellipse3084.txt holds the command.
+TRAFFIC = {"far_ellipse3084": None}
 
-def run_aux(args):
-    """Norm / condition (graded square, N = 8192, k = 200) and numerical range
-    (unit square, N = 2048, k = 50, 360 angles):
-    one step = mixed assembly + ChangeBasis(A, Id) + the study, through the C
-    ABI.  The results are checked once, untimed, against dense cuSOLVER
-    spectra (torch.linalg)."""
+
+def measured_peaks():
+    """HBM copy bandwidth and cuBLAS bf16 throughput measured on this GPU
+    model (MEASURED_PEAKS.json beside this script), else the fallback figures
+    of an earlier GB300 measurement."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        d["source"] = "measured"
+        return d
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "source": "fallback"}
+
+
+def far_roofline(n, far_ms, fp32_peak, key=None):
+    """The float-float far field against the FP32 FMA pipe: 100 flops per
+    kernel evaluation (the frozen convention), 25 (N^2 - 3N) evaluations per
+    assembly.  Algorithmic DRAM bytes: the complex128 entries written
+    (16 N^2) plus their complex64 copy (8 N^2)."""
+    flops = 100.0 * 25 * (n * n - 3 * n)
+    ach = flops / (far_ms * 1e-3) / 1e12
+    return {"bound": "fp32", "kernel": "far_ff_kernel + deferred_ff_kernel",
+            "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+            "peak_source": "bem2d_fma_peak: FP32 FMA throughput measured in this run "
+                           "(MEASURED_PEAKS.json has no FP32 figure)",
+            "traffic": TRAFFIC.get(key) if key else None,
+            "algorithmic_bytes": 24.0 * n * n,
+            "note": "N=%d; 25 (N^2-3N) evaluations x 100 flops per launch; traffic = ncu "
+                    "dram bytes read+write per far-field launch at this N (null: not captured)"
+                    % n}
+
+
+def lu_roofline(n, lu_ms, peaks):
+    """The complex64 LU against the TF32 tensor peak (half the measured bf16
+    rate): 8N^3/3 real flops per factorisation (zgetrf's count).  The
+    trailing update issues each product as three TF32 MMAs (hi*hi, hi*lo,
+    lo*hi), so the tensor pipe executes about 3x the algorithmic flops."""
+    flops = 8.0 * n ** 3 / 3.0
+    ach = flops / (lu_ms * 1e-3) / 1e12
+    peak = peaks["bf16_tflops"] / 2.0
+    return {"bound": "tensor", "kernel": "complex64 LU (panels, trsm, tcgen05 trailing update)",
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "peak_source": "TF32 dense = bf16 burst / 2, bf16 %s (MEASURED_PEAKS.json)"
+                           % peaks["source"],
+            "traffic": None,
+            "note": "N=%d; 8N^3/3 flops per factorisation; 3xTF32 split issues 3x" % n}
+
+
+class Stepper:
+    """Device-timed steps on the library's stream: a 256 MB L2 flush before
+    each step (outside the events), then events around the host-synchronous
+    call."""
+
+    def __init__(self, ctx, ws=1):
+        import torch
+        self.torch = torch
+        self.ws = ws
+        self.stream = torch.cuda.ExternalStream(ctx.stream)
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier(self):
+        self.torch.cuda.synchronize()
+        if self.ws > 1:
+            self.torch.distributed.barrier()
+
+    def run(self, fn, k, warm):
+        torch = self.torch
+        if callable(warm):
+            warm()
+        else:
+            for _ in range(warm):
+                fn()
+        self.barrier()
+        ms = []
+        for _ in range(k):
+            self.flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(self.stream):
+                e0.record()
+            fn()
+            with torch.cuda.stream(self.stream):
+                e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        self.barrier()
+        return ms
+
+
+def device_ms(fn):
+    """Event time (ms) of one host-synchronous call."""
     import torch
-    from bem2d_gb300 import capi
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    out = fn()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def aux_record(ctx, name, steps, warmup, check=True):
+    """Norm / condition (graded square, N = 8192, k = 200) and numerical range
+    (unit square, N = 2048, k = 50, 360 angles): one step = mixed assembly +
+    ChangeBasis(A, Id) + the study, through the C ABI.  The plain FP64 study
+    is timed beside it; results are checked once, untimed, against dense
+    cuSOLVER spectra (torch.linalg)."""
+    import torch
     from bem2d_gb300 import geometry as G
-    ctx = capi.Context(0)
-    if args.workload == "square8192_normcond":
+    if name == "square8192_normcond":
         g = G.graded_square(2032, 8, 0.15).add_poly_basis(0)
         k = 200.0
     else:
@@ -230,85 +337,92 @@ def run_aux(args):
     B = torch.empty((n, n), dtype=torch.complex128, device=dev)
     bstart = np.arange(n + 1, dtype=np.int32)  # P0: 1 x 1 mass blocks
     thetas = 2 * np.pi * np.arange(360) / 360.0
+    normcond = name == "square8192_normcond"
+
+    def study(prec):
+        if normcond:
+            return ctx.norm_cond(B, precision=prec)
+        return ctx.num_range_lmax(B, thetas, tol=NR_TOL, precision=prec)
+
     ph = {}
 
     def step():
         t = []
-        for name, fn in (
+        for nm, fn in (
                 ("assembly", lambda: ctx.discrete_kernel_mixed(arrays, "combined", k, k, QUAD,
                                                                2.0, 1.0, out=A, out32=A32)),
                 ("change_basis", lambda: (ctx.eval_ident(arrays, QUAD, out=M),
                                           ctx.change_basis(A, M, bstart, out=B))),
-                ("study", lambda: ph.__setitem__(
-                    "out", ctx.norm_cond(B) if args.workload == "square8192_normcond"
-                    else ctx.num_range_lmax(B, thetas, tol=NR_TOL, precision="mixed")))):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record()
-            fn()
-            e1.record()
-            e1.synchronize()
-            t.append((name, e0.elapsed_time(e1)))
+                ("study", lambda: ph.__setitem__("out", study("mixed")))):
+            t.append((nm, device_ms(fn)[0]))
         return t
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
-    runs = [step() for _ in range(args.steps)]
+    runs = [step() for _ in range(steps)]
     ms = [sum(v for _, v in r) for r in runs]
-    phases = {name: sum(r[i][1] for r in runs) / len(runs) for i, (name, _) in enumerate(runs[0])}
+    phases = {nm: sum(r[i][1] for r in runs) / len(runs) for i, (nm, _) in enumerate(runs[0])}
+    study("fp64")  # warm the FP64 path's workspace
+    t64, out64 = device_ms(lambda: study("fp64"))
+    pre = phases["assembly"] + phases["change_basis"]
+    res = {"metric": "norm-cond evaluations/s" if normcond else "numerical-range scans/s",
+           "value": 1e3 * len(ms) / sum(ms), "unit": "1/s", "n_gpus": 1, "steps": steps,
+           "warmup": warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True,
+           "dtype": "mixed assembly; sigma_min by c64 Lanczos on complex64 LU solves, then "
+                    "f64 Lanczos on refined solves from its Ritz vector" if normcond else
+                    "mixed assembly; c64 Lanczos, then f64 Lanczos from its Ritz vectors",
+           "data": "synthetic", "config": {"workload": AUX[name], "n_unknowns": n},
+           "phases_ms": phases,
+           "plain_fp64": {"study_ms": t64, "value": 1e3 / (t64 + pre), "unit": "1/s",
+                          "dtype": "f64 assembly products, complex128 LU / Lanczos"},
+           "mixed_over_fp64_study": t64 / phases["study"]}
     Bt = B.T  # the column-major matrix as a torch view
-    res = {"metric": "norm-cond evaluations/s" if args.workload == "square8192_normcond"
-           else "numerical-range scans/s",
-           "value": 1e3 * len(ms) / sum(ms), "unit": "1/s", "n_gpus": 1, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True,
-           "dtype": "mixed assembly; f64 Lanczos on the complex128 operator"
-           if args.workload == "square8192_normcond" else
-           "mixed assembly; c64 Lanczos, then f64 Lanczos from its Ritz vectors",
-           "data": "synthetic", "config": {"workload": AUX[args.workload], "n_unknowns": n},
-           "phases_ms": phases}
-    if args.workload == "square8192_normcond":
+    if normcond:
         nrm, cond = ph["out"]
-        sv = torch.linalg.svdvals(Bt)
-        smax, smin = float(sv[0]), float(sv[-1])
+        nrm64, cond64 = out64
         res["result"] = {"norm": nrm, "norm_inv": cond / nrm, "cond": cond}
-        res["rel_err_vs_dense_svd"] = {"norm": abs(nrm - smax) / smax,
-                                      "norm_inv": abs(cond / nrm - 1 / smin) * smin,
-                                      "cond": abs(cond - smax / smin) / (smax / smin)}
+        res["mixed_vs_fp64_rel_err"] = {"norm": abs(nrm - nrm64) / nrm64,
+                                        "cond": abs(cond - cond64) / cond64}
+        if check:
+            # dense check: the extreme eigenvalues of B^H B (cuSOLVER zheevd)
+            ev = torch.linalg.eigvalsh(Bt.conj().T @ Bt)
+            smax, smin = float(ev[-1]) ** 0.5, float(ev[0]) ** 0.5
+            res["rel_err_vs_dense_eig_BhB"] = {
+                "norm": abs(nrm - smax) / smax, "norm_inv": abs(cond / nrm - 1 / smin) * smin,
+                "cond": abs(cond - smax / smin) / (smax / smin),
+                "note": "sigma = sqrt(eig(B^H B)): sigma_min to ~eps cond^2 relative, "
+                        "so the sigma_min comparison is only as good as that"}
     else:
-        lm = ph["out"]
-        # the plain FP64 path (complex128 Lanczos from the start), timed once
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        lm64 = ctx.num_range_lmax(B, thetas, tol=NR_TOL, precision="fp64")
-        e1.record()
-        e1.synchronize()
-        t64 = e0.elapsed_time(e1)
-        res["plain_fp64"] = {"study_ms": t64, "value": 1e3 / (t64 + phases["assembly"] +
-                                                              phases["change_basis"]),
-                             "unit": "1/s"}
-        res["mixed_over_fp64_study"] = t64 / phases["study"]
+        lm, lm64 = ph["out"], out64
         res["mixed_vs_fp64_max_rel_err"] = float(np.max(np.abs(lm - lm64)) / np.max(np.abs(lm64)))
-        errs, errs64 = [], []
-        for j in range(0, 360, 45):
-            z = complex(np.cos(thetas[j]), np.sin(thetas[j]))
-            H = 0.5 * (z * Bt + np.conj(z) * Bt.conj().T)
-            ev = float(torch.linalg.eigvalsh(H)[-1])
-            errs.append(abs(lm[j] - ev) / max(abs(ev), 1e-300))
-            errs64.append(abs(lm64[j] - ev) / max(abs(ev), 1e-300))
         res["result"] = {"lambda_max_min": float(np.min(lm)), "lambda_max_max": float(np.max(lm))}
         res["config"]["tol"] = NR_TOL
-        res["max_rel_err_vs_dense_eigvalsh"] = max(errs)
-        res["plain_fp64"]["max_rel_err_vs_dense_eigvalsh"] = max(errs64)
-        res["checked_angles"] = 8
-    print(json.dumps(res))
+        if check:
+            errs, errs64 = [], []
+            for j in range(0, 360, 45):
+                z = complex(np.cos(thetas[j]), np.sin(thetas[j]))
+                H = 0.5 * (z * Bt + np.conj(z) * Bt.conj().T)
+                ev = float(torch.linalg.eigvalsh(H)[-1])
+                errs.append(abs(lm[j] - ev) / max(abs(ev), 1e-300))
+                errs64.append(abs(lm64[j] - ev) / max(abs(ev), 1e-300))
+            res["max_rel_err_vs_dense_eigvalsh"] = max(errs)
+            res["plain_fp64"]["max_rel_err_vs_dense_eigvalsh"] = max(errs64)
+            res["checked_angles"] = 8
+    del A, A32, M, B
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_aux(args):
+    from bem2d_gb300 import capi
+    ctx = capi.Context(0)
+    print(json.dumps(aux_record(ctx, args.workload, args.steps, args.warmup)))
 
 
 def run_only(args):
-    """Profiling driver: one phase only (assembly or solve) of the largest
-    problem of the workload, or the whole mixed sweep; no JSON line."""
+    """Profiling driver: one phase only (assembly, mixed assembly or solve)
+    of the largest problem of the workload, or the whole mixed sweep; no JSON
+    bench line."""
     import torch
     from bem2d_gb300 import capi
     w = workload(args.workload)
@@ -319,7 +433,9 @@ def run_only(args):
     ctx = capi.Context(0)
     ctx.enable_timers(args.only != "sweep")
     A = torch.empty((n, n), dtype=torch.complex128, device="cuda") \
-        if args.only == "assembly" else None
+        if args.only in ("assembly", "assembly_mixed") else None
+    A32 = torch.empty((n, n), dtype=torch.complex64, device="cuda") \
+        if args.only == "assembly_mixed" else None
     x = torch.zeros(n, dtype=torch.complex128, device="cuda")
     if args.only == "sweep":  # as the headline: geometry staged once, device results
         holds = [capi._GeomHold(p[0]) for p in probs]
@@ -332,6 +448,8 @@ def run_only(args):
         e0.record()
         if args.only == "assembly":
             ctx.discrete_kernel(arrays, "combined", k, eta, QUAD, 2.0, 1.0, out=A)
+        elif args.only == "assembly_mixed":
+            ctx.discrete_kernel_mixed(arrays, "combined", k, eta, QUAD, 2.0, 1.0, out=A, out32=A32)
         elif args.only == "sweep":
             ctx.sweep_solve(holds, [p[1] for p in probs], w["d"], [p[2] for p in probs], QUAD,
                             "mixed", nworkers=args.workers, outs=outs)
@@ -347,20 +465,50 @@ def run_only(args):
                       "timers_ms": {k: v[0] / max(v[1], 1) for k, v in ctx.timers().items()}}))
 
 
-def run_ours(args):
+def lshape_cpu_leg(g, k, eta, threads, A_dev):
+    """CPU baseline for the graded L-shape (N = 16384), where the oracle needs
+    hours for a whole solve: 64 seeded rows of the oracle's assembly (timed,
+    scaled by N/64, and compared with the GPU's rows) plus scipy's LAPACK
+    zgetrf + zgetrs on a seeded random N/2 system (timed, scaled by 8 = the
+    N^3 ratio)."""
+    import scipy.linalg as sl
+    from oracle import oracle as O
+    from bem2d_gb300 import _build
+    _build.build_oracle(with_reference=False)
+    n = g.n_unknowns
+    rows = np.sort(np.random.default_rng(0).choice(n, 64, replace=False))
+    t0 = time.perf_counter()
+    R = O.discrete_kernel_rows(g, rows, "combined", k, eta, QUAD, alpha=2.0, beta=1.0,
+                               threads=threads)
+    t_rows = time.perf_counter() - t0
+    G = A_dev.T[rows.tolist()].cpu().numpy()  # rows of the column-major matrix
+    row_err = float(np.linalg.norm(G - R) / np.linalg.norm(R))
+    m = n // 2
+    rng = np.random.default_rng(1)
+    M = rng.standard_normal((m, m)) + 1j * rng.standard_normal((m, m))
+    b = rng.standard_normal(m) + 0j
+    t0 = time.perf_counter()
+    lu = sl.lu_factor(M, overwrite_a=True, check_finite=False)
+    sl.lu_solve(lu, b, check_finite=False)
+    t_lu = time.perf_counter() - t0
+    secs = t_rows * n / 64.0 + 8.0 * t_lu
+    return {"value": 1.0 / secs, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": "64 seeded rows of the oracle's assembly (%.2f s, x N/64) + scipy "
+                      "LAPACK zgetrf/zgetrs at N/2=%d (%.2f s, x 8): %.1f s per solve"
+                      % (t_rows, m, t_lu, secs)}, row_err
+
+
+def solve_record(ctx, args, wname, steps, warmup, ws=1, rank=0, sub=False):
+    """Scattering solves of one workload through the C ABI: the mixed path
+    device-resident (value), end to end with host results (e2e), the plain
+    FP64 path, per-phase events of the largest problem and the rooflines.
+    `sub`: a secondary record inside the headline line (fewer legs)."""
     import torch
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.set_device(local)
     from bem2d_gb300 import capi
-    w = workload(args.workload)
+    w = workload(wname)
     probs = w["problems"]
     P = len(probs)
-    ctx = capi.Context(local)
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    st = Stepper(ctx, ws)
     holds = [capi._GeomHold(g.arrays()) for g, _, _ in probs]
     ks = [p[1] for p in probs]
     etas = [p[2] for p in probs]
@@ -371,34 +519,6 @@ def run_ours(args):
     x_fp64 = [torch.zeros(n, dtype=torch.complex128, device="cuda") for n in ns]
     h2d = sum(a.nbytes for h in holds for a in h.arrays.values()) + 16 * P
     d2h = 16 * sum(ns)
-
-    def barrier():
-        torch.cuda.synchronize()
-        if ws > 1:
-            torch.distributed.barrier()
-
-    def timed(fn, k, warm):
-        if callable(warm):
-            warm()
-        else:
-            for _ in range(warm):
-                fn()
-        barrier()
-        ms = []
-        for _ in range(k):
-            flush.zero_()  # L2 flush, outside the timed events
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                e0.record()
-            fn()  # host-synchronous: returns when every problem is solved
-            with torch.cuda.stream(stream):
-                e1.record()
-            e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-        barrier()
-        return ms
 
     def mixed(outs):
         if P == 1:
@@ -418,23 +538,24 @@ def run_ours(args):
         ctx.scattering_solve(holds[big].arrays, ks[big], w["d"], etas[big], QUAD,
                              precision="fp64", out=x_fp64[big])
 
-    # -- headline: mixed path, device-resident results ------------------------
+    # -- mixed path, device-resident results ----------------------------------
     clk_path = os.path.join(os.environ.get("BEM2D_CLOCKS_DIR", os.path.join(ROOT, "_build")),
-                            "bench_clocks_%d.csv" % rank)
+                            "bench_clocks_%s_%d.csv" % (wname, rank))
     os.makedirs(os.path.dirname(clk_path), exist_ok=True)
     cp, cf = clocks_start(clk_path)
     l0 = ctx.launches
-    ms_mixed = timed(mixed(x_dev), args.steps, args.warmup)
-    launches = (ctx.launches - l0) // (args.steps + args.warmup) * args.steps
-    clocks = clocks_stop(cp, cf, clk_path, local)
+    ms_mixed = st.run(mixed(x_dev), steps, warmup)
+    launches = (ctx.launches - l0) // (steps + warmup) * steps
+    clocks = clocks_stop(cp, cf, clk_path, torch.cuda.current_device())
     infos = ctx.sweep_infos if P > 1 else [ctx.last_info]
     # -- e2e: host results (device -> host copies inside the timed region) ----
-    ms_e2e = timed(mixed(x_host), args.steps, 1)
+    ms_e2e = st.run(mixed(x_host), steps, 1)
     # -- plain FP64 GPU path, one problem after another -----------------------
-    fp64_steps = 1 if P > 1 or ns[0] > 8192 else max(2, args.steps // 2)
-    ms_fp64 = timed(fp64_all, fp64_steps, fp64_warm)
+    fp64_steps = 1 if P > 1 or ns[0] > 8192 else max(2, steps // 2)
+    ms_fp64 = st.run(fp64_all, fp64_steps, fp64_warm)
     errs = [float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
             for a, b in zip(x_dev, x_fp64)]
+
     # -- phases of the largest problem (events around each phase) -------------
     def phases(prec):
         ctx.enable_timers(True)
@@ -444,39 +565,24 @@ def run_ours(args):
         ctx.enable_timers(False)
         return {k: v[0] for k, v in t.items()}
 
-    ph_mixed, ph_fp64 = phases("mixed"), phases("fp64")
+    ph_mixed = phases("mixed")
+    ph_fp64 = phases("fp64") if ns[big] <= 8192 else None
     nb = ns[big]
+    peaks = measured_peaks()
     fp32_peak = capi.fma_peak("mixed")
-    lu_flops = 8.0 * nb ** 3 / 3.0
-    far_flops = 100.0 * 25 * (nb * nb - 3 * nb)
-    roof = {
-        "lu": {"bound": "fp32", "kernel": "complex64 LU (panels, trsm, tcgen05 trailing update)",
-               "achieved": lu_flops / (ph_mixed["lu"] * 1e-3) / 1e12,
-               "note": "8N^3/3 real flops (zgetrf count) per factorisation, N=%d; peak shown "
-                       "is the FP32 CUDA-core pipe, the trailing update runs on the tensor "
-                       "cores" % nb},
-        "far": {"bound": "fp32", "kernel": "far_ff_kernel + deferred_ff_kernel",
-                "achieved": far_flops / (ph_mixed["far"] * 1e-3) / 1e12,
-                "note": "100 flops per kernel evaluation (frozen convention), "
-                        "25 (N^2-3N) evaluations per launch, N=%d" % nb},
-    }
-    for r in roof.values():
-        r.update(peak=fp32_peak, unit="TFLOP/s", frac=r["achieved"] / fp32_peak, traffic=None)
-    # the far-field kernels are the path's throughput-bound hot spot (the LU
-    # panels, the largest share at these sizes, are bound by latency);
-    # the LU line follows as roofline_other
-    dom = "far"
+    key = "far_%s%d" % ("ellipse" if wname.startswith("ellipse") else wname.rstrip("0123456789"),
+                        nb)
+    roof_far = far_roofline(nb, ph_mixed["far"], fp32_peak, key)
+    roof_lu = lu_roofline(nb, ph_mixed["lu"], peaks)
 
     t_mixed = sum(ms_mixed) / len(ms_mixed)
     t_e2e = sum(ms_e2e) / len(ms_e2e)
     t_fp64 = sum(ms_fp64) / len(ms_fp64)
     t_mixed, t_e2e, t_fp64 = max_over_ranks([t_mixed, t_e2e, t_fp64], ws, "cuda")
-    if rank != 0:
-        return
     entries = float(sum(n * n for n in ns))
     res = {
         "metric": "solves/s", "value": ws * P * 1e3 / t_mixed, "unit": "solves/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mixed,
+        "n_gpus": ws, "steps": steps, "warmup": warmup, "ms_per_step": t_mixed,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 LU + f64 refinement; float-float Bessel functions, f64 geometry",
         "data": "synthetic",
@@ -496,13 +602,38 @@ def run_ours(args):
         "refinement": {"max_iterations": max(i[1] for i in infos),
                        "max_backward_error": max(i[2] for i in infos)},
         "phases_ms_largest": {"n": nb, "mixed": ph_mixed, "fp64": ph_fp64},
-        "roofline": dict(roof[dom], phase=dom),
-        "roofline_other": dict(roof["far" if dom == "lu" else "lu"]),
+        # the far field is the path's throughput-bound hot spot; the LU
+        # (panels latency-bound, trailing update on the tensor cores) follows
+        "roofline": dict(roof_far, phase="far"),
+        "roofline_other": dict(roof_lu, phase="lu"),
     }
-    res["roofline_other"]["phase"] = "far" if dom == "lu" else "lu"
     if clocks:
         res["clocks"] = clocks
-    if not args.no_cpu and w["cpu_sample"]:
+    if P == 1 and nb > 8192:
+        # backward errors of both solutions against the FP64 system, on the device
+        g, k, eta = probs[0]
+        A = torch.empty((nb, nb), dtype=torch.complex128, device="cuda")
+        A32 = torch.empty((nb, nb), dtype=torch.complex64, device="cuda")
+        ctx.discrete_kernel_mixed(holds[0].arrays, "combined", k, eta, QUAD, 2.0, 1.0,
+                                  out=A, out32=A32)
+        del A32
+        b = torch.from_numpy(ctx.rhs(holds[0].arrays, k, w["d"], eta, QUAD)).cuda()
+        Am = A.T  # the column-major matrix
+        nA = float(torch.linalg.matrix_norm(Am))
+        nb_ = float(torch.linalg.vector_norm(b))
+
+        def berr(x):
+            return float(torch.linalg.vector_norm(b - Am @ x)) / (
+                nA * float(torch.linalg.vector_norm(x)) + nb_)
+
+        res["backward_error"] = {"mixed": berr(x_dev[0]), "fp64": berr(x_fp64[0]),
+                                 "measure": "|b - A x| / (|A|_F |x| + |b|), FP64 A"}
+        if not args.no_cpu and rank == 0:
+            threads = os.cpu_count() or 1
+            res["cpu_baseline"], res["rows_rel_err_vs_oracle"] = lshape_cpu_leg(
+                g, k, eta, threads, A)
+        del A
+    elif not args.no_cpu and w["cpu_sample"] and rank == 0:
         threads = os.cpu_count() or 1
         secs, xr = cpu_solves(w, w["cpu_sample"], threads)
         v = len(w["cpu_sample"]) / secs
@@ -515,7 +646,31 @@ def run_ours(args):
             "mixed": max(rel(x_dev[i].cpu().numpy(), xr[i]) for i in xr),
             "fp64": max(rel(x_fp64[i].cpu().numpy(), xr[i]) for i in xr),
             "problems": sorted(xr)}
-    print(json.dumps(res))
+    del x_dev, x_fp64, x_pin, x_host
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from bem2d_gb300 import capi
+    ctx = capi.Context(local)
+    res = solve_record(ctx, args, args.workload, args.steps, args.warmup, ws, rank)
+    if ws == 1 and not args.no_sub and args.workload == "ellipse_sweep256":
+        # the other single-GPU configurations of the path, each with its own
+        # FP64 comparison and checks (not part of the headline value)
+        sub = {}
+        sub["lshape16384"] = solve_record(ctx, args, "lshape16384", args.sub_steps, 3, sub=True)
+        for name in AUX:
+            sub[name] = aux_record(ctx, name, args.sub_steps, 3)
+        res["sub"] = sub
+    if rank == 0:
+        print(json.dumps(res))
 
 
 def main():
@@ -528,7 +683,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--workers", type=int, default=SWEEP_WORKERS,
                     help="concurrent problems (host workers, one stream each) of a sweep")
-    ap.add_argument("--only", choices=["assembly", "mixed", "fp64", "sweep"],
+    ap.add_argument("--no-sub", action="store_true",
+                    help="headline workload only (skip the L-shape, norm/cond and "
+                         "numerical-range records)")
+    ap.add_argument("--sub-steps", type=int, default=3,
+                    help="timed steps of each secondary record")
+    ap.add_argument("--only", choices=["assembly", "assembly_mixed", "mixed", "fp64", "sweep"],
                     help="profiling driver: run one phase, print its timers")
     args = ap.parse_args()
     if args.workload in AUX:
