@@ -209,8 +209,8 @@ def _check_eigenvectors(A, w, V, tol_res, tol_vec=None):
             gap = np.partition(np.abs(w - w[i]), 1)[1] if n > 1 else np.inf
             if gap < 1e-3 * nrm:
                 continue
-            c = abs(np.vdot(Vl[:, j], V[:, i]))  # |cos| of the angle between the lines
-            dist = np.sqrt(max(0.0, 2.0 - 2.0 * c))
+            p = np.vdot(Vl[:, j], V[:, i])  # Vl_j rotated onto V_i's phase
+            dist = np.linalg.norm(V[:, i] - (p / abs(p)) * Vl[:, j])
             assert dist <= tol_vec * nrm / gap, (i, gap, dist)
 
 
