@@ -297,7 +297,7 @@ class Context:
             b = np.ascontiguousarray(b, dtype=np.complex128)
             lda = n
         else:
-            lda = A.stride(1)
+            lda = _ld(A, n)
         info = SolveInfo_c()
         self._check(self.lib.bem2d_solve_system(self.h, n, _ptr(A), lda, _ptr(b), _ptr(out),
                                                 PREC[precision], float(tol), ctypes.byref(info)))
@@ -316,7 +316,7 @@ class Context:
             b = np.ascontiguousarray(b, dtype=np.complex128)
             lda = n
         else:
-            lda = A.stride(1)
+            lda = _ld(A, n)
         info = SolveInfo_c()
         self._check(self.lib.bem2d_solve_system_noalloc(self.h, n, _ptr(A), lda, _ptr(b),
                                                         _ptr(out), ctypes.byref(info)))

@@ -208,7 +208,7 @@ AUX = {
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the mixed assembly
 # of the sweep's largest problem (ellipse, N = 3084); the file under
 # profiles/ named traffic_far_ff_kernel_ellipse3084.txt holds the command.
-TRAFFIC = {"far_ellipse3084": None}
+TRAFFIC = {"far_ellipse3084": 1036800 + 167379456}
 
 
 def measured_peaks():
