@@ -84,9 +84,6 @@ struct PanelSlots {
   __device__ __forceinline__ char* krow(int par) const { return slot(par, kMaxPanelBlocks); }
 };
 
-size_t lu_scratch_bytes(int) {
-  return (size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + sizeof(double2) * kNB) + 256;
-}
 
 static size_t slots_bytes(size_t elem) {
   return (size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + elem * kNB);
@@ -1019,6 +1016,249 @@ static cudaError_t launch_cluster(K kern, int C, int threads, size_t smem, cudaS
   return cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
+// ---- tournament pivoting for tall complex64 panels --------------------------
+// A complex64 panel taller than the register-window cluster holds (16 x 256
+// rows) is factored with tournament pivoting (TSLU: Grigori, Demmel and
+// Xiang, "CALU: a communication optimal LU factorization algorithm", SIAM J.
+// Matrix Anal. Appl. 32, 2011):
+//   1. select: G blocks of R rows, one CTA each, run partial pivoting on
+//      their own rows in shared memory (no exchange between CTAs) and name
+//      the nb rows they pivoted on;
+//   2. the G nb candidate rows, with their original values, are gathered and
+//      factored with partial pivoting by the register-window cluster kernel:
+//      its nb pivot rows are the panel's, its top nb rows are L11 \ U11;
+//   3. every other row a of the panel becomes L21 = a U11^{-1} (substitution
+//      across the columns, one warp per row), and the panel is written back
+//      in pivot order; the pivot sequence is returned as LAPACK row
+//      interchanges (ipiv), so the rest of the factorisation is unchanged.
+// One exchange between CTAs per panel instead of one per column.  The pivots
+// can differ from partial pivoting's (its growth is as small in practice);
+// the complex64 factor is the preconditioner of the FP64 refinement, whose
+// backward-error test decides the result.
+constexpr int kTsluMaxRows = 384;  // rows of one select CTA (shared memory: 192 KB)
+constexpr int kTsluMinRows = 256;
+constexpr int kTsluMaxCand = kMaxClusterPanel * kWinMaxRows;  // 4096
+
+// Scratch of the tournament (behind the panel exchange slots in
+// LuWork::scratch): candidates' matrix, candidate rows, their pivots and
+// info, row positions, the factored panel.
+static size_t slots_region() {
+  return ((size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + sizeof(double2) * kNB) + 511) / 256 *
+         256;
+}
+static size_t tslu_bytes(int n) {
+  if (n <= kTsluMaxCand) return 0;
+  return sizeof(float2) * (size_t)kTsluMaxCand * kNB + sizeof(int) * ((size_t)kTsluMaxCand + 256) +
+         sizeof(int) * 2 * (size_t)n + sizeof(float2) * (size_t)n * kNB + 1024;
+}
+
+size_t lu_scratch_bytes(int n) { return slots_region() + tslu_bytes(n); }
+
+// grid G, R threads (one per row, R a multiple of 32), R nb float2 of
+// dynamic shared memory (the block's rows, column-major).  cand[b nb + c] =
+// the row of A (absolute) block b pivoted on in its step c, or -1.
+__global__ void __launch_bounds__(kTsluMaxRows)
+tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb, int R,
+                   int* __restrict__ cand) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* S = reinterpret_cast<float2*>(smem_raw);  // S[c R + t]: row t, column c
+  __shared__ float wv[kTsluMaxRows / 32];
+  __shared__ int wi[kTsluMaxRows / 32];
+  __shared__ int s_piv;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = (int)blockDim.x >> 5;
+  const int r0 = k0 + blockIdx.x * R;
+  const int nr = max(0, min(R, n - r0));
+  bool active = t < nr;
+  for (int c = 0; c < nb; ++c)
+    S[c * R + t] = active ? A[(size_t)(k0 + c) * lda + r0 + t] : make_float2(0.f, 0.f);
+  int* out = cand + (size_t)blockIdx.x * nb;
+  const int npiv = min(nb, nr);
+  __syncthreads();
+  int c = 0;
+  for (; c < npiv; ++c) {
+    // block arg-max of |re| + |im| over the rows not yet pivoted (ties: the
+    // smaller row); the rows left always include one, since c < nr
+    float v = active ? cabs1(S[c * R + t]) : -1.f;
+    if (!(v >= 0.f)) v = active ? 0.f : -1.f;  // NaN: never above a number
+    int idx = active ? t : 0x7fffffff;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
+                   __shfl_xor_sync(0xffffffffu, idx, o));
+    if (lane == 0) {
+      wv[wid] = v;
+      wi[wid] = idx;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      float v3 = lane < nw ? wv[lane] : -1.f;
+      int i3 = lane < nw ? wi[lane] : 0x7fffffff;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        argmax_merge(v3, i3, __shfl_xor_sync(0xffffffffu, v3, o),
+                     __shfl_xor_sync(0xffffffffu, i3, o));
+      if (lane == 0) {
+        s_piv = i3;
+        out[c] = (i3 >= 0 && i3 < nr) ? r0 + i3 : -1;
+      }
+    }
+    __syncthreads();
+    const int p = s_piv;  // an active row (one is left while c < nr)
+    if (p < 0 || p >= nr) break;
+    if (t == p) active = false;  // row p is not written from here on
+    if (active) {
+      const float2 piv = S[c * R + p];
+      if (piv.x != 0.f || piv.y != 0.f) {
+        const float2 l = cmul(S[c * R + t], crcp(piv));
+        for (int j = c + 1; j < nb; ++j) S[j * R + t] = cfms(S[j * R + t], l, S[j * R + p]);
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = c + t; j < nb; j += blockDim.x) out[j] = -1;  // steps not taken
+}
+
+// Cb (Gc x nb, column-major, ld Gc) = the original values of the candidate
+// rows (zero rows for -1).  grid (ceil(Gc / 256), nb), 256 threads.
+__global__ void tslu_gather_kernel(const float2* __restrict__ A, long long lda, int k0, int nb,
+                                   const int* __restrict__ cand, int Gc, float2* __restrict__ Cb) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (j >= Gc || c >= nb) return;
+  const int r = cand[j];
+  Cb[(size_t)c * Gc + j] = r >= 0 ? A[(size_t)(k0 + c) * lda + r] : make_float2(0.f, 0.f);
+}
+
+// The panel's pivot rows from the candidates' factorisation (ipc: its row
+// interchanges, infc: its first zero pivot), as LAPACK interchanges ipiv[k0
+// ..]; at[i] = the row of A that ends at position i (i >= k0).  One CTA.
+__global__ void __launch_bounds__(1024)
+tslu_perm_kernel(int n, int k0, int nb, const int* __restrict__ cand, int Gc,
+                 const int* __restrict__ ipc, const int* __restrict__ infc, int* __restrict__ pos,
+                 int* __restrict__ at, int* __restrict__ ipiv, int* info) {
+  __shared__ int cw[kTsluMaxCand];
+  for (int i = k0 + threadIdx.x; i < n; i += blockDim.x) {
+    pos[i] = i;
+    at[i] = i;
+  }
+  for (int j = threadIdx.x; j < Gc; j += blockDim.x) cw[j] = cand[j];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int c = 0; c < nb; ++c) {  // the candidates' interchanges: cw[c] = pivot row c
+      const int q = ipc[c];
+      if (q != c && q >= 0 && q < Gc) {
+        const int tmp = cw[c];
+        cw[c] = cw[q];
+        cw[q] = tmp;
+      }
+    }
+    for (int c = 0; c < nb; ++c) {
+      const int t = k0 + c, r = cw[c];
+      if (r < k0 || r >= n) {  // a zero column: no interchange (info is set)
+        ipiv[t] = t;
+        continue;
+      }
+      const int p = pos[r], rt = at[t];
+      ipiv[t] = p;
+      at[p] = rt;
+      pos[rt] = p;
+      at[t] = r;
+      pos[r] = t;
+    }
+    if (*infc && *info == 0) *info = k0 + *infc;
+  }
+}
+
+// P (H x nb, column-major, ld H = n - k0): the factored panel in its final
+// row order.  Positions k0 .. k0 + nb - 1: rows 0 .. nb - 1 of the
+// candidates' factor (L11 \ U11); position i beyond: x U11 = A(at[i], :)
+// solved for x = L21(i).  grid ceil(H / 8), 256 threads (a warp per
+// position; lane j holds columns j and j + 32).
+__global__ void __launch_bounds__(256)
+tslu_rows_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb,
+                 const float2* __restrict__ Cb, int Gc, const int* __restrict__ at,
+                 float2* __restrict__ P) {
+  __shared__ float2 U[kNB * kNB];  // U[r kNB + c] = U11(r, c): a row per 512 bytes
+  __shared__ float2 dv[kNB];
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e % nb;
+    U[r * kNB + c] = Cb[(size_t)c * Gc + r];
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+    const float2 d = U[c * kNB + c];
+    dv[c] = (d.x != 0.f || d.y != 0.f) ? crcp(d) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int H = n - k0, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= H) return;
+  if (i < nb) {
+    for (int c = lane; c < nb; c += 32) P[(size_t)c * H + i] = Cb[(size_t)c * Gc + i];
+    return;
+  }
+  const int r = at[k0 + i];
+  const int j0 = lane, j1 = lane + 32;
+  float2 a0 = j0 < nb ? A[(size_t)(k0 + j0) * lda + r] : make_float2(0.f, 0.f);
+  float2 a1 = j1 < nb ? A[(size_t)(k0 + j1) * lda + r] : make_float2(0.f, 0.f);
+  for (int c = 0; c < nb; ++c) {
+    const float2 src = c < 32 ? a0 : a1;
+    const float2 ac = make_float2(__shfl_sync(0xffffffffu, src.x, c & 31),
+                                  __shfl_sync(0xffffffffu, src.y, c & 31));
+    const float2 x = cmul(ac, dv[c]);
+    if (j0 == c) a0 = x;
+    if (j1 == c) a1 = x;
+    if (j0 > c && j0 < nb) a0 = cfms(a0, x, U[c * kNB + j0]);
+    if (j1 > c && j1 < nb) a1 = cfms(a1, x, U[c * kNB + j1]);
+  }
+  if (j0 < nb) P[(size_t)j0 * H + i] = a0;
+  if (j1 < nb) P[(size_t)j1 * H + i] = a1;
+}
+
+// Tournament-pivoted panel of columns k0 .. k0 + nb - 1 (rows k0 .. n - 1).
+// false: not applicable (taller than the tournament holds, scratch too
+// small, or the cluster launch refused); A and ipiv are then untouched.
+static bool tslu_panel(float2* A, long long lda, int n, int k0, int nb, const LuWork& w, int cmax,
+                       int min_rpb, cudaStream_t s, long long* launches) {
+  const int H = n - k0;
+  const int cand_max = std::min(kTsluMaxCand, cmax * kWinMaxRows);
+  const int gmax = cand_max / nb;
+  int R = std::max(kTsluMinRows, ((H + gmax - 1) / gmax + 31) / 32 * 32);
+  if (R > kTsluMaxRows) return false;
+  const int G = (H + R - 1) / R, Gc = G * nb;
+  if (w.scratch_bytes < slots_region() + tslu_bytes(n) || tslu_bytes(n) == 0) return false;
+  char* p = static_cast<char*>(w.scratch) + slots_region();
+  float2* Cb = reinterpret_cast<float2*>(p);
+  p += sizeof(float2) * (size_t)kTsluMaxCand * kNB;
+  int* cand = reinterpret_cast<int*>(p);
+  int* ipc = cand + kTsluMaxCand;
+  int* infc = ipc + 128;
+  int* pos = ipc + 256;
+  int* at = pos + n;
+  float2* P = reinterpret_cast<float2*>(
+      (reinterpret_cast<uintptr_t>(at + n) + 255) / 256 * 256);
+  // the candidates' cluster (as the register-window panels: up to cmax CTAs)
+  int C = std::max(1, std::min(cmax, (Gc + min_rpb - 1) / min_rpb));
+  while ((Gc + C - 1) / C > kWinMaxRows) ++C;
+  if (C > cmax) return false;
+  const int rpb = (Gc + C - 1) / C;
+  const int threads = std::max(64, (2 * rpb + 31) / 32 * 32);
+  cudaMemsetAsync(infc, 0, sizeof(int), s);
+  tslu_select_kernel<<<G, R, sizeof(float2) * (size_t)R * nb, s>>>(A, lda, n, k0, nb, R, cand);
+  tslu_gather_kernel<<<dim3((Gc + 255) / 256, nb), 256, 0, s>>>(A, lda, k0, nb, cand, Gc, Cb);
+  if (launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s, Cb, (long long)Gc, Gc,
+                     0, nb, rpb, ipc, infc) != cudaSuccess) {
+    cudaGetLastError();
+    *launches += 2;
+    return false;
+  }
+  tslu_perm_kernel<<<1, 1024, 0, s>>>(n, k0, nb, cand, Gc, ipc, infc, pos, at, w.ipiv, w.info);
+  tslu_rows_kernel<<<(H + 7) / 8, 256, 0, s>>>(A, lda, n, k0, nb, Cb, Gc, at, P);
+  cudaMemcpy2DAsync(A + (size_t)k0 * lda + k0, sizeof(float2) * lda, P, sizeof(float2) * H,
+                    sizeof(float2) * H, nb, cudaMemcpyDeviceToDevice, s);
+  *launches += 4;  // + the panel launch the caller counts
+  return true;
+}
+
 constexpr int kMaxCluster = 16;
 constexpr size_t kClusterSmem = 220 * 1024;
 
@@ -1175,6 +1415,8 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     cudaFuncSetAttribute(dinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(T) * kNB * kNB));
     cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(tslu_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(float2) * kTsluMaxRows * kNB));
   });
   // complex64 matrices are factored in outer blocks of kOuterNB columns:
   // inside a block each 64-column panel updates only the block's columns;
@@ -1213,6 +1455,11 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
         cudaGetLastError();
         if (cmax > 8) cluster16 = false;
       }
+    }
+    if (!done && sizeof(T) == sizeof(float2)) {  // taller: tournament pivoting
+      const int min_rpb = std::min(kWinMaxRows, w.min_rows > 0 ? w.min_rows : kRowsMinRpb);
+      done = tslu_panel(reinterpret_cast<float2*>(A), lda, n, k0, nb, w,
+                        cluster16 ? kMaxClusterPanel : 8, min_rpb, s, launches);
     }
     if (!done && sizeof(T) == sizeof(float2)) {  // taller: shared-memory rows panel
       for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {

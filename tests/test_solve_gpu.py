@@ -97,3 +97,58 @@ def test_large_order_grid_solve():
             assert berr < bound, (prec, berr)
     finally:
         ctx.close()
+
+
+def _device_system(n, seed, row_scale=False):
+    """A seeded complex Gaussian matrix on the device (no diagonal shift:
+    pivoting matters on every column), optionally with rows scaled by
+    10^U(-3, 3); column-major view and right-hand side."""
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    A = torch.randn((n, n), dtype=torch.complex128, device="cuda", generator=g)
+    if row_scale:
+        s = 10.0 ** (6.0 * torch.rand(n, dtype=torch.float64, device="cuda", generator=g) - 3.0)
+        A = A * s[:, None]
+    b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    return A, A.T.contiguous().T, b
+
+
+@pytest.mark.parametrize("n,row_scale", [(4200, False), (6000, True), (9000, False)])
+def test_tall_panels_tournament_pivoting(ctx, n, row_scale):
+    """Orders above 4096 factor their tall complex64 panels (more rows than
+    a 16-CTA cluster holds in registers) with tournament pivoting.  The mixed
+    solve must still reach FP64 backward error, |b - A x| / (|A|_F |x| +
+    |b|) < 1e-14, and agree with the FP64 path (partial pivoting) to the
+    conditioning: |x_mixed - x_fp64| / |x_fp64| <= cond_est * 1e-14, with
+    cond_est = |A|_F |x| / |b| (a lower bound of cond) times 10."""
+    torch = pytest.importorskip("torch")
+    A, Acm, b = _device_system(n, n, row_scale)
+    xs = {}
+    for prec in ("fp64", "mixed"):
+        x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+        ctx.solve(Acm, b, prec, out=x)
+        r = torch.linalg.vector_norm(b - A @ x)
+        nA = torch.linalg.matrix_norm(A)
+        berr = float(r / (nA * torch.linalg.vector_norm(x) + torch.linalg.vector_norm(b)))
+        assert berr < 1e-14, (prec, berr, ctx.last_info)
+        xs[prec] = x
+    cond_est = 10.0 * float(torch.linalg.matrix_norm(A) * torch.linalg.vector_norm(xs["fp64"]) /
+                            torch.linalg.vector_norm(b))
+    err = float(torch.linalg.vector_norm(xs["mixed"] - xs["fp64"]) /
+                torch.linalg.vector_norm(xs["fp64"]))
+    assert err <= cond_est * 1e-14, (err, cond_est)
+
+
+def test_tall_panel_zero_column_reports_its_pivot(ctx):
+    """A zero column inside a tall panel (n = 5000, column 101 of the panel
+    starting at row 64, 4936 rows): the tournament's candidates are all zero
+    there, and both paths report LAPACK's info = 101 as LapackError."""
+    torch = pytest.importorskip("torch")
+    from bem2d_gb300 import capi
+    A, Acm, b = _device_system(5000, 77)
+    Acm[:, 100] = 0
+    for prec in ("fp64", "mixed"):
+        x = torch.zeros(5000, dtype=torch.complex128, device="cuda")
+        with pytest.raises(capi.LapackError) as e:
+            ctx.solve(Acm, b, prec, out=x)
+        assert e.value.code == 101, prec
