@@ -1596,6 +1596,10 @@ int bem2d_l2_norm_cond(bem2d_ctx* c, int n, const void* A, int64_t lda, double t
   return bem2d_l2_norm_cond_prec(c, n, A, lda, tol, BEM2D_PREC_FP64, norm, cond);
 }
 
+// Order from which the mixed norm / condition number iterates with the
+// explicit complex64 inverse instead of triangular solves.
+static constexpr int kInverseMinN = 1024;
+
 int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, double tol,
                             int precision, double* norm, double* cond) {
   if (!c) return BEM2D_ERR_ARG;
@@ -1681,11 +1685,48 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
   }
   float2* LU32 = static_cast<float2*>(LU);
   double2* r = static_cast<double2*>(ws(c, "nc_r", sizeof(double2) * n, &rc));
-  float2* d = static_cast<float2*>(ws(c, "nc_d", 2 * sizeof(float2) * n, &rc));
+  float2* d = static_cast<float2*>(ws(c, "nc_d", 3 * sizeof(float2) * n, &rc));
+  if (!d) return rc;
+  // From kInverseMinN unknowns on, every product with A^{-1} / A^{-H} is a
+  // complex64 matrix-vector product with the explicit inverse W = U^{-1}
+  // L^{-1} (one pass over N^2 entries) instead of two triangular solves (a
+  // chain of 2N/64 dependent block steps); the iterations below need
+  // hundreds of such products.
+  float2* Winv = nullptr;
+  void* zw = nullptr;
+  const size_t zw_bytes = zgemm_work_bytes(n, 1, sizeof(float2));
+  if (n >= kInverseMinN) {
+    Winv = static_cast<float2*>(ws(c, "lu_inv32", sizeof(float2) * (size_t)n * n, &rc));
+    zw = ws(c, "inv_zw", zw_bytes + 256, &rc);
+    if (!Winv || !zw) return rc;
+    if ((rc = lu_inverse_c64(LU32, n, n, w, Winv, n, c->stream, &c->launches)))
+      return fail(c, rc, "inverse launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    CHECK_LAUNCH(c);
+  }
+  // out = op(A)^{-1} (scale x) in complex64 (out: d + n; d, d + 2n: scratch)
+  auto inv32 = [&](bool herm, const double2* x, double scale) -> int {
+    if (Winv) {
+      if (herm) {
+        launch_scale_to_c64(n, x, scale, d, c->stream);
+        launch_zgemm(true, Winv, n, n, d, n, 1, d + 2 * n, n, zw, zw_bytes, c->stream);
+        launch_scatter_c64(n, d + 2 * n, w.perm, d + n, c->stream);
+      } else {
+        launch_gather_to_c64(n, x, w.perm, scale, d, c->stream);
+        launch_zgemm(false, Winv, n, n, d, n, 1, d + n, n, zw, zw_bytes, c->stream);
+      }
+      c->launches += 3;
+      return BEM2D_OK;
+    }
+    launch_scale_to_c64(n, x, scale, d, c->stream);
+    ++c->launches;
+    const int e = herm ? lu_solve_h<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches)
+                       : lu_solve<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches);
+    return e ? fail(c, e, "triangular solve launch failed") : BEM2D_OK;
+  };
   double2* rpart = static_cast<double2*>(ws(c, "ir_part", residual_part_bytes(n), &rc));
   double* red = static_cast<double*>(ws(c, "ir_red", sumsq_part_bytes() + 64, &rc));
   double2* v1 = static_cast<double2*>(ws(c, "nc_v1", sizeof(double2) * n, &rc));
-  if (!r || !d || !rpart || !red || !v1) return rc;
+  if (!r || !rpart || !red || !v1) return rc;
   double* scal = red + sumsq_part_bytes() / sizeof(double);  // [0] |A|^2 [1] |x|^2 [2] |r|^2 [3] |y|^2
   launch_sumsq(dA, la, n, n, red, scal, c->stream);
   c->launches += 2;
@@ -1712,10 +1753,7 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
       if (rnorm == 0.0 || rnorm <= 2.2e-16 * (normA * ynorm + xnorm)) break;
       if (!(rnorm < 0.5 * best)) break;
       best = rnorm;
-      launch_scale_to_c64(n, r, 1.0 / rnorm, d, c->stream);
-      int e = herm ? lu_solve_h<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches)
-                   : lu_solve<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches);
-      if (e) return fail(c, e, "triangular solve launch failed");
+      if ((rc = inv32(herm, r, 1.0 / rnorm))) return rc;
       launch_axpy_c64(n, rnorm, d + n, y, c->stream);
       if (herm) {
         launch_mvh(dA, la, n, y, tmp, c->stream);
@@ -1745,12 +1783,9 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
   // operator accurate to ~1e-7), until its estimate settles to 1e-10: its
   // Ritz vector starts the refined phase, which then needs only a few steps
   auto op32 = [&](bool herm, const double2* x, double2* y) -> int {
-    launch_scale_to_c64(n, x, 1.0, d, c->stream);
-    int e = herm ? lu_solve_h<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches)
-                 : lu_solve<float2>(LU32, n, n, w, d, d + n, c->stream, &c->launches);
-    if (e) return fail(c, e, "triangular solve launch failed");
+    if ((rc = inv32(herm, x, 1.0))) return rc;
     launch_widen(n, d + n, n, y, n, 1, c->stream);
-    c->launches += 2;
+    ++c->launches;
     return BEM2D_OK;
   };
   double s32 = 0;

@@ -459,6 +459,16 @@ template <typename T>
 int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
                cudaStream_t s, long long* launches);
 
+// W = U^{-1} L^{-1} (complex64, n x n, ld ldw) from the factor of
+// lu_factor<float2> (needs w.pack for K = 64 and w.dinv): A^{-1} x =
+// W (P x), A^{-H} x = P^T (W^H x), P x = x[w.perm[i]].
+int lu_inverse_c64(const float2* LU, long long lda, int n, const LuWork& w, float2* W,
+                   long long ldw, cudaStream_t s, long long* launches);
+// dst[i] = (complex64)(scale src[perm[i]]);  dst[perm[i]] = src[i]
+void launch_gather_to_c64(int n, const double2* src, const int* perm, double scale, float2* dst,
+                          cudaStream_t s);
+void launch_scatter_c64(int n, const float2* src, const int* perm, float2* dst, cudaStream_t s);
+
 // C -= A B for complex64 column-major operands on the tensor cores
 // (tcgen05 kind::tf32, 3xTF32 split; lu_tc.cu).  C is M x N, A M x K, B K x N.
 // Sets *status on a device-side wait timeout.

@@ -2072,6 +2072,118 @@ __global__ void axpy_c64_kernel(int n, double scale, const float2* __restrict__ 
   }
 }
 
+// ---- explicit inverse of a complex64 factor ---------------------------------
+// W = U^{-1} L^{-1} from the factor P A = L U of lu_factor<float2>, so that
+// A^{-1} x = W (P x) and A^{-H} x = P^T (W^H x).  Blocked substitution on
+// the identity, 64 rows at a time:
+//   forward  Y_k = L_kk^{-1} Y_k, then Y_below -= L_below,k Y_k (Y stays lower
+//            triangular: only columns 0 .. k64 + 63 are touched);
+//   backward W_k = U_kk^{-1} W_k, then W_above -= U_above,k W_k.
+// The diagonal-block inverses are lu_factor's (w.dinv); the rank-64 updates
+// run on the tensor cores (the trailing-update kernel).  About 2.7 N^3
+// complex flops; an inverse pays for itself once an iteration needs more
+// than a few dozen solves with the factor (a product with W streams N^2
+// entries; the substitution is a chain of 2 N / 64 dependent steps).
+
+// Xb (rows r0 .. r0 + bs - 1 of X, column-major, ld ldx) = D Xb, D a 64 x 64
+// column-major block (zero beyond bs).  grid ceil(ncols / 16), 256 threads.
+__global__ void __launch_bounds__(256)
+block_apply_kernel(const float2* __restrict__ D, float2* __restrict__ X, long long ldx, int bs,
+                   int ncols) {
+  __shared__ float2 Ds[kNB * kNB];  // Ds[k * 64 + r] = D(r, k)
+  __shared__ float2 T[kNB * 17];    // T[k * 17 + c] = X(r0 + k, c0 + c)
+  const int c0 = blockIdx.x * 16;
+  for (int e = threadIdx.x; e < kNB * kNB; e += blockDim.x) Ds[e] = D[e];
+  for (int e = threadIdx.x; e < kNB * 16; e += blockDim.x) {
+    const int c = e / kNB, k = e - c * kNB;  // coalesced along k (rows)
+    T[k * 17 + c] = (k < bs && c0 + c < ncols) ? X[(size_t)(c0 + c) * ldx + k]
+                                                : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int c = threadIdx.x & 15, rb = threadIdx.x >> 4;  // rows rb + 16 q
+  float2 acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = make_float2(0.f, 0.f);
+  for (int k = 0; k < bs; ++k) {
+    const float2 t = T[k * 17 + c];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q] = cfma(Ds[k * kNB + rb + 16 * q], t, acc[q]);
+  }
+  if (c0 + c >= ncols) return;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = rb + 16 * q;
+    if (r < bs) X[(size_t)(c0 + c) * ldx + r] = acc[q];
+  }
+}
+
+__global__ void identity_c64_kernel(int n, float2* __restrict__ X, long long ldx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) X[(size_t)i * ldx + i] = make_float2(1.f, 0.f);
+}
+
+int lu_inverse_c64(const float2* LU, long long lda, int n, const LuWork& w, float2* W,
+                   long long ldw, cudaStream_t s, long long* launches) {
+  if (n <= 0) return BEM2D_OK;
+  if (!w.pack || !w.dinv) return BEM2D_ERR_ARG;
+  const int nk = (n + kNB - 1) / kNB;
+  if (tc_pack_bytes(n, n, kNB) > w.pack_bytes) return BEM2D_ERR_ARG;
+  if (cudaMemset2DAsync(W, sizeof(float2) * ldw, 0, sizeof(float2) * n, n, s) != cudaSuccess)
+    return BEM2D_ERR_CUDA;
+  identity_c64_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, W, ldw);
+  ++*launches;
+  const float2* dinv = static_cast<const float2*>(w.dinv);
+  for (int k = 0; k < nk; ++k) {  // forward: Y = L^{-1}
+    const int r0 = k * kNB, bs = std::min(kNB, n - r0), nc = r0 + bs;
+    block_apply_kernel<<<(nc + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * k) * kNB * kNB,
+                                                      W + r0, ldw, bs, nc);
+    ++*launches;
+    const int M = n - nc;
+    if (M > 0) {
+      if (launch_tc_cgemm_sub(W + nc, ldw, LU + (size_t)r0 * lda + nc, lda, W + r0, ldw, M, nc,
+                              bs, w.pack, w.pack_bytes, w.status, s))
+        return BEM2D_ERR_CUDA;
+      *launches += 3;
+    }
+  }
+  for (int k = nk - 1; k >= 0; --k) {  // backward: W = U^{-1} Y
+    const int r0 = k * kNB, bs = std::min(kNB, n - r0);
+    block_apply_kernel<<<(n + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * k + 1) * kNB * kNB,
+                                                     W + r0, ldw, bs, n);
+    ++*launches;
+    if (r0 > 0) {
+      if (launch_tc_cgemm_sub(W, ldw, LU + (size_t)r0 * lda, lda, W + r0, ldw, r0, n, bs, w.pack,
+                              w.pack_bytes, w.status, s))
+        return BEM2D_ERR_CUDA;
+      *launches += 3;
+    }
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
+}
+
+// dst[i] = (complex64) (scale src[perm[i]]): P x of an FP64 vector.
+__global__ void gather_to_c64_kernel(int n, const double2* __restrict__ src,
+                                     const int* __restrict__ perm, double scale,
+                                     float2* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = src[perm[i]];
+  dst[i] = make_float2((float)(v.x * scale), (float)(v.y * scale));
+}
+// dst[perm[i]] = src[i]: P^T y (complex64).
+__global__ void scatter_c64_kernel(int n, const float2* __restrict__ src,
+                                   const int* __restrict__ perm, float2* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[perm[i]] = src[i];
+}
+void launch_gather_to_c64(int n, const double2* src, const int* perm, double scale, float2* dst,
+                          cudaStream_t s) {
+  gather_to_c64_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, src, perm, scale, dst);
+}
+void launch_scatter_c64(int n, const float2* src, const int* perm, float2* dst, cudaStream_t s) {
+  scatter_c64_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, src, perm, dst);
+}
+
 void launch_scale_to_c64(int n, const double2* src, double scale, float2* dst, cudaStream_t s) {
   scale_to_c64_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, src, scale, dst);
 }
