@@ -63,6 +63,7 @@ struct bem2d_ctx {
   cudaStream_t stream_hi = nullptr;
   cudaEvent_t ev_asm = nullptr, ev_sol = nullptr;
   int panel_min_rows = 0;  // LuWork::min_rows of this context's factorisations
+  int tc_ctas = 0;         // LuWork::tc_ctas of this context's factorisations
 };
 
 namespace bem2d_gpu {
@@ -811,6 +812,7 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
   bem2d_solve_info rep{0, 0, 0.0};
   LuWork w;
   w.min_rows = c->panel_min_rows;
+  w.tc_ctas = c->tc_ctas;
   // ints: [0] info [1] status [8, 8+n) ipiv
   int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
   if (!ints) return rc;
@@ -2139,8 +2141,13 @@ std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c) { return c->workers; }
 #ifndef BEM2D_SWEEP_PANEL_ROWS
 #define BEM2D_SWEEP_PANEL_ROWS 256
 #endif
+// Persistent CTAs of a sweep worker's tensor-core updates (0: one per SM).
+#ifndef BEM2D_SWEEP_TC_CTAS
+#define BEM2D_SWEEP_TC_CTAS 0
+#endif
 int ctx_make_sweep_worker(bem2d_ctx* c) {
   c->panel_min_rows = BEM2D_SWEEP_PANEL_ROWS;
+  c->tc_ctas = BEM2D_SWEEP_TC_CTAS;
   if (c->stream_hi) return BEM2D_OK;
   cudaSetDevice(c->device);
   int least = 0, greatest = 0;

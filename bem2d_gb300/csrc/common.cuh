@@ -431,6 +431,9 @@ struct LuWork {
   // larger values use fewer, fuller CTAs, so that more panels of concurrent
   // factorisations fit on the GPU at once)
   int min_rows = 0;
+  // persistent CTAs of the tensor-core update (0: one per SM); fewer leave
+  // SMs to concurrent factorisations
+  int tc_ctas = 0;
 };
 
 // Bytes of LuWork::scratch the panel kernels need for n unknowns.
@@ -476,7 +479,7 @@ void launch_scatter_c64(int n, const float2* src, const int* perm, float2* dst, 
 size_t tc_pack_bytes(int M, int N, int K);
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
                         const float2* B, long long ldb, int M, int N, int K, void* pack,
-                        size_t pack_bytes, int* status, cudaStream_t s);
+                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas = 0);
 
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);

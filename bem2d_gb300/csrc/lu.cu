@@ -1035,33 +1035,65 @@ static cudaError_t launch_cluster(K kern, int C, int threads, size_t smem, cudaS
 // can differ from partial pivoting's (its growth is as small in practice);
 // the complex64 factor is the preconditioner of the FP64 refinement, whose
 // backward-error test decides the result.
-constexpr int kTsluMaxRows = 384;  // rows of one select CTA (shared memory: 192 KB)
+constexpr int kTsluMaxRows = 384;  // rows of one select CTA (one row per thread)
 constexpr int kTsluMinRows = 256;
 constexpr int kTsluMaxCand = kMaxClusterPanel * kWinMaxRows;  // 4096
+constexpr int kTsluFinalCand = 1024;  // candidates left for the cluster kernel
+constexpr int kTsluMaxH = 64 * kTsluMaxRows;                  // tallest panel (24576)
 
-// Scratch of the tournament (behind the panel exchange slots in
-// LuWork::scratch): candidates' matrix, candidate rows, their pivots and
-// info, row positions, the factored panel.
+// Scratch of the tournament, behind the panel exchange slots in
+// LuWork::scratch.
+struct TsluScratch {
+  float2* Cb;    // [kTsluMaxCand][kNB] level-1 candidates (original values)
+  float2* Cb2;   // [kTsluFinalCand][kNB] level-2 candidates
+  float2* P;     // [H][kNB] the factored panel
+  int* cand;     // [kTsluMaxCand] rows of A (level 1)
+  int* cand2;    // [kTsluFinalCand] rows of Cb (level 2)
+  int* candF;    // [kTsluFinalCand] rows of A of the final candidates
+  int* ipc;      // [kNB] the final candidates' interchanges
+  int* infc;     // [1] their first zero pivot
+  int* moved;    // [2 kNB + 1] count, then (position, row) pairs beyond the pivots
+};
 static size_t slots_region() {
   return ((size_t)2 * (kMaxPanelBlocks + 1) * (kSlotHead + sizeof(double2) * kNB) + 511) / 256 *
          256;
 }
 static size_t tslu_bytes(int n) {
   if (n <= kTsluMaxCand) return 0;
-  return sizeof(float2) * (size_t)kTsluMaxCand * kNB + sizeof(int) * ((size_t)kTsluMaxCand + 256) +
-         sizeof(int) * 2 * (size_t)n + sizeof(float2) * (size_t)n * kNB + 1024;
+  return sizeof(float2) * (size_t)(kTsluMaxCand + kTsluFinalCand + n) * kNB +
+         sizeof(int) * ((size_t)kTsluMaxCand + 2 * kTsluFinalCand + 4 * kNB + 64) + 2048;
+}
+static TsluScratch tslu_scratch(void* base, int n) {
+  auto al = [](char* q) { return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(q) + 255) / 256 * 256); };
+  char* p = al(static_cast<char*>(base));
+  TsluScratch t;
+  t.Cb = reinterpret_cast<float2*>(p);
+  p = al(p + sizeof(float2) * (size_t)kTsluMaxCand * kNB);
+  t.Cb2 = reinterpret_cast<float2*>(p);
+  p = al(p + sizeof(float2) * (size_t)kTsluFinalCand * kNB);
+  t.P = reinterpret_cast<float2*>(p);
+  p = al(p + sizeof(float2) * (size_t)n * kNB);
+  t.cand = reinterpret_cast<int*>(p);
+  t.cand2 = t.cand + kTsluMaxCand;
+  t.candF = t.cand2 + kTsluFinalCand;
+  t.ipc = t.candF + kTsluFinalCand;
+  t.infc = t.ipc + kNB;
+  t.moved = t.infc + 32;
+  return t;
 }
 
 size_t lu_scratch_bytes(int n) { return slots_region() + tslu_bytes(n); }
 
-// grid G, R threads (one per row, R a multiple of 32), R nb float2 of
-// dynamic shared memory (the block's rows, column-major).  cand[b nb + c] =
-// the row of A (absolute) block b pivoted on in its step c, or -1.
-__global__ void __launch_bounds__(kTsluMaxRows)
+// One tournament round: grid G, R threads (one row each, R a multiple of
+// 32), the block's rows held in registers (the pivot loop is unrolled, so
+// every column index is static).  Block b runs partial pivoting on rows
+// r0 .. r0 + R - 1 (r0 = k0 + b R) of columns k0 .. k0 + nb - 1 and writes
+// the rows it pivoted on (absolute indices) to cand[b nb + c], -1 for steps
+// not taken.
+__global__ void __launch_bounds__(kTsluMaxRows, 1)
 tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb, int R,
                    int* __restrict__ cand) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* S = reinterpret_cast<float2*>(smem_raw);  // S[c R + t]: row t, column c
+  __shared__ float2 prow[kNB];
   __shared__ float wv[kTsluMaxRows / 32];
   __shared__ int wi[kTsluMaxRows / 32];
   __shared__ int s_piv;
@@ -1069,78 +1101,98 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
   const int r0 = k0 + blockIdx.x * R;
   const int nr = max(0, min(R, n - r0));
   bool active = t < nr;
-  for (int c = 0; c < nb; ++c)
-    S[c * R + t] = active ? A[(size_t)(k0 + c) * lda + r0 + t] : make_float2(0.f, 0.f);
+  float2 a[kNB];
+#pragma unroll
+  for (int c = 0; c < kNB; ++c)
+    a[c] = (active && c < nb) ? A[(size_t)(k0 + c) * lda + r0 + t] : make_float2(0.f, 0.f);
   int* out = cand + (size_t)blockIdx.x * nb;
   const int npiv = min(nb, nr);
-  __syncthreads();
-  int c = 0;
-  for (; c < npiv; ++c) {
-    // block arg-max of |re| + |im| over the rows not yet pivoted (ties: the
-    // smaller row); the rows left always include one, since c < nr
-    float v = active ? cabs1(S[c * R + t]) : -1.f;
-    if (!(v >= 0.f)) v = active ? 0.f : -1.f;  // NaN: never above a number
-    int idx = active ? t : 0x7fffffff;
+  int done = 0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-      argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
-                   __shfl_xor_sync(0xffffffffu, idx, o));
-    if (lane == 0) {
-      wv[wid] = v;
-      wi[wid] = idx;
-    }
-    __syncthreads();
-    if (wid == 0) {
-      float v3 = lane < nw ? wv[lane] : -1.f;
-      int i3 = lane < nw ? wi[lane] : 0x7fffffff;
+  for (int c = 0; c < kNB; ++c) {
+    if (c < npiv && done == c) {
+      // block arg-max of |re| + |im| over the rows not yet pivoted (ties: the
+      // smaller row); NaN counts as zero
+      float v = active ? cabs1(a[c]) : -1.f;
+      if (!(v >= 0.f)) v = active ? 0.f : -1.f;
+      int idx = active ? t : 0x7fffffff;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
-        argmax_merge(v3, i3, __shfl_xor_sync(0xffffffffu, v3, o),
-                     __shfl_xor_sync(0xffffffffu, i3, o));
+        argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
+                     __shfl_xor_sync(0xffffffffu, idx, o));
       if (lane == 0) {
-        s_piv = i3;
-        out[c] = (i3 >= 0 && i3 < nr) ? r0 + i3 : -1;
+        wv[wid] = v;
+        wi[wid] = idx;
+      }
+      __syncthreads();
+      if (wid == 0) {
+        float v3 = lane < nw ? wv[lane] : -1.f;
+        int i3 = lane < nw ? wi[lane] : 0x7fffffff;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          argmax_merge(v3, i3, __shfl_xor_sync(0xffffffffu, v3, o),
+                       __shfl_xor_sync(0xffffffffu, i3, o));
+        if (lane == 0) {
+          s_piv = i3;
+          out[c] = (i3 >= 0 && i3 < nr) ? r0 + i3 : -1;
+        }
+      }
+      __syncthreads();
+      const int p = s_piv;
+      if (p >= 0 && p < nr) {
+        if (t == p) {  // stage the pivot row; it is not updated from here on
+#pragma unroll
+          for (int j = c; j < kNB; ++j) prow[j] = a[j];
+          active = false;
+        }
+        __syncthreads();
+        if (active) {
+          const float2 pv = prow[c];
+          if (pv.x != 0.f || pv.y != 0.f) {
+            const float2 l = cmul(a[c], crcp(pv));
+#pragma unroll
+            for (int j = c + 1; j < kNB; ++j) a[j] = cfms(a[j], l, prow[j]);
+          }
+        }
+        done = c + 1;
       }
     }
-    __syncthreads();
-    const int p = s_piv;  // an active row (one is left while c < nr)
-    if (p < 0 || p >= nr) break;
-    if (t == p) active = false;  // row p is not written from here on
-    if (active) {
-      const float2 piv = S[c * R + p];
-      if (piv.x != 0.f || piv.y != 0.f) {
-        const float2 l = cmul(S[c * R + t], crcp(piv));
-        for (int j = c + 1; j < nb; ++j) S[j * R + t] = cfms(S[j * R + t], l, S[j * R + p]);
-      }
-    }
-    __syncthreads();
   }
-  for (int j = c + t; j < nb; j += blockDim.x) out[j] = -1;  // steps not taken
+  for (int j = done + t; j < nb; j += blockDim.x) out[j] = -1;  // steps not taken
 }
 
-// Cb (Gc x nb, column-major, ld Gc) = the original values of the candidate
-// rows (zero rows for -1).  grid (ceil(Gc / 256), nb), 256 threads.
-__global__ void tslu_gather_kernel(const float2* __restrict__ A, long long lda, int k0, int nb,
-                                   const int* __restrict__ cand, int Gc, float2* __restrict__ Cb) {
+// Cb (Gc x nb, column-major, ld Gc) = rows src[j] of S (column-major, ld
+// lds; zero rows for -1); optionally map[j] = idx[src[j]].
+// grid (ceil(Gc / 256), nb), 256 threads.
+__global__ void tslu_gather_kernel(const float2* __restrict__ S, long long lds, int k0, int nb,
+                                   const int* __restrict__ src, int Gc, float2* __restrict__ Cb,
+                                   const int* __restrict__ idx, int* __restrict__ map) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
   if (j >= Gc || c >= nb) return;
-  const int r = cand[j];
-  Cb[(size_t)c * Gc + j] = r >= 0 ? A[(size_t)(k0 + c) * lda + r] : make_float2(0.f, 0.f);
+  const int r = src[j];
+  Cb[(size_t)c * Gc + j] = r >= 0 ? S[(size_t)(k0 + c) * lds + r] : make_float2(0.f, 0.f);
+  if (map && c == 0) map[j] = (r >= 0 && idx) ? idx[r] : r;
 }
 
-// The panel's pivot rows from the candidates' factorisation (ipc: its row
-// interchanges, infc: its first zero pivot), as LAPACK interchanges ipiv[k0
-// ..]; at[i] = the row of A that ends at position i (i >= k0).  One CTA.
+// The panel's interchanges from the final candidates' factorisation (ipc,
+// infc): ipiv[k0 + c] (LAPACK), and the rows that end beyond the pivots at
+// positions other than their own: moved[0] = count, then (position, row)
+// pairs.  Positions relative to k0 live in shared memory (2 H ints).  One
+// CTA of 1024 threads.
 __global__ void __launch_bounds__(1024)
-tslu_perm_kernel(int n, int k0, int nb, const int* __restrict__ cand, int Gc,
-                 const int* __restrict__ ipc, const int* __restrict__ infc, int* __restrict__ pos,
-                 int* __restrict__ at, int* __restrict__ ipiv, int* info) {
-  __shared__ int cw[kTsluMaxCand];
-  for (int i = k0 + threadIdx.x; i < n; i += blockDim.x) {
+tslu_perm_kernel(int n, int k0, int nb, const int* __restrict__ candF, int Gc,
+                 const int* __restrict__ ipc, const int* __restrict__ infc, int* __restrict__ ipiv,
+                 int* info, int* __restrict__ moved) {
+  extern __shared__ int sh[];
+  const int H = n - k0;
+  int* pos = sh;       // [H] position of row k0 + i
+  int* at = sh + H;    // [H] row at position k0 + i
+  __shared__ int cw[kTsluFinalCand];
+  for (int i = threadIdx.x; i < H; i += blockDim.x) {
     pos[i] = i;
     at[i] = i;
   }
-  for (int j = threadIdx.x; j < Gc; j += blockDim.x) cw[j] = cand[j];
+  for (int j = threadIdx.x; j < Gc; j += blockDim.x) cw[j] = candF[j];
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int c = 0; c < nb; ++c) {  // the candidates' interchanges: cw[c] = pivot row c
@@ -1152,66 +1204,97 @@ tslu_perm_kernel(int n, int k0, int nb, const int* __restrict__ cand, int Gc,
       }
     }
     for (int c = 0; c < nb; ++c) {
-      const int t = k0 + c, r = cw[c];
-      if (r < k0 || r >= n) {  // a zero column: no interchange (info is set)
-        ipiv[t] = t;
+      const int r = cw[c] - k0;
+      if (r < 0 || r >= H) {  // a zero column: no interchange (info is set)
+        ipiv[k0 + c] = k0 + c;
         continue;
       }
-      const int p = pos[r], rt = at[t];
-      ipiv[t] = p;
+      const int p = pos[r], rt = at[c];
+      ipiv[k0 + c] = k0 + p;
       at[p] = rt;
       pos[rt] = p;
-      at[t] = r;
-      pos[r] = t;
+      at[c] = r;
+      pos[r] = c;
     }
+    int m = 0;
+    for (int c = 0; c < nb; ++c) {
+      const int p = ipiv[k0 + c] - k0;
+      if (p >= nb && at[p] != p) {
+        bool seen = false;
+        for (int u = 0; u < m; ++u) seen |= moved[1 + 2 * u] == k0 + p;
+        if (!seen) {
+          moved[1 + 2 * m] = k0 + p;
+          moved[2 + 2 * m] = k0 + at[p];
+          ++m;
+        }
+      }
+    }
+    moved[0] = m;
     if (*infc && *info == 0) *info = k0 + *infc;
   }
 }
 
 // P (H x nb, column-major, ld H = n - k0): the factored panel in its final
 // row order.  Positions k0 .. k0 + nb - 1: rows 0 .. nb - 1 of the
-// candidates' factor (L11 \ U11); position i beyond: x U11 = A(at[i], :)
-// solved for x = L21(i).  grid ceil(H / 8), 256 threads (a warp per
-// position; lane j holds columns j and j + 32).
+// candidates' factor (L11 \ U11, Cf: ld Gc); position i beyond: the row r
+// there (i itself unless listed in `moved`), x U11 = A(r, :) solved for x =
+// L21(i).  A warp per position (lane j holds columns j and j + 32), each CTA
+// looping over positions with stride.
 __global__ void __launch_bounds__(256)
 tslu_rows_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb,
-                 const float2* __restrict__ Cb, int Gc, const int* __restrict__ at,
+                 const float2* __restrict__ Cf, int Gc, const int* __restrict__ moved,
                  float2* __restrict__ P) {
-  __shared__ float2 U[kNB * kNB];  // U[r kNB + c] = U11(r, c): a row per 512 bytes
+  __shared__ float2 U[kNB * (kNB + 1)];  // U[c (kNB + 1) + r] = U11(c, r): row c of U11
   __shared__ float2 dv[kNB];
+  __shared__ int mv[2 * kNB + 1];
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e % nb;
-    U[r * kNB + c] = Cb[(size_t)c * Gc + r];
+    const int c = e / nb, r = e - c * nb;  // coalesced: consecutive rows of column c
+    U[r * (kNB + 1) + c] = Cf[(size_t)c * Gc + r];
   }
+  for (int e = threadIdx.x; e < 2 * kNB + 1; e += blockDim.x) mv[e] = moved[e];
   __syncthreads();
   for (int c = threadIdx.x; c < nb; c += blockDim.x) {
-    const float2 d = U[c * kNB + c];
+    const float2 d = U[c * (kNB + 1) + c];
     dv[c] = (d.x != 0.f || d.y != 0.f) ? crcp(d) : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const int H = n - k0, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (i >= H) return;
-  if (i < nb) {
-    for (int c = lane; c < nb; c += 32) P[(size_t)c * H + i] = Cb[(size_t)c * Gc + i];
-    return;
-  }
-  const int r = at[k0 + i];
+  const int H = n - k0, lane = threadIdx.x & 31, m = mv[0];
   const int j0 = lane, j1 = lane + 32;
-  float2 a0 = j0 < nb ? A[(size_t)(k0 + j0) * lda + r] : make_float2(0.f, 0.f);
-  float2 a1 = j1 < nb ? A[(size_t)(k0 + j1) * lda + r] : make_float2(0.f, 0.f);
-  for (int c = 0; c < nb; ++c) {
-    const float2 src = c < 32 ? a0 : a1;
-    const float2 ac = make_float2(__shfl_sync(0xffffffffu, src.x, c & 31),
-                                  __shfl_sync(0xffffffffu, src.y, c & 31));
-    const float2 x = cmul(ac, dv[c]);
-    if (j0 == c) a0 = x;
-    if (j1 == c) a1 = x;
-    if (j0 > c && j0 < nb) a0 = cfms(a0, x, U[c * kNB + j0]);
-    if (j1 > c && j1 < nb) a1 = cfms(a1, x, U[c * kNB + j1]);
+  for (int i = blockIdx.x * 8 + (threadIdx.x >> 5); i < H; i += gridDim.x * 8) {
+    if (i < nb) {
+      for (int c = lane; c < nb; c += 32) P[(size_t)c * H + i] = Cf[(size_t)c * Gc + i];
+      continue;
+    }
+    int f = -1;  // the row moved to position k0 + i, if any
+    for (int u = lane; u < m; u += 32)
+      if (mv[1 + 2 * u] == k0 + i) f = mv[2 + 2 * u];
+    f = __reduce_max_sync(0xffffffffu, f);
+    const int r = f >= 0 ? f : k0 + i;
+    float2 a0 = j0 < nb ? A[(size_t)(k0 + j0) * lda + r] : make_float2(0.f, 0.f);
+    float2 a1 = j1 < nb ? A[(size_t)(k0 + j1) * lda + r] : make_float2(0.f, 0.f);
+    for (int c = 0; c < nb; ++c) {
+      const float2 src = c < 32 ? a0 : a1;
+      const float2 ac = make_float2(__shfl_sync(0xffffffffu, src.x, c & 31),
+                                    __shfl_sync(0xffffffffu, src.y, c & 31));
+      const float2 x = cmul(ac, dv[c]);
+      if (j0 == c) a0 = x;
+      if (j1 == c) a1 = x;
+      if (j0 > c && j0 < nb) a0 = cfms(a0, x, U[c * (kNB + 1) + j0]);
+      if (j1 > c && j1 < nb) a1 = cfms(a1, x, U[c * (kNB + 1) + j1]);
+    }
+    if (j0 < nb) P[(size_t)j0 * H + i] = a0;
+    if (j1 < nb) P[(size_t)j1 * H + i] = a1;
   }
-  if (j0 < nb) P[(size_t)j0 * H + i] = a0;
-  if (j1 < nb) P[(size_t)j1 * H + i] = a1;
+}
+
+static int num_sms_lu() {
+  static const int v = [] {
+    int dev = 0, c = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+    return c > 0 ? c : 1;
+  }();
+  return v;
 }
 
 // Tournament-pivoted panel of columns k0 .. k0 + nb - 1 (rows k0 .. n - 1).
@@ -1220,42 +1303,61 @@ tslu_rows_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int
 static bool tslu_panel(float2* A, long long lda, int n, int k0, int nb, const LuWork& w, int cmax,
                        int min_rpb, cudaStream_t s, long long* launches) {
   const int H = n - k0;
-  const int cand_max = std::min(kTsluMaxCand, cmax * kWinMaxRows);
-  const int gmax = cand_max / nb;
-  int R = std::max(kTsluMinRows, ((H + gmax - 1) / gmax + 31) / 32 * 32);
+  if (H > kTsluMaxH || tslu_bytes(n) == 0 ||
+      w.scratch_bytes < slots_region() + tslu_bytes(n))
+    return false;
+  const int gmax = std::min(kTsluMaxCand, cmax * kWinMaxRows) / nb;
+  const int R = std::max(kTsluMinRows, ((H + gmax - 1) / gmax + 31) / 32 * 32);
   if (R > kTsluMaxRows) return false;
   const int G = (H + R - 1) / R, Gc = G * nb;
-  if (w.scratch_bytes < slots_region() + tslu_bytes(n) || tslu_bytes(n) == 0) return false;
-  char* p = static_cast<char*>(w.scratch) + slots_region();
-  float2* Cb = reinterpret_cast<float2*>(p);
-  p += sizeof(float2) * (size_t)kTsluMaxCand * kNB;
-  int* cand = reinterpret_cast<int*>(p);
-  int* ipc = cand + kTsluMaxCand;
-  int* infc = ipc + 128;
-  int* pos = ipc + 256;
-  int* at = pos + n;
-  float2* P = reinterpret_cast<float2*>(
-      (reinterpret_cast<uintptr_t>(at + n) + 255) / 256 * 256);
-  // the candidates' cluster (as the register-window panels: up to cmax CTAs)
-  int C = std::max(1, std::min(cmax, (Gc + min_rpb - 1) / min_rpb));
-  while ((Gc + C - 1) / C > kWinMaxRows) ++C;
-  if (C > cmax) return false;
-  const int rpb = (Gc + C - 1) / C;
-  const int threads = std::max(64, (2 * rpb + 31) / 32 * 32);
-  cudaMemsetAsync(infc, 0, sizeof(int), s);
-  tslu_select_kernel<<<G, R, sizeof(float2) * (size_t)R * nb, s>>>(A, lda, n, k0, nb, R, cand);
-  tslu_gather_kernel<<<dim3((Gc + 255) / 256, nb), 256, 0, s>>>(A, lda, k0, nb, cand, Gc, Cb);
-  if (launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s, Cb, (long long)Gc, Gc,
-                     0, nb, rpb, ipc, infc) != cudaSuccess) {
-    cudaGetLastError();
+  const TsluScratch ts = tslu_scratch(static_cast<char*>(w.scratch) + slots_region(), n);
+  // round 1: blocks of R rows of the panel -> Gc candidates (a launch the
+  // GPU refuses leaves the panel to the other kernels)
+  cudaGetLastError();
+  tslu_select_kernel<<<G, R, 0, s>>>(A, lda, n, k0, nb, R, ts.cand);
+  if (cudaGetLastError() != cudaSuccess) return false;
+  tslu_gather_kernel<<<dim3((Gc + 255) / 256, nb), 256, 0, s>>>(A, lda, k0, nb, ts.cand, Gc, ts.Cb,
+                                                                nullptr, nullptr);
+  const float2* Cf = ts.Cb;
+  const int* candF = ts.cand;
+  int Gf = Gc;
+  *launches += 2;
+  if (Gc > kTsluFinalCand) {
+    // round 2: blocks of the candidates -> at most kTsluFinalCand
+    const int R2 = std::max(kTsluMinRows, ((Gc + kTsluFinalCand / nb - 1) / (kTsluFinalCand / nb) +
+                                           31) / 32 * 32);
+    const int G2 = (Gc + R2 - 1) / R2;
+    Gf = G2 * nb;
+    if (R2 > kTsluMaxRows || Gf > kTsluFinalCand) return false;
+    tslu_select_kernel<<<G2, R2, 0, s>>>(ts.Cb, Gc, Gc, 0, nb, R2, ts.cand2);
+    if (cudaGetLastError() != cudaSuccess) return false;
+    tslu_gather_kernel<<<dim3((Gf + 255) / 256, nb), 256, 0, s>>>(ts.Cb, Gc, 0, nb, ts.cand2, Gf,
+                                                                  ts.Cb2, ts.cand, ts.candF);
+    Cf = ts.Cb2;
+    candF = ts.candF;
     *launches += 2;
+  }
+  const int ld = Gf;
+  // the final candidates: partial pivoting in one cluster
+  int C = std::max(1, std::min(cmax, (Gf + min_rpb - 1) / min_rpb));
+  while ((Gf + C - 1) / C > kWinMaxRows) ++C;
+  if (C > cmax) return false;
+  const int rpb = (Gf + C - 1) / C;
+  const int threads = std::max(64, (2 * rpb + 31) / 32 * 32);
+  cudaMemsetAsync(ts.infc, 0, sizeof(int), s);
+  if (launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s,
+                     const_cast<float2*>(Cf), (long long)ld, Gf, 0, nb, rpb, ts.ipc,
+                     ts.infc) != cudaSuccess) {
+    cudaGetLastError();
     return false;
   }
-  tslu_perm_kernel<<<1, 1024, 0, s>>>(n, k0, nb, cand, Gc, ipc, infc, pos, at, w.ipiv, w.info);
-  tslu_rows_kernel<<<(H + 7) / 8, 256, 0, s>>>(A, lda, n, k0, nb, Cb, Gc, at, P);
-  cudaMemcpy2DAsync(A + (size_t)k0 * lda + k0, sizeof(float2) * lda, P, sizeof(float2) * H,
+  tslu_perm_kernel<<<1, 1024, sizeof(int) * 2 * (size_t)H, s>>>(n, k0, nb, candF, Gf, ts.ipc,
+                                                                ts.infc, w.ipiv, w.info, ts.moved);
+  const int rgrid = std::min((H + 7) / 8, 4 * num_sms_lu());
+  tslu_rows_kernel<<<rgrid, 256, 0, s>>>(A, lda, n, k0, nb, Cf, ld, ts.moved, ts.P);
+  cudaMemcpy2DAsync(A + (size_t)k0 * lda + k0, sizeof(float2) * lda, ts.P, sizeof(float2) * H,
                     sizeof(float2) * H, nb, cudaMemcpyDeviceToDevice, s);
-  *launches += 4;  // + the panel launch the caller counts
+  *launches += 2;  // + the cluster launch the caller counts
   return true;
 }
 
@@ -1356,7 +1458,7 @@ static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N
         return launch_tc_cgemm_sub(reinterpret_cast<float2*>(C), ld,
                                    reinterpret_cast<const float2*>(Am), ld,
                                    reinterpret_cast<const float2*>(Bm), ld, M, N, K, w.pack,
-                                   w.pack_bytes, w.status, s)
+                                   w.pack_bytes, w.status, s, w.tc_ctas)
                    ? BEM2D_ERR_CUDA
                    : BEM2D_OK;
       }
@@ -1415,8 +1517,8 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
     cudaFuncSetAttribute(dinv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(sizeof(T) * kNB * kNB));
     cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(tslu_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(sizeof(float2) * kTsluMaxRows * kNB));
+    cudaFuncSetAttribute(tslu_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(int) * 2 * kTsluMaxH));
   });
   // complex64 matrices are factored in outer blocks of kOuterNB columns:
   // inside a block each 64-column panel updates only the block's columns;

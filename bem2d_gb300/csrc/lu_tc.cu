@@ -421,7 +421,7 @@ size_t tc_pack_bytes(int M, int N, int K) {
 
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
                         const float2* B, long long ldb, int M, int N, int K, void* pack,
-                        size_t pack_bytes, int* status, cudaStream_t s) {
+                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas) {
   static const cudaError_t attr = cudaFuncSetAttribute(
       tc_cgemm_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (attr != cudaSuccess) return BEM2D_ERR_CUDA;
@@ -434,7 +434,7 @@ int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda
   pack_a_kernel<<<dim3((mt * kTcBM + 127) / 128, nkc * kTcBK), 128, 0, s>>>(A, lda, M, K, nkc,
                                                                             Apk);
   pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc, Bpk);
-  const int grid = std::min(mt * nt, num_sms());
+  const int grid = std::min(mt * nt, max_ctas > 0 ? max_ctas : num_sms());
   tc_cgemm_sub_kernel<<<grid, kTcThreads, kTcSmem, s>>>(C, ldc, Apk, Bpk, M, N, nkc, mt, nt,
                                                         status);
   return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
