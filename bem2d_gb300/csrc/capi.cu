@@ -1441,8 +1441,7 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
   }
   alpha.push_back(a);
   if ((rc = normalize(U, a))) return rc;
-  double prev = -1, sig = a;
-  int stable = 0;
+  double sig = a;
   for (int j = 0; j < mmax; ++j) {
     double2* vn = V + (size_t)(j + 1) * n;
     double2* un = U + (size_t)(j + 1) * n;
@@ -1452,7 +1451,28 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
     reorth(V, j + 1, vn);
     double b = 0;
     if ((rc = norm_of(vn, &b))) return rc;
-    if (!(b > 1e-300)) break;
+    {
+      // the largest Ritz value theta^2 of T = B^H B (alpha_0..j, beta_0..j-1)
+      // with unit eigenvector y has residual r = |beta_j alpha_j y_j| as an
+      // eigenpair of A^H A, so |sigma^2 - theta^2| <= min(r, r^2 / gap)
+      // (gap: to the next Ritz value); stop when that bounds the relative
+      // error of sigma by tol
+      const int k = (int)alpha.size();
+      std::vector<double> d(k), e(k, 0.0), e1(k > 1 ? k - 1 : 0), ev;
+      for (int i = 0; i < k; ++i) {
+        d[i] = alpha[i] * alpha[i] + (i > 0 ? beta[i - 1] * beta[i - 1] : 0.0);
+        if (i + 1 < k) e[i] = e1[i] = alpha[i] * beta[i];
+      }
+      if (!tridiag_eigenvalues(d, e, &ev)) return fail(c, BEM2D_ERR_NOCONV, "tridiagonal QL failed");
+      std::sort(ev.begin(), ev.end());
+      const double l1 = ev.back(), l2 = k > 1 ? ev[k - 2] : 0.0;
+      sig = std::sqrt(l1);
+      const std::vector<double> y = tridiag_eigenvector(d, e1, l1);
+      const double r = std::fabs(b * alpha[k - 1] * y[k - 1]);
+      const double gap = l1 - l2;
+      const double err = (k > 1 && gap > 0) ? std::min(r, r * r / gap) : r;
+      if (!(b > 1e-300) || err <= 2.0 * tol * l1) break;
+    }
     beta.push_back(b);
     if ((rc = normalize(vn, b))) return rc;
     // u_{j+1} = (op v_{j+1} - beta_j u_j) / alpha_{j+1}
@@ -1463,21 +1483,6 @@ static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const c
     if (!(a > 1e-300)) break;
     alpha.push_back(a);
     if ((rc = normalize(un, a))) return rc;
-    // largest eigenvalue of B^T B (B: alpha on the diagonal, beta above)
-    const int k = (int)alpha.size();
-    std::vector<double> d(k), e(k, 0.0), ev;
-    for (int i = 0; i < k; ++i) {
-      d[i] = alpha[i] * alpha[i] + (i > 0 ? beta[i - 1] * beta[i - 1] : 0.0);
-      if (i + 1 < k) e[i] = alpha[i] * beta[i];
-    }
-    if (!tridiag_eigenvalues(d, e, &ev)) return fail(c, BEM2D_ERR_NOCONV, "tridiagonal QL failed");
-    sig = std::sqrt(*std::max_element(ev.begin(), ev.end()));
-    if (prev > 0 && std::fabs(sig - prev) <= tol * sig) {
-      if (++stable >= 2 && j >= 3) break;
-    } else {
-      stable = 0;
-    }
-    prev = sig;
   }
   *sigma = sig;
   if (ritz) {
