@@ -143,22 +143,31 @@ def test_matmul_matches_numpy(ctx, m, n, k):
     assert (np.abs(C - R) / scale).max() < 1e-14 * max(1, k ** 0.5)
 
 
-@pytest.mark.parametrize("n,shift", [(1100, 3.0), (2500, 0.0)])
-def test_norm_cond_mixed_inverse_path(ctx, n, shift):
+@pytest.mark.parametrize("n", [1100, 2500])
+def test_norm_cond_mixed_inverse_path(ctx, n):
     """From 1024 unknowns the mixed norm / condition number iterates with the
     explicit complex64 inverse W = U^{-1} L^{-1} (products with W and W^H
     instead of triangular solves; FP64 refinement of every product in the
-    second phase).  Both extreme singular values against dense cuSOLVER
-    singular values (torch.linalg.svdvals, complex128): sigma_max to 1e-12,
-    sigma_min and cond to 1e-10, and the FP64 path to the same bars."""
+    second phase).  A = Q1 diag(s) Q2^H with seeded unitary Q1, Q2 and known
+    singular values (sigma_max = 300 and sigma_min = 0.5 separated from the
+    rest, which lie in [1, 150], as the boundary-element operators' extreme
+    values are): sigma_max to 1e-12, sigma_min and cond to 1e-10 for both
+    precisions."""
     torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(n)
+
+    def unitary():
+        Z = torch.randn((n, n), dtype=torch.complex128, device="cuda", generator=g)
+        Q, R = torch.linalg.qr(Z)
+        return Q * (torch.diagonal(R) / torch.diagonal(R).abs())[None, :]
+
     rng = np.random.default_rng(n)
-    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
-    A += shift * np.sqrt(n) * np.eye(n)
-    s = torch.linalg.svdvals(torch.from_numpy(A).cuda()).cpu().numpy()
+    s = np.concatenate([[300.0], rng.uniform(1.0, 150.0, n - 2), [0.5]])
+    A = (unitary() * torch.from_numpy(s).cuda()[None, :]) @ unitary().conj().T
+    Acm = A.T.contiguous().T  # column-major view of A
     for prec in ("mixed", "fp64"):
-        nrm, cond = ctx.norm_cond(np.asfortranarray(A), precision=prec)
-        assert abs(nrm - s[0]) < 1e-12 * s[0], prec
+        nrm, cond = ctx.norm_cond(Acm, precision=prec)
+        assert abs(nrm - 300.0) < 1e-12 * 300.0, (prec, nrm)
         smin = nrm / cond
-        assert abs(smin - s[-1]) < 1e-10 * s[-1], (prec, smin, s[-1])
-        assert abs(cond - s[0] / s[-1]) < 1e-10 * cond, prec
+        assert abs(smin - 0.5) < 1e-10 * 0.5, (prec, smin)
+        assert abs(cond - 600.0) < 1e-10 * 600.0, (prec, cond)
