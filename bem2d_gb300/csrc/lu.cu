@@ -1038,18 +1038,19 @@ static cudaError_t launch_cluster(K kern, int C, int threads, size_t smem, cudaS
 constexpr int kTsluMaxRows = 384;  // rows of one select CTA (one row per thread)
 constexpr int kTsluMinRows = 256;
 constexpr int kTsluMaxCand = kMaxClusterPanel * kWinMaxRows;  // 4096
-constexpr int kTsluFinalCand = 1024;  // candidates left for the cluster kernel
+constexpr int kTsluFinalCand = 1024;  // capacity of the second candidates' buffer
+constexpr int kTsluLastCand = 256;    // candidates left for the final factorisation (one CTA)
 constexpr int kTsluMaxH = 64 * kTsluMaxRows;                  // tallest panel (24576)
 
 // Scratch of the tournament, behind the panel exchange slots in
 // LuWork::scratch.
 struct TsluScratch {
-  float2* Cb;    // [kTsluMaxCand][kNB] level-1 candidates (original values)
-  float2* Cb2;   // [kTsluFinalCand][kNB] level-2 candidates
+  float2* Cb;    // [kTsluMaxCand][kNB] candidates of rounds 1, 3, ... (original values)
+  float2* Cb2;   // [kTsluFinalCand][kNB] candidates of rounds 2, 4, ...
   float2* P;     // [H][kNB] the factored panel
-  int* cand;     // [kTsluMaxCand] rows of A (level 1)
-  int* cand2;    // [kTsluFinalCand] rows of Cb (level 2)
-  int* candF;    // [kTsluFinalCand] rows of A of the final candidates
+  int* sel;      // [kTsluMaxCand] a round's picks (rows of its input)
+  int* mapX;     // [kTsluMaxCand] rows of A of a round's candidates
+  int* mapY;     // [kTsluMaxCand] (alternating with mapX)
   int* ipc;      // [kNB] the final candidates' interchanges
   int* infc;     // [1] their first zero pivot
   int* moved;    // [2 kNB + 1] count, then (position, row) pairs beyond the pivots
@@ -1061,7 +1062,7 @@ static size_t slots_region() {
 static size_t tslu_bytes(int n) {
   if (n <= kTsluMaxCand) return 0;
   return sizeof(float2) * (size_t)(kTsluMaxCand + kTsluFinalCand + n) * kNB +
-         sizeof(int) * ((size_t)kTsluMaxCand + 2 * kTsluFinalCand + 4 * kNB + 64) + 2048;
+         sizeof(int) * ((size_t)3 * kTsluMaxCand + 4 * kNB + 64) + 2048;
 }
 static TsluScratch tslu_scratch(void* base, int n) {
   auto al = [](char* q) { return reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(q) + 255) / 256 * 256); };
@@ -1073,10 +1074,10 @@ static TsluScratch tslu_scratch(void* base, int n) {
   p = al(p + sizeof(float2) * (size_t)kTsluFinalCand * kNB);
   t.P = reinterpret_cast<float2*>(p);
   p = al(p + sizeof(float2) * (size_t)n * kNB);
-  t.cand = reinterpret_cast<int*>(p);
-  t.cand2 = t.cand + kTsluMaxCand;
-  t.candF = t.cand2 + kTsluFinalCand;
-  t.ipc = t.candF + kTsluFinalCand;
+  t.sel = reinterpret_cast<int*>(p);
+  t.mapX = t.sel + kTsluMaxCand;
+  t.mapY = t.mapX + kTsluMaxCand;
+  t.ipc = t.mapY + kTsluMaxCand;
   t.infc = t.ipc + kNB;
   t.moved = t.infc + 32;
   return t;
@@ -1085,18 +1086,24 @@ static TsluScratch tslu_scratch(void* base, int n) {
 size_t lu_scratch_bytes(int n) { return slots_region() + tslu_bytes(n); }
 
 // One tournament round: grid G, R threads (one row each, R a multiple of
-// 32), the block's rows held in registers (the pivot loop is unrolled, so
-// every column index is static).  Block b runs partial pivoting on rows
-// r0 .. r0 + R - 1 (r0 = k0 + b R) of columns k0 .. k0 + nb - 1 and writes
-// the rows it pivoted on (absolute indices) to cand[b nb + c], -1 for steps
-// not taken.
+// 32, at most kTsluMaxRows).  Block b runs partial pivoting on rows r0 ..
+// r0 + R - 1 (r0 = k0 + b R) of columns k0 .. k0 + nb - 1 and writes the
+// rows it pivoted on (absolute indices) to cand[b nb + c], -1 for steps not
+// taken.  Each thread holds its row in registers as a window over the
+// columns: in block q of four columns, a[i] is column 4 q + i, so every
+// register index is static while the loop over blocks stays a loop (the
+// window shifts by four after each block).  Per column: the warp's best row
+// (reduce by shuffles) stages itself in shared memory, one barrier, every
+// warp picks the block's best from the warp bests and updates its rows from
+// the staged row.  The staging area alternates between two buffers, so one
+// barrier per column suffices.
 __global__ void __launch_bounds__(kTsluMaxRows, 1)
 tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb, int R,
                    int* __restrict__ cand) {
-  __shared__ float2 prow[kNB];
-  __shared__ float wv[kTsluMaxRows / 32];
-  __shared__ int wi[kTsluMaxRows / 32];
-  __shared__ int s_piv;
+  constexpr int kW = kTsluMaxRows / 32;
+  __shared__ float2 stage[2][kW][kNB];
+  __shared__ float wv[2][kW];
+  __shared__ int wi[2][kW];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = (int)blockDim.x >> 5;
   const int r0 = k0 + blockIdx.x * R;
   const int nr = max(0, min(R, n - r0));
@@ -1107,58 +1114,57 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
     a[c] = (active && c < nb) ? A[(size_t)(k0 + c) * lda + r0 + t] : make_float2(0.f, 0.f);
   int* out = cand + (size_t)blockIdx.x * nb;
   const int npiv = min(nb, nr);
-  int done = 0;
+  int taken = 0;
+  for (int q = 0; 4 * q < npiv && taken == 4 * q; ++q) {
 #pragma unroll
-  for (int c = 0; c < kNB; ++c) {
-    if (c < npiv && done == c) {
-      // block arg-max of |re| + |im| over the rows not yet pivoted (ties: the
-      // smaller row); NaN counts as zero
-      float v = active ? cabs1(a[c]) : -1.f;
-      if (!(v >= 0.f)) v = active ? 0.f : -1.f;
-      int idx = active ? t : 0x7fffffff;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-        argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
-                     __shfl_xor_sync(0xffffffffu, idx, o));
-      if (lane == 0) {
-        wv[wid] = v;
-        wi[wid] = idx;
-      }
-      __syncthreads();
-      if (wid == 0) {
-        float v3 = lane < nw ? wv[lane] : -1.f;
-        int i3 = lane < nw ? wi[lane] : 0x7fffffff;
+    for (int cc = 0; cc < 4; ++cc) {
+      const int col = 4 * q + cc, par = cc & 1;
+      if (col < npiv && taken == col) {  // uniform over the block
+        float v = active ? cabs1(a[cc]) : -1.f;
+        if (!(v >= 0.f)) v = active ? 0.f : -1.f;  // NaN: never above a number
+        int idx = active ? t : 0x7fffffff;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
-          argmax_merge(v3, i3, __shfl_xor_sync(0xffffffffu, v3, o),
-                       __shfl_xor_sync(0xffffffffu, i3, o));
+          argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
+                       __shfl_xor_sync(0xffffffffu, idx, o));
         if (lane == 0) {
-          s_piv = i3;
-          out[c] = (i3 >= 0 && i3 < nr) ? r0 + i3 : -1;
+          wv[par][wid] = v;
+          wi[par][wid] = idx;
         }
-      }
-      __syncthreads();
-      const int p = s_piv;
-      if (p >= 0 && p < nr) {
-        if (t == p) {  // stage the pivot row; it is not updated from here on
+        if (t == idx) {  // the warp's best row: stage columns col .. (window cc ..)
 #pragma unroll
-          for (int j = c; j < kNB; ++j) prow[j] = a[j];
-          active = false;
+          for (int j = cc; j < kNB; ++j) stage[par][wid][j] = a[j];
         }
         __syncthreads();
-        if (active) {
-          const float2 pv = prow[c];
-          if (pv.x != 0.f || pv.y != 0.f) {
-            const float2 l = cmul(a[c], crcp(pv));
+        float bv = lane < nw ? wv[par][lane] : -1.f;
+        int bi = lane < nw ? wi[par][lane] : 0x7fffffff;
 #pragma unroll
-            for (int j = c + 1; j < kNB; ++j) a[j] = cfms(a[j], l, prow[j]);
+        for (int o = 16; o > 0; o >>= 1)
+          argmax_merge(bv, bi, __shfl_xor_sync(0xffffffffu, bv, o),
+                       __shfl_xor_sync(0xffffffffu, bi, o));
+        const int p = bi;  // an active row (one is left while col < nr)
+        if (p >= 0 && p < nr) {
+          if (t == 0) out[col] = r0 + p;
+          if (t == p) active = false;  // the pivot row is not updated from here on
+          if (active) {
+            const float2* pr = stage[par][p >> 5];
+            const float2 pv = pr[cc];
+            if (pv.x != 0.f || pv.y != 0.f) {
+              const float2 l = cmul(a[cc], crcp(pv));
+#pragma unroll
+              for (int j = cc + 1; j < kNB; ++j) a[j] = cfms(a[j], l, pr[j]);
+            }
           }
+          taken = col + 1;
         }
-        done = c + 1;
       }
     }
+#pragma unroll
+    for (int i = 0; i < kNB - 4; ++i) a[i] = a[i + 4];
+#pragma unroll
+    for (int i = kNB - 4; i < kNB; ++i) a[i] = make_float2(0.f, 0.f);
   }
-  for (int j = done + t; j < nb; j += blockDim.x) out[j] = -1;  // steps not taken
+  for (int j = taken + t; j < nb; j += blockDim.x) out[j] = -1;  // steps not taken
 }
 
 // Cb (Gc x nb, column-major, ld Gc) = rows src[j] of S (column-major, ld
@@ -1301,53 +1307,57 @@ static int num_sms_lu() {
 // false: not applicable (taller than the tournament holds, scratch too
 // small, or the cluster launch refused); A and ipiv are then untouched.
 static bool tslu_panel(float2* A, long long lda, int n, int k0, int nb, const LuWork& w, int cmax,
-                       int min_rpb, cudaStream_t s, long long* launches) {
+                       cudaStream_t s, long long* launches) {
   const int H = n - k0;
   if (H > kTsluMaxH || tslu_bytes(n) == 0 ||
       w.scratch_bytes < slots_region() + tslu_bytes(n))
     return false;
-  const int gmax = std::min(kTsluMaxCand, cmax * kWinMaxRows) / nb;
-  const int R = std::max(kTsluMinRows, ((H + gmax - 1) / gmax + 31) / 32 * 32);
-  if (R > kTsluMaxRows) return false;
-  const int G = (H + R - 1) / R, Gc = G * nb;
+  const int gmax = kTsluMaxCand / nb;
+  const int R0 = std::max(kTsluMinRows, ((H + gmax - 1) / gmax + 31) / 32 * 32);
+  if (R0 > kTsluMaxRows) return false;
   const TsluScratch ts = tslu_scratch(static_cast<char*>(w.scratch) + slots_region(), n);
-  // round 1: blocks of R rows of the panel -> Gc candidates (a launch the
-  // GPU refuses leaves the panel to the other kernels)
+  // rounds: blocks of the current candidates (the panel's rows first), one
+  // CTA each, until at most kTsluLastCand are left; a launch the GPU refuses
+  // leaves the panel to the other kernels (A is only read until the end)
+  const float2* src = A;
+  long long lds = lda;
+  int koff = k0, rows = H, round = 0, R = R0;
+  int* mapPrev = nullptr;
+  int* mapNext = ts.mapX;
+  float2* Cf = ts.Cb;
+  int Gf = 0;
   cudaGetLastError();
-  tslu_select_kernel<<<G, R, 0, s>>>(A, lda, n, k0, nb, R, ts.cand);
-  if (cudaGetLastError() != cudaSuccess) return false;
-  tslu_gather_kernel<<<dim3((Gc + 255) / 256, nb), 256, 0, s>>>(A, lda, k0, nb, ts.cand, Gc, ts.Cb,
-                                                                nullptr, nullptr);
-  const float2* Cf = ts.Cb;
-  const int* candF = ts.cand;
-  int Gf = Gc;
-  *launches += 2;
-  if (Gc > kTsluFinalCand) {
-    // round 2: blocks of the candidates -> at most kTsluFinalCand
-    const int R2 = std::max(kTsluMinRows, ((Gc + kTsluFinalCand / nb - 1) / (kTsluFinalCand / nb) +
-                                           31) / 32 * 32);
-    const int G2 = (Gc + R2 - 1) / R2;
-    Gf = G2 * nb;
-    if (R2 > kTsluMaxRows || Gf > kTsluFinalCand) return false;
-    tslu_select_kernel<<<G2, R2, 0, s>>>(ts.Cb, Gc, Gc, 0, nb, R2, ts.cand2);
+  for (;;) {
+    const int G = (rows + R - 1) / R;
+    Gf = G * nb;
+    Cf = (round & 1) ? ts.Cb2 : ts.Cb;
+    if (Gf > ((round & 1) ? kTsluFinalCand : kTsluMaxCand)) return false;
+    tslu_select_kernel<<<G, R, 0, s>>>(src, lds, koff + rows, koff, nb, R, ts.sel);
     if (cudaGetLastError() != cudaSuccess) return false;
-    tslu_gather_kernel<<<dim3((Gf + 255) / 256, nb), 256, 0, s>>>(ts.Cb, Gc, 0, nb, ts.cand2, Gf,
-                                                                  ts.Cb2, ts.cand, ts.candF);
-    Cf = ts.Cb2;
-    candF = ts.candF;
+    tslu_gather_kernel<<<dim3((Gf + 255) / 256, nb), 256, 0, s>>>(src, lds, koff, nb, ts.sel, Gf,
+                                                                  Cf, mapPrev, mapNext);
     *launches += 2;
+    if (Gf <= kTsluLastCand || G == 1) break;
+    src = Cf;
+    lds = Gf;
+    koff = 0;
+    rows = Gf;
+    R = kTsluMinRows;
+    mapPrev = mapNext;
+    mapNext = (mapNext == ts.mapX) ? ts.mapY : ts.mapX;
+    ++round;
   }
+  const int* candF = mapNext;
   const int ld = Gf;
-  // the final candidates: partial pivoting in one cluster
-  int C = std::max(1, std::min(cmax, (Gf + min_rpb - 1) / min_rpb));
-  while ((Gf + C - 1) / C > kWinMaxRows) ++C;
+  // the final candidates: partial pivoting in one cluster (one CTA for up to
+  // 256 rows)
+  int C = std::max(1, (Gf + kWinMaxRows - 1) / kWinMaxRows);
   if (C > cmax) return false;
   const int rpb = (Gf + C - 1) / C;
   const int threads = std::max(64, (2 * rpb + 31) / 32 * 32);
   cudaMemsetAsync(ts.infc, 0, sizeof(int), s);
-  if (launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s,
-                     const_cast<float2*>(Cf), (long long)ld, Gf, 0, nb, rpb, ts.ipc,
-                     ts.infc) != cudaSuccess) {
+  if (launch_cluster(panel_win_kernel, C, threads, panel_win_smem(rpb), s, Cf, (long long)ld, Gf,
+                     0, nb, rpb, ts.ipc, ts.infc) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
@@ -1559,9 +1569,8 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
       }
     }
     if (!done && sizeof(T) == sizeof(float2)) {  // taller: tournament pivoting
-      const int min_rpb = std::min(kWinMaxRows, w.min_rows > 0 ? w.min_rows : kRowsMinRpb);
       done = tslu_panel(reinterpret_cast<float2*>(A), lda, n, k0, nb, w,
-                        cluster16 ? kMaxClusterPanel : 8, min_rpb, s, launches);
+                        cluster16 ? kMaxClusterPanel : 8, s, launches);
     }
     if (!done && sizeof(T) == sizeof(float2)) {  // taller: shared-memory rows panel
       for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
