@@ -1101,7 +1101,7 @@ __global__ void __launch_bounds__(kTsluMaxRows, 1)
 tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, int nb, int R,
                    int* __restrict__ cand) {
   constexpr int kW = kTsluMaxRows / 32;
-  __shared__ float2 stage[2][kW][kNB];
+  __shared__ __align__(16) float2 stage[2][kW][kNB];
   __shared__ float wv[2][kW];
   __shared__ int wi[2][kW];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = (int)blockDim.x >> 5;
@@ -1131,9 +1131,12 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
           wv[par][wid] = v;
           wi[par][wid] = idx;
         }
+        const int lim = kNB - 4 * q;  // window positions still holding columns
         if (t == idx) {  // the warp's best row: stage columns col .. (window cc ..)
+          float4* st4 = reinterpret_cast<float4*>(stage[par][wid]);
 #pragma unroll
-          for (int j = cc; j < kNB; ++j) stage[par][wid][j] = a[j];
+          for (int j = cc & ~1; j < kNB; j += 2)
+            if (j < lim) st4[j >> 1] = make_float4(a[j].x, a[j].y, a[j + 1].x, a[j + 1].y);
         }
         __syncthreads();
         float bv = lane < nw ? wv[par][lane] : -1.f;
@@ -1147,12 +1150,20 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
           if (t == 0) out[col] = r0 + p;
           if (t == p) active = false;  // the pivot row is not updated from here on
           if (active) {
-            const float2* pr = stage[par][p >> 5];
-            const float2 pv = pr[cc];
+            const float4* pr4 = reinterpret_cast<const float4*>(stage[par][p >> 5]);
+            const float4 pc = pr4[cc >> 1];
+            const float2 pv = (cc & 1) ? make_float2(pc.z, pc.w) : make_float2(pc.x, pc.y);
             if (pv.x != 0.f || pv.y != 0.f) {
               const float2 l = cmul(a[cc], crcp(pv));
+              if (!(cc & 1)) a[cc + 1] = cfms(a[cc + 1], l, make_float2(pc.z, pc.w));
 #pragma unroll
-              for (int j = cc + 1; j < kNB; ++j) a[j] = cfms(a[j], l, pr[j]);
+              for (int j = (cc & ~1) + 2; j < kNB; j += 2) {
+                if (j < lim) {
+                  const float4 u = pr4[j >> 1];
+                  a[j] = cfms(a[j], l, make_float2(u.x, u.y));
+                  a[j + 1] = cfms(a[j + 1], l, make_float2(u.z, u.w));
+                }
+              }
             }
           }
           taken = col + 1;
