@@ -1148,7 +1148,8 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
                             const double* dth, double tol, int mmax, const double2* start,
                             double* lam_out, T* ritz, bool full_reorth = true,
                             double rtol = 0.0, double etol = 0.0,
-                            const double* gap_in = nullptr, double* gap_out = nullptr) {
+                            const double* gap_in = nullptr, double* gap_out = nullptr,
+                            const float2* ffhi = nullptr, const float2* fflo = nullptr) {
   int rc = 0;
   const long long qs = (long long)n * (mmax + 1);  // per-angle basis stride
   T* Q = static_cast<T*>(ws(c, LzNames<T>::Q, sizeof(T) * (size_t)qs * nang, &rc));
@@ -1245,8 +1246,18 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
   };
   for (int j = 0; j < mmax; ++j) {
     const T* Qj = Q + (size_t)j * n;
-    launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
-    launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+    if constexpr (sizeof(T) == sizeof(double2)) {
+      if (ffhi) {  // the products in float-float on the FP32 pipe
+        launch_zgemm_ff(false, ffhi, fflo, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
+        launch_zgemm_ff(true, ffhi, fflo, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+      } else {
+        launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
+        launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+      }
+    } else {
+      launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
+      launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+    }
     launch_herm_combine(n, Y1, Y2, n, theta, W, n, na, c->stream);
     // Gram-Schmidt (two passes) against q_0..q_j, or, without full
     // reorthogonalisation, against q_{j-1}, q_j only (the three-term
@@ -1940,8 +1951,16 @@ int bem2d_num_range(bem2d_ctx* c, int n, const void* A, int64_t lda, int nang,
   for (int a = 0; a < nang; ++a) gap[a] = std::max(0.0, 0.25 * gap[a] - 1e-6 * hs);
   launch_widen(n, R32, n, S64, n, nang, c->stream);
   ++c->launches;
+  // the complex128 phase's products in float-float (~1e-13 relative to
+  // |A| |x|, a hundred times below tol): A split once into fl32(A) and the
+  // rest, 16 N^2 bytes
+  float2* Ahi = static_cast<float2*>(ws(c, "nr_Ahi", sizeof(float2) * (size_t)n * n, &rc));
+  float2* Alo = static_cast<float2*>(ws(c, "nr_Alo", sizeof(float2) * (size_t)n * n, &rc));
+  if (!Ahi || !Alo) return rc;
+  launch_split_ff(dA, la, n, Ahi, Alo, c->stream);
+  ++c->launches;
   return numrange_lanczos<double2>(c, n, dA, la, nang, dth, tol, mmax, S64, lmax, nullptr, true,
-                                   0.0, tol, gap.data());
+                                   0.0, tol, gap.data(), nullptr, Ahi, Alo);
 }
 
 }  // extern "C"

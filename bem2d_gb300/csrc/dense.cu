@@ -288,6 +288,178 @@ static void zgemm_t(bool herm, const T* A, long long lda, int n, const T* B, lon
   else
     zgemm_bn_t<T, 64>(herm, A, lda, n, B, ldb, m, C, ldc, P, z, s);
 }
+// ---- complex GEMM in float-float on the FP32 pipe ----------------------------
+// C = op(A) B for complex128 data whose products are wanted to ~1e-13
+// relative (the second, FP64-accurate phase of the numerical range), on the
+// FP32 pipe, which issues 64x the FP64 pipe's FMAs on GB300.  A is given
+// split once into A_hi = fl32(A), A_lo = fl32(A - A_hi) (float2 each); B is
+// split while it is staged.  Per complex multiply-add the four hi*hi real
+// products are exact as two-products (p + e) and accumulated with two-sum
+// into a float-float sum; the hi*lo and lo*hi terms (2^-24 of the main ones)
+// and the two-product errors go into a plain FP32 companion sum; lo*lo
+// (2^-48) is dropped.  Result: hi + lo + companion, in FP64.  Partial sums
+// of a K split are reduced in FP64.
+struct FfAcc {
+  float hi, lo, x;  // value = hi + lo + x
+};
+
+__device__ __forceinline__ void ffacc_add(FfAcc& a, float p) {
+  const float s = a.hi + p;
+  const float bb = s - a.hi;
+  a.lo += (a.hi - (s - bb)) + (p - bb);
+  a.hi = s;
+}
+
+template <bool HERM, int BN>
+__global__ void __launch_bounds__(256)
+zgemm_ff_kernel(const float2* __restrict__ Ahi, const float2* __restrict__ Alo, long long lda,
+                int n, const double2* __restrict__ B, long long ldb, int m,
+                double2* __restrict__ C, long long ldc, int kchunk, long long cz, int rows) {
+  constexpr int TY = BN >= 16 ? 16 : BN, TX = 256 / TY, RA = 64 / TX, RB = BN / TY;
+  __shared__ float2 Ah[16][64 + 1], Al[16][64 + 1];
+  __shared__ float2 Bh[16][BN + 1], Bl[16][BN + 1];
+  const int i0 = blockIdx.x * 64, j0 = blockIdx.y * BN;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const int kb = blockIdx.z * kchunk, ke = min(n, kb + kchunk);
+  double2* Cz = C + (size_t)blockIdx.z * cz;
+  FfAcc re[RA][RB], im[RA][RB];
+#pragma unroll
+  for (int a = 0; a < RA; ++a)
+#pragma unroll
+    for (int b = 0; b < RB; ++b) re[a][b] = im[a][b] = FfAcc{0.f, 0.f, 0.f};
+  for (int k0 = kb; k0 < ke; k0 += 16) {
+    for (int v = threadIdx.x; v < 16 * 64; v += 256) {
+      const int kk = v / 64, ii = v - kk * 64;
+      const int i = i0 + ii, k = k0 + kk;
+      float2 h = make_float2(0.f, 0.f), l = h;
+      if (i < rows && k < ke) {
+        const size_t o = HERM ? (size_t)i * lda + k : (size_t)k * lda + i;
+        h = Ahi[o];
+        l = Alo[o];
+        if (HERM) {  // (A^H)_{ik} = conj(A_{ki})
+          h.y = -h.y;
+          l.y = -l.y;
+        }
+      }
+      Ah[kk][ii] = h;
+      Al[kk][ii] = l;
+    }
+    for (int v = threadIdx.x; v < 16 * BN; v += 256) {
+      const int jj = v / 16, kk = v - jj * 16;
+      const int j = j0 + jj, k = k0 + kk;
+      const double2 d = (j < m && k < ke) ? B[(size_t)j * ldb + k] : make_double2(0.0, 0.0);
+      const float hx = (float)d.x, hy = (float)d.y;
+      Bh[kk][jj] = make_float2(hx, hy);
+      Bl[kk][jj] = make_float2((float)(d.x - (double)hx), (float)(d.y - (double)hy));
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < 16; ++kk) {
+      float2 ah[RA], al[RA], bh[RB], bl[RB];
+#pragma unroll
+      for (int a = 0; a < RA; ++a) {
+        ah[a] = Ah[kk][tx + TX * a];
+        al[a] = Al[kk][tx + TX * a];
+      }
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        bh[b] = Bh[kk][ty + TY * b];
+        bl[b] = Bl[kk][ty + TY * b];
+      }
+#pragma unroll
+      for (int a = 0; a < RA; ++a)
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+          // re += ar br - ai bi,  im += ar bi + ai br
+          const float p1 = __fmul_rn(ah[a].x, bh[b].x), p2 = __fmul_rn(ah[a].y, bh[b].y);
+          const float p3 = __fmul_rn(ah[a].x, bh[b].y), p4 = __fmul_rn(ah[a].y, bh[b].x);
+          float xr = fmaf(ah[a].x, bh[b].x, -p1) - fmaf(ah[a].y, bh[b].y, -p2);
+          float xi = fmaf(ah[a].x, bh[b].y, -p3) + fmaf(ah[a].y, bh[b].x, -p4);
+          xr = fmaf(ah[a].x, bl[b].x, xr);
+          xr = fmaf(al[a].x, bh[b].x, xr);
+          xr = fmaf(-ah[a].y, bl[b].y, xr);
+          xr = fmaf(-al[a].y, bh[b].y, xr);
+          xi = fmaf(ah[a].x, bl[b].y, xi);
+          xi = fmaf(al[a].x, bh[b].y, xi);
+          xi = fmaf(ah[a].y, bl[b].x, xi);
+          xi = fmaf(al[a].y, bh[b].x, xi);
+          ffacc_add(re[a][b], p1);
+          ffacc_add(re[a][b], -p2);
+          ffacc_add(im[a][b], p3);
+          ffacc_add(im[a][b], p4);
+          re[a][b].x += xr;
+          im[a][b].x += xi;
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int b = 0; b < RB; ++b) {
+    const int j = j0 + ty + TY * b;
+    if (j >= m) continue;
+#pragma unroll
+    for (int a = 0; a < RA; ++a) {
+      const int i = i0 + tx + TX * a;
+      if (i < rows) {
+        const FfAcc& r = re[a][b];
+        const FfAcc& q = im[a][b];
+        Cz[(size_t)j * ldc + i] = make_double2((double)r.hi + ((double)r.lo + (double)r.x),
+                                               (double)q.hi + ((double)q.lo + (double)q.x));
+      }
+    }
+  }
+}
+
+__global__ void split_ff_kernel(const double2* __restrict__ A, long long lda, int n,
+                                float2* __restrict__ hi, float2* __restrict__ lo) {
+  const long long tot = (long long)n * n;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < tot;
+       v += (long long)gridDim.x * blockDim.x) {
+    const long long j = v / n, i = v - j * n;
+    const double2 d = A[j * lda + i];
+    const float hx = (float)d.x, hy = (float)d.y;
+    hi[v] = make_float2(hx, hy);
+    lo[v] = make_float2((float)(d.x - (double)hx), (float)(d.y - (double)hy));
+  }
+}
+
+void launch_split_ff(const double2* A, long long lda, int n, float2* hi, float2* lo,
+                     cudaStream_t s) {
+  split_ff_kernel<<<1024, 256, 0, s>>>(A, lda, n, hi, lo);
+}
+
+template <int BN>
+static void zgemm_ff_bn(bool herm, const float2* Ahi, const float2* Alo, int n, const double2* B,
+                        long long ldb, int m, double2* C, long long ldc, double2* P, int z,
+                        cudaStream_t s) {
+  const int kchunk = ((n + z - 1) / z + 15) / 16 * 16;
+  dim3 g((n + 63) / 64, (m + BN - 1) / BN, z);
+  double2* out = z > 1 ? P : C;
+  const long long lo = z > 1 ? n : ldc, cz = z > 1 ? (long long)n * m : 0;
+  if (herm)
+    zgemm_ff_kernel<true, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, B, ldb, m, out, lo, kchunk, cz, n);
+  else
+    zgemm_ff_kernel<false, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, B, ldb, m, out, lo, kchunk, cz, n);
+  if (z > 1)
+    zgemm_reduce_kernel<double2><<<dim3((n + 255) / 256, m), 256, 0, s>>>(P, cz, z, n, m, C, ldc);
+}
+
+void launch_zgemm_ff(bool herm, const float2* Ahi, const float2* Alo, int n, const double2* B,
+                     long long ldb, int m, double2* C, long long ldc, void* work,
+                     size_t work_bytes, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return;
+  const int bn = zgemm_bn(m);
+  int z = zgemm_splits(n, m, bn);
+  if (z > 1 && work_bytes < sizeof(double2) * (size_t)z * n * m) z = 1;
+  double2* P = static_cast<double2*>(work);
+  if (bn == 4)
+    zgemm_ff_bn<4>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+  else if (bn == 16)
+    zgemm_ff_bn<16>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+  else
+    zgemm_ff_bn<64>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+}
+
 void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
                   long long ldb, int m, double2* C, long long ldc, void* work,
                   size_t work_bytes, cudaStream_t s) {

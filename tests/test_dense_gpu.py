@@ -171,3 +171,29 @@ def test_norm_cond_mixed_inverse_path(ctx, n):
         smin = nrm / cond
         assert abs(smin - 0.5) < 1e-10 * 0.5, (prec, smin)
         assert abs(cond - 600.0) < 1e-10 * 600.0, (prec, cond)
+
+
+def test_num_range_mixed_matches_fp64_at_size(ctx):
+    """Unit square with 256 elements per side (N = 1024), k = 20, 36
+    angles, tol = 1e-11: the mixed scan (complex64 Lanczos, then the
+    complex128 Lanczos whose products with A run in float-float on the FP32
+    pipe) against the plain FP64 scan: |lambda_mixed - lambda_fp64| <=
+    2e-11 max |lambda| (both stop at 1e-11 of |H|), and both against dense
+    eigvalsh (torch, complex128) at six angles to the same bar."""
+    torch = pytest.importorskip("torch")
+    from bem2d_gb300 import geometry as G
+    g = G.polygon_uniform([(0, 0), (1, 0), (1, 1), (0, 1)], 256).add_poly_basis(0)
+    A = ctx.discrete_kernel(g, "combined", 20.0, 20.0, QUAD, alpha=2.0, beta=1.0)
+    B = ctx.change_basis(A, ctx.eval_ident(g, QUAD), blocks_of(g))
+    th = 2 * np.pi * np.arange(36) / 36
+    lm = ctx.num_range_lmax(B, th, tol=1e-11, precision="mixed")
+    l64 = ctx.num_range_lmax(B, th, tol=1e-11, precision="fp64")
+    scale = np.abs(l64).max()
+    assert np.abs(lm - l64).max() <= 2e-11 * scale
+    Bt = torch.from_numpy(np.asarray(B)).cuda()
+    for j in range(0, 36, 6):
+        z = complex(np.cos(th[j]), np.sin(th[j]))
+        H = 0.5 * (z * Bt + np.conj(z) * Bt.conj().T)
+        ev = float(torch.linalg.eigvalsh(H)[-1])
+        assert abs(lm[j] - ev) <= 2e-11 * scale, (j, lm[j], ev)
+        assert abs(l64[j] - ev) <= 2e-11 * scale, (j, l64[j], ev)
