@@ -1102,8 +1102,7 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
                    int* __restrict__ cand) {
   constexpr int kW = kTsluMaxRows / 32;
   __shared__ __align__(16) float2 stage[2][kW][kNB];
-  __shared__ float wv[2][kW];
-  __shared__ int wi[2][kW];
+  __shared__ unsigned wv[2][kW], wi[2][kW];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = (int)blockDim.x >> 5;
   const int r0 = k0 + blockIdx.x * R;
   const int nr = max(0, min(R, n - r0));
@@ -1120,32 +1119,33 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
     for (int cc = 0; cc < 4; ++cc) {
       const int col = 4 * q + cc, par = cc & 1;
       if (col < npiv && taken == col) {  // uniform over the block
-        float v = active ? cabs1(a[cc]) : -1.f;
-        if (!(v >= 0.f)) v = active ? 0.f : -1.f;  // NaN: never above a number
-        int idx = active ? t : 0x7fffffff;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-          argmax_merge(v, idx, __shfl_xor_sync(0xffffffffu, v, o),
-                       __shfl_xor_sync(0xffffffffu, idx, o));
+        // keys: bits of |re| + |im| plus one (non-negative floats order like
+        // their bits; 0 = not a candidate, NaN counts as zero); the warp's
+        // best key, then the smallest row holding it (LAPACK's izamax)
+        float v = cabs1(a[cc]);
+        if (!(v >= 0.f)) v = 0.f;
+        const unsigned key = active ? __float_as_uint(v) + 1u : 0u;
+        const unsigned m = __reduce_max_sync(0xffffffffu, key);
+        const unsigned lab = __reduce_min_sync(0xffffffffu, (key == m && m) ? (unsigned)t : 0xffffffffu);
         if (lane == 0) {
-          wv[par][wid] = v;
-          wi[par][wid] = idx;
+          wv[par][wid] = m;
+          wi[par][wid] = lab;
         }
         const int lim = kNB - 4 * q;  // window positions still holding columns
-        if (t == idx) {  // the warp's best row: stage columns col .. (window cc ..)
+        if (m && (unsigned)t == lab) {  // the warp's best row: stage columns col ..
           float4* st4 = reinterpret_cast<float4*>(stage[par][wid]);
 #pragma unroll
-          for (int j = cc & ~1; j < kNB; j += 2)
-            if (j < lim) st4[j >> 1] = make_float4(a[j].x, a[j].y, a[j + 1].x, a[j + 1].y);
+          for (int j = cc & ~1; j < kNB; j += 2) {
+            if (j >= lim) break;
+            st4[j >> 1] = make_float4(a[j].x, a[j].y, a[j + 1].x, a[j + 1].y);
+          }
         }
         __syncthreads();
-        float bv = lane < nw ? wv[par][lane] : -1.f;
-        int bi = lane < nw ? wi[par][lane] : 0x7fffffff;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-          argmax_merge(bv, bi, __shfl_xor_sync(0xffffffffu, bv, o),
-                       __shfl_xor_sync(0xffffffffu, bi, o));
-        const int p = bi;  // an active row (one is left while col < nr)
+        const unsigned kv = lane < nw ? wv[par][lane] : 0u;
+        const unsigned bm = __reduce_max_sync(0xffffffffu, kv);
+        const unsigned bl = __reduce_min_sync(0xffffffffu,
+                                              (kv == bm && bm) ? wi[par][lane] : 0xffffffffu);
+        const int p = bm ? (int)bl : -1;  // an active row (one is left while col < nr)
         if (p >= 0 && p < nr) {
           if (t == 0) out[col] = r0 + p;
           if (t == p) active = false;  // the pivot row is not updated from here on
@@ -1154,15 +1154,14 @@ tslu_select_kernel(const float2* __restrict__ A, long long lda, int n, int k0, i
             const float4 pc = pr4[cc >> 1];
             const float2 pv = (cc & 1) ? make_float2(pc.z, pc.w) : make_float2(pc.x, pc.y);
             if (pv.x != 0.f || pv.y != 0.f) {
-              const float2 l = cmul(a[cc], crcp(pv));
+              const float2 l = cmul(a[cc], crcp_fast(pv));
               if (!(cc & 1)) a[cc + 1] = cfms(a[cc + 1], l, make_float2(pc.z, pc.w));
 #pragma unroll
               for (int j = (cc & ~1) + 2; j < kNB; j += 2) {
-                if (j < lim) {
-                  const float4 u = pr4[j >> 1];
-                  a[j] = cfms(a[j], l, make_float2(u.x, u.y));
-                  a[j + 1] = cfms(a[j + 1], l, make_float2(u.z, u.w));
-                }
+                if (j >= lim) break;
+                const float4 u = pr4[j >> 1];
+                a[j] = cfms(a[j], l, make_float2(u.x, u.y));
+                a[j + 1] = cfms(a[j + 1], l, make_float2(u.z, u.w));
               }
             }
           }
