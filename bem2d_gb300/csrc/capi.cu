@@ -64,6 +64,9 @@ struct bem2d_ctx {
   cudaEvent_t ev_asm = nullptr, ev_sol = nullptr;
   int panel_min_rows = 0;  // LuWork::min_rows of this context's factorisations
   int tc_ctas = 0;         // LuWork::tc_ctas of this context's factorisations
+  // look-ahead of large complex64 factorisations: a second stream, two events
+  cudaStream_t stream_aux = nullptr;
+  cudaEvent_t ev_u12 = nullptr, ev_far = nullptr;
 };
 
 namespace bem2d_gpu {
@@ -636,6 +639,7 @@ void bem2d_ctx_destroy(bem2d_ctx* c) {
   for (bem2d_ctx* w : c->workers) bem2d_ctx_destroy(w);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->stream_aux) cudaStreamSynchronize(c->stream_aux);
   for (auto& kv : c->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   for (auto& kv : c->rules) cudaFree(kv.second.first);
@@ -645,6 +649,12 @@ void bem2d_ctx_destroy(bem2d_ctx* c) {
   }
   if (c->ev_asm) cudaEventDestroy(c->ev_asm);
   if (c->ev_sol) cudaEventDestroy(c->ev_sol);
+  if (c->stream_aux) {
+    cudaStreamSynchronize(c->stream_aux);
+    cudaStreamDestroy(c->stream_aux);
+  }
+  if (c->ev_u12) cudaEventDestroy(c->ev_u12);
+  if (c->ev_far) cudaEventDestroy(c->ev_far);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -802,6 +812,26 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
 
 namespace bem2d_gpu {
 
+// Look-ahead resources of a complex64 factorisation of order n (none below
+// the order that uses outer blocks).
+static int attach_lookahead(bem2d_ctx* c, LuWork& w, int n) {
+  if (!lu_lookahead(n)) return BEM2D_OK;
+  if (!c->stream_aux) {
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c->stream_aux, cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_u12, cudaEventDisableTiming));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c->ev_far, cudaEventDisableTiming));
+  }
+  int rc = 0;
+  w.pack2_bytes = lu_pack_bytes(n);
+  w.pack2 = ws(c, "lu_pack2", w.pack2_bytes, &rc);
+  if (!w.pack2) return rc;
+  w.aux = c->stream_aux;
+  w.ev_u12 = c->ev_u12;
+  w.ev_far = c->ev_far;
+  w.aux_ctas = lu_lookahead_ctas();
+  return BEM2D_OK;
+}
+
 // Solve with device-resident A (lda) and b; x written to device memory.
 // A32pre: a complex64 copy of A already in the "lu32" workspace (mixed
 // assembly writes it); otherwise A is converted here.
@@ -868,6 +898,7 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
   if (!LU) return rc;
   w.pack_bytes = lu_pack_bytes(n);
   w.pack = ws(c, "lu_pack", w.pack_bytes, &rc);
+  if (w.pack && (rc = attach_lookahead(c, w, n))) return rc;
   if (!w.pack) return rc;
   double2* r = static_cast<double2*>(ws(c, "ir_r", sizeof(double2) * n, &rc));
   float2* d = static_cast<float2*>(ws(c, "ir_d", sizeof(float2) * n, &rc));
@@ -1665,6 +1696,7 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
     w.pack_bytes = lu_pack_bytes(n);
     w.pack = ws(c, "lu_pack", w.pack_bytes, &rc);
     if (!w.pack) return rc;
+    if ((rc = attach_lookahead(c, w, n))) return rc;
     launch_to_c64(dA, la, static_cast<float2*>(LU), n, n, n, c->stream);
     ++c->launches;
     rc = lu_factor<float2>(static_cast<float2*>(LU), n, n, w, c->stream, &c->launches);

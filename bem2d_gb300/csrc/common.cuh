@@ -434,6 +434,15 @@ struct LuWork {
   // persistent CTAs of the tensor-core update (0: one per SM); fewer leave
   // SMs to concurrent factorisations
   int tc_ctas = 0;
+  // look-ahead of the blocked complex64 factorisation (all set, or none):
+  // the trailing update of the columns beyond the next block runs on `aux`
+  // (packing buffer pack2, aux_ctas persistent CTAs) while the next block's
+  // panels run on the main stream; ev_u12 / ev_far order the two
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_u12 = nullptr, ev_far = nullptr;
+  void* pack2 = nullptr;
+  size_t pack2_bytes = 0;
+  int aux_ctas = 0;
 };
 
 // Bytes of LuWork::scratch the panel kernels need for n unknowns.
@@ -442,6 +451,12 @@ size_t lu_scratch_bytes(int n);
 size_t lu_aux_bytes(int n, size_t elem);
 // Bytes of LuWork::pack for a complex64 factorisation of order n.
 size_t lu_pack_bytes(int n);
+// Whether a complex64 factorisation of order n uses the look-ahead (and so
+// LuWork::aux, ev_u12, ev_far, pack2 of lu_pack_bytes(n) bytes), and the
+// persistent CTAs its far updates get (the rest of the SMs stay free for
+// the next block's panels).
+bool lu_lookahead(int n);
+int lu_lookahead_ctas();
 
 // LU with partial pivoting in place; T = double2 (complex128) or float2.
 // Also fills w.perm and w.dinv for lu_solve.

@@ -253,6 +253,30 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
   }
 }
 
+// Row swaps ipiv[k0 .. k0 + np) (LAPACK order) on columns [c0, c1).
+template <typename T>
+__global__ void laswp_cols_kernel(T* __restrict__ A, long long lda, const int* __restrict__ ipiv,
+                                  int k0, int np, int c0, int c1) {
+  const int j = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= c1) return;
+  T* col = A + (size_t)j * lda;
+  for (int s = 0; s < np; ++s) {
+    const int p = ipiv[k0 + s];
+    if (p != k0 + s) {
+      const T t = col[k0 + s];
+      col[k0 + s] = col[p];
+      col[p] = t;
+    }
+  }
+}
+template <typename T>
+static void laswp_cols(T* A, long long lda, const int* ipiv, int k0, int np, int c0, int c1,
+                       cudaStream_t s, long long* launches) {
+  if (c1 <= c0 || np <= 0) return;
+  laswp_cols_kernel<T><<<(c1 - c0 + 127) / 128, 128, 0, s>>>(A, lda, ipiv, k0, np, c0, c1);
+  ++*launches;
+}
+
 // Row swaps of panel [k0, k0+nb) on every column outside it.
 template <typename T>
 __global__ void laswp_kernel(T* __restrict__ A, long long lda, int n,
@@ -1462,6 +1486,16 @@ size_t lu_pack_bytes(int n) {
   return tc_pack_bytes(n, n, n >= kOuterMinN ? kOuterNB : kNB);
 }
 
+// SMs left to the panels while a look-ahead update runs beside them
+constexpr int kLookaheadFreeSMs = 40;
+bool lu_lookahead(int n) { return n >= kOuterMinN; }
+int lu_lookahead_ctas() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return std::max(1, v - kLookaheadFreeSMs);
+}
+
 size_t lu_aux_bytes(int n, size_t elem) {
   const size_t nk = (n + kNB - 1) / kNB;
   return sizeof(int) * (size_t)n + 2 * nk * kNB * kNB * elem + 256;
@@ -1552,6 +1586,20 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
   // kOuterNB on the tensor cores), which reads and writes the trailing
   // matrix once per block instead of once per panel.
   const int outer = (sizeof(T) == sizeof(float2) && n >= kOuterMinN) ? kOuterNB : kNB;
+  // look-ahead (complex64, outer blocks): block b's update of the columns
+  // beyond block b + 1 runs on w.aux while block b + 1's panels run here;
+  // until that update is done, block b + 1 applies its row swaps to its own
+  // columns only (the update reads block b's L21 and writes the columns
+  // beyond), then to the rest
+  const bool la = outer > kNB && w.aux && w.ev_u12 && w.ev_far && w.pack2 &&
+                  w.pack2_bytes >= lu_pack_bytes(n);
+  LuWork w2 = w;  // the far updates' work: second packing buffer, fewer CTAs
+  if (la) {
+    w2.pack = w.pack2;
+    w2.pack_bytes = w.pack2_bytes;
+    w2.tc_ctas = w.aux_ctas;
+  }
+  bool far_pending = false;
   for (int K0 = 0; K0 < n; K0 += outer) {
   const int bend = std::min(n, K0 + outer);
   for (int k0 = K0; k0 < bend; k0 += kNB) {
@@ -1637,7 +1685,10 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
       if (e != cudaSuccess) return BEM2D_ERR_CUDA;
     }
     ++*launches;
-    if (n > nb) {
+    if (la) {  // the block's own columns; the rest after the far update
+      laswp_cols(A, lda, w.ipiv, k0, nb, K0, k0, s, launches);
+      laswp_cols(A, lda, w.ipiv, k0, nb, k0 + nb, bend, s, launches);
+    } else if (n > nb) {
       laswp_kernel<T><<<(n - nb + 127) / 128, 128, 0, s>>>(A, lda, n, w.ipiv, k0, nb);
       ++*launches;
     }
@@ -1649,6 +1700,12 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
                           A + (size_t)c0 * lda + k0, lda, n - c0, ncb, nb, w, s, launches);
       if (rc) return rc;
     }
+  }
+  if (la) {  // the block's swaps on the columns outside it
+    if (far_pending && cudaStreamWaitEvent(s, w.ev_far, 0) != cudaSuccess) return BEM2D_ERR_CUDA;
+    far_pending = false;
+    laswp_cols(A, lda, w.ipiv, K0, bend - K0, 0, K0, s, launches);
+    laswp_cols(A, lda, w.ipiv, K0, bend - K0, bend, n, s, launches);
   }
   // columns right of the block: U12 = L11^{-1} A12 block row by block row,
   // then A22 -= L21 U12 with K = the block width
@@ -1663,11 +1720,32 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
         if (rc) return rc;
       }
     }
-    int rc = update_sub(A + (size_t)bend * lda + bend, A + (size_t)K0 * lda + bend,
-                        A + (size_t)bend * lda + K0, lda, nc, nc, bend - K0, w, s, launches);
-    if (rc) return rc;
+    if (la) {
+      // the next block's columns here; the columns beyond it on w.aux
+      const int next = std::min(n, bend + outer);
+      int rc = update_sub(A + (size_t)bend * lda + bend, A + (size_t)K0 * lda + bend,
+                          A + (size_t)bend * lda + K0, lda, nc, next - bend, bend - K0, w, s,
+                          launches);
+      if (rc) return rc;
+      if (next < n) {
+        if (cudaEventRecord(w.ev_u12, s) != cudaSuccess ||
+            cudaStreamWaitEvent(w.aux, w.ev_u12, 0) != cudaSuccess)
+          return BEM2D_ERR_CUDA;
+        rc = update_sub(A + (size_t)next * lda + bend, A + (size_t)K0 * lda + bend,
+                        A + (size_t)next * lda + K0, lda, nc, n - next, bend - K0, w2, w.aux,
+                        launches);
+        if (rc) return rc;
+        if (cudaEventRecord(w.ev_far, w.aux) != cudaSuccess) return BEM2D_ERR_CUDA;
+        far_pending = true;
+      }
+    } else {
+      int rc = update_sub(A + (size_t)bend * lda + bend, A + (size_t)K0 * lda + bend,
+                          A + (size_t)bend * lda + K0, lda, nc, nc, bend - K0, w, s, launches);
+      if (rc) return rc;
+    }
   }
   }
+  if (far_pending && cudaStreamWaitEvent(s, w.ev_far, 0) != cudaSuccess) return BEM2D_ERR_CUDA;
   // solve aids: permutation and diagonal-block inverses
   const int nk = (n + kNB - 1) / kNB;
   perm_kernel<<<1, 1024, sizeof(int) * n, s>>>(n, w.ipiv, w.perm);
