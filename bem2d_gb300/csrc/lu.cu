@@ -1488,7 +1488,10 @@ size_t lu_pack_bytes(int n) {
 
 // SMs left to the panels while a look-ahead update runs beside them
 constexpr int kLookaheadFreeSMs = 40;
-bool lu_lookahead(int n) { return n >= kOuterMinN; }
+#ifndef BEM2D_LOOKAHEAD_MIN_N
+#define BEM2D_LOOKAHEAD_MIN_N 8192
+#endif
+bool lu_lookahead(int n) { return n >= BEM2D_LOOKAHEAD_MIN_N; }
 int lu_lookahead_ctas() {
   int dev = 0, v = 0;
   cudaGetDevice(&dev);
@@ -1586,13 +1589,14 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
   // kOuterNB on the tensor cores), which reads and writes the trailing
   // matrix once per block instead of once per panel.
   const int outer = (sizeof(T) == sizeof(float2) && n >= kOuterMinN) ? kOuterNB : kNB;
-  // look-ahead (complex64, outer blocks): block b's update of the columns
+  // look-ahead (complex64, from BEM2D_LOOKAHEAD_MIN_N on; a block is an
+  // outer block, or a single panel below kOuterMinN): block b's update of the columns
   // beyond block b + 1 runs on w.aux while block b + 1's panels run here;
   // until that update is done, block b + 1 applies its row swaps to its own
   // columns only (the update reads block b's L21 and writes the columns
   // beyond), then to the rest
-  const bool la = outer > kNB && w.aux && w.ev_u12 && w.ev_far && w.pack2 &&
-                  w.pack2_bytes >= lu_pack_bytes(n);
+  const bool la = sizeof(T) == sizeof(float2) && lu_lookahead(n) && w.aux && w.ev_u12 &&
+                  w.ev_far && w.pack2 && w.pack2_bytes >= lu_pack_bytes(n);
   LuWork w2 = w;  // the far updates' work: second packing buffer, fewer CTAs
   if (la) {
     w2.pack = w.pack2;
