@@ -416,7 +416,8 @@ def aux_record(ctx, name, steps, warmup, check=True):
 def run_aux(args):
     from bem2d_gb300 import capi
     ctx = capi.Context(0)
-    print(json.dumps(aux_record(ctx, args.workload, args.steps, args.warmup)))
+    print(json.dumps(aux_record(ctx, args.workload, args.steps, args.warmup,
+                                check=not args.no_check)))
 
 
 def run_only(args):
@@ -683,6 +684,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--workers", type=int, default=SWEEP_WORKERS,
                     help="concurrent problems (host workers, one stream each) of a sweep")
+    ap.add_argument("--no-check", action="store_true",
+                    help="norm/cond and numerical-range workloads: skip the dense cuSOLVER check")
     ap.add_argument("--no-sub", action="store_true",
                     help="headline workload only (skip the L-shape, norm/cond and "
                          "numerical-range records)")
