@@ -1422,12 +1422,12 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
 
 // Largest singular value of an operator given y = op(x) and y = op^H(x), by
 // Golub-Kahan-Lanczos bidiagonalisation with two-pass Gram-Schmidt
-// reorthogonalisation of both bases.
-// sigma_max of the operator `op` (adjoint `oph`) by Golub-Kahan-Lanczos
-// with full reorthogonalisation, until the estimate changes by less than
-// tol (relative) twice.  v0: start vector (device, need not be normalised;
-// null: the deterministic default); ritz: if not null, receives the unit
-// right Ritz vector of the final estimate (device, n entries).
+// reorthogonalisation of both bases, until the Ritz residual bound
+// min(r, r^2 / gap) of the largest Ritz value bounds its relative error by
+// tol (at most 300 steps).  v0: start vector (device, need not be
+// normalised; null: the deterministic default); ritz: if not null,
+// receives the unit right Ritz vector of the final estimate (device, n
+// entries).
 template <typename Op, typename OpH>
 static int gk_sigma_max(bem2d_ctx* c, int n, Op op, OpH oph, double tol, const char* tag,
                         double* sigma, const double2* v0 = nullptr, double2* ritz = nullptr) {
