@@ -812,6 +812,155 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
 
 namespace bem2d_gpu {
 
+// GMRES-based iterative refinement (GMRES-IR: Carson and Higham,
+// "Accelerating the solution of linear systems by iterative refinement in
+// three precisions", SIAM J. Sci. Comput. 40, 2018): the fallback of the
+// mixed solve when plain refinement with the complex64 factor stalls or
+// diverges (cond(A) times the factor's error above one).  Outer steps: r =
+// b - A x in FP64; d from GMRES on (M^{-1} A / |A|) d' = M^{-1} (r / |r|),
+// M = the complex64 factor (left preconditioning), Arnoldi basis and
+// Hessenberg matrix in FP64 (two Gram-Schmidt passes), restart length
+// kGmresM, inner tolerance 1e-6 relative; x += (|r| / |A|) d'.  Stops at
+// backward error tol, or when an outer step no longer halves it (accepted
+// if at most `accept`).  *solves counts the applications of the factor.
+static constexpr int kGmresM = 40;
+static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const double2* b,
+                    double2* x, const float2* LU, const LuWork& w, double normA, double normb,
+                    double tol, double accept, double2* r, double2* part, double* red,
+                    double* scal, bem2d_solve_info* rep, int* solves) {
+  int rc = 0;
+  const int m = std::min(n, kGmresM);
+  double2* V = static_cast<double2*>(ws(c, "gm_V", sizeof(double2) * (size_t)n * (m + 1), &rc));
+  double2* wv = static_cast<double2*>(ws(c, "gm_w", sizeof(double2) * n, &rc));
+  float2* z = static_cast<float2*>(ws(c, "gm_z", sizeof(float2) * n, &rc));
+  double2* hd = static_cast<double2*>(ws(c, "gm_h", sizeof(double2) * (m + 2) * 2, &rc));
+  double* nd = static_cast<double*>(ws(c, "gm_n", sizeof(double) * 4, &rc));
+  double2* mvp = static_cast<double2*>(ws(c, "mv_part", mv_part_bytes(n), &rc));
+  if (!V || !wv || !z || !hd || !nd || !mvp) return rc;
+  using cd = std::complex<double>;
+  // w = M^{-1} (scale v) in FP64
+  auto precond = [&](const double2* v, double scale, double2* out) -> int {
+    launch_scale_to_c64(n, v, scale, z, c->stream);
+    int e = lu_solve<float2>(LU, n, n, w, z, z, c->stream, &c->launches);
+    if (e) return fail(c, e, "triangular solve launch: %s", cudaGetErrorString(cudaGetLastError()));
+    launch_widen(n, z, n, out, n, 1, c->stream);
+    c->launches += 2;
+    ++*solves;
+    return BEM2D_OK;
+  };
+  auto host_norm = [&](const double2* v, double* out) -> int {
+    launch_batched_norm2(n, v, n, nd, 1, c->stream);
+    CUDA_TRY(c, cudaMemcpyAsync(out, nd, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    *out = std::sqrt(*out);
+    ++c->launches;
+    return BEM2D_OK;
+  };
+  auto scale_into = [&](const double2* v, double f, double2* out) -> int {
+    CUDA_TRY(c, cudaMemcpyAsync(nd + 2, &f, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    launch_batched_scale(n, v, n, nd + 2, out, n, 1, c->stream);
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // f is host memory
+    ++c->launches;
+    return BEM2D_OK;
+  };
+  double best = INFINITY;
+  for (int outer = 0; outer < 20; ++outer) {
+    // residual and backward error
+    launch_residual(A, lda, n, x, b, r, part, c->stream);
+    launch_sumsq(r, n, n, 1, red, scal + 2, c->stream);
+    launch_sumsq(x, n, n, 1, red, scal + 3, c->stream);
+    c->launches += 6;
+    double hs[2];
+    CUDA_TRY(c, cudaMemcpyAsync(hs, scal + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const double rnorm = std::sqrt(hs[0]), xnorm = std::sqrt(hs[1]);
+    const double berr = rnorm / (normA * xnorm + normb);
+    rep->residual = berr;
+    if (!std::isfinite(berr)) return fail(c, BEM2D_ERR_NONFINITE, "non-finite residual in GMRES-IR");
+    if (berr <= tol || rnorm == 0.0) return BEM2D_OK;
+    if (!(berr < 0.5 * best)) {
+      if (berr <= accept) return BEM2D_OK;
+      return fail(c, BEM2D_ERR_NOCONV, "GMRES-IR stalled at backward error %.3e", berr);
+    }
+    best = berr;
+    // v0 = M^{-1} (r / |r|) / beta
+    if ((rc = precond(r, 1.0 / rnorm, V))) return rc;
+    double beta = 0;
+    if ((rc = host_norm(V, &beta))) return rc;
+    if (!(beta > 0) || !std::isfinite(beta))
+      return fail(c, BEM2D_ERR_NONFINITE, "GMRES-IR: bad preconditioned residual");
+    if ((rc = scale_into(V, 1.0 / beta, V))) return rc;
+    std::vector<cd> H((size_t)(m + 1) * m, 0.0), g(m + 1, 0.0), cs(m), sn(m);
+    g[0] = beta;
+    int k = 0;
+    for (int j = 0; j < m; ++j) {
+      double2* vj = V + (size_t)j * n;
+      double2* vn = V + (size_t)(j + 1) * n;
+      launch_mv(A, lda, n, vj, wv, mvp, c->stream);
+      c->launches += 2;
+      if ((rc = precond(wv, 1.0 / normA, vn))) return rc;
+      std::vector<cd> h(j + 1, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        launch_batched_dots(V, 0, n, j + 1, vn, 0, hd, 0, 1, c->stream);
+        launch_batched_sub(V, 0, n, j + 1, vn, 0, hd, 0, 1, c->stream);
+        std::vector<double2> hh(j + 1);
+        CUDA_TRY(c, cudaMemcpyAsync(hh.data(), hd, sizeof(double2) * (j + 1),
+                                    cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+        for (int i = 0; i <= j; ++i) h[i] += cd(hh[i].x, hh[i].y);
+        c->launches += 2;
+      }
+      double hn = 0;
+      if ((rc = host_norm(vn, &hn))) return rc;
+      for (int i = 0; i <= j; ++i) H[(size_t)j * (m + 1) + i] = h[i];
+      H[(size_t)j * (m + 1) + j + 1] = hn;
+      // previous rotations on column j, then a new one zeroing H(j+1, j)
+      cd* col = &H[(size_t)j * (m + 1)];
+      for (int i = 0; i < j; ++i) {
+        const cd t = cs[i] * col[i] + sn[i] * col[i + 1];
+        col[i + 1] = -std::conj(sn[i]) * col[i] + cs[i] * col[i + 1];
+        col[i] = t;
+      }
+      const double a = std::abs(col[j]), bb = std::abs(col[j + 1]);
+      const double rr = std::hypot(a, bb);
+      if (rr == 0.0) {
+        cs[j] = 1.0;
+        sn[j] = 0.0;
+      } else {
+        const cd ph = a > 0 ? col[j] / a : cd(1.0, 0.0);
+        cs[j] = a / rr;
+        sn[j] = ph * std::conj(col[j + 1]) / rr;
+        col[j] = ph * rr;
+        col[j + 1] = 0.0;
+      }
+      g[j + 1] = -std::conj(sn[j]) * g[j];
+      g[j] = cs[j] * g[j];
+      k = j + 1;
+      if (std::abs(g[j + 1]) <= 1e-6 * beta || !(hn > 1e-300 * beta)) break;
+      if ((rc = scale_into(vn, 1.0 / hn, vn))) return rc;
+    }
+    // y = R^{-1} g (upper triangular k x k), d' = V y, x += (|r| / |A|) d'
+    std::vector<cd> y(k);
+    for (int i = k - 1; i >= 0; --i) {
+      cd t = g[i];
+      for (int l = i + 1; l < k; ++l) t -= H[(size_t)l * (m + 1) + i] * y[l];
+      const cd dgl = H[(size_t)i * (m + 1) + i];
+      y[i] = std::abs(dgl) > 0 ? t / dgl : cd(0.0, 0.0);
+    }
+    std::vector<double2> yd(k);
+    const double f = rnorm / normA;
+    for (int i = 0; i < k; ++i) yd[i] = make_double2(-f * y[i].real(), -f * y[i].imag());
+    CUDA_TRY(c, cudaMemcpyAsync(hd, yd.data(), sizeof(double2) * k, cudaMemcpyHostToDevice,
+                                c->stream));
+    // x -= V (-f y)
+    launch_batched_sub(V, 0, n, k, x, 0, hd, 0, 1, c->stream);
+    ++c->launches;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));  // yd is host memory
+    rep->iterations += k;
+  }
+  return fail(c, BEM2D_ERR_NOCONV, "GMRES-IR did not reach %.1e", tol);
+}
+
 // Look-ahead resources of a complex64 factorisation of order n (none below
 // the order that uses outer blocks).
 static int attach_lookahead(bem2d_ctx* c, LuWork& w, int n) {
@@ -944,18 +1093,31 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
       return fail(c, BEM2D_ERR_NONFINITE, "non-finite residual in refinement");
     }
     if (berr <= tol || rnorm == 0.0) break;
+    bool fallback = false;
     if (berr < 0.5 * best) {
       best = berr;
       stall = 0;
     } else if (++stall >= 2) {
       if (berr <= accept) break;
-      if (info) *info = rep;
-      return fail(c, BEM2D_ERR_NOCONV, "refinement stalled at backward error %.3e", berr);
+      fallback = true;
     }
     if (it >= max_it) {
       if (berr <= accept) break;
+      fallback = true;
+    }
+    if (fallback) {
+      // plain refinement cannot converge with this factor: GMRES-IR, from
+      // x = 0 if the iterates have grown away from the solution
+      if (berr > 1e-2) CUDA_TRY(c, cudaMemsetAsync(x, 0, sizeof(double2) * n, c->stream));
+      int solves = 0;
+      const int ts = tic(c, BEM2D_PHASE_SOLVE);
+      rc = gmres_ir(c, n, A, lda, b, x, LU, w, normA, normb, tol, accept, r, part, red, scal,
+                    &rep, &solves);
+      toc(c, ts);
+      rep.iterations = it + solves;
       if (info) *info = rep;
-      return fail(c, BEM2D_ERR_NOCONV, "refinement did not reach %.1e in %d steps", tol, max_it);
+      if (rc) return rc;
+      break;
     }
     // d = LU32^{-1} (r / |r|);  x += |r| d;  r = b - A x
     const int ts = tic(c, BEM2D_PHASE_SOLVE);

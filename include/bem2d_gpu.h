@@ -167,11 +167,15 @@ int bem2d_dot_prod_basfuns(bem2d_ctx* ctx, const bem2d_geometry* geom,
 /* x = A^{-1} b: replaces SolveSystem (lib/bem2d_mathroutines.cpp:323-351,
  * LAPACK zgetrf + zgetrs).  A (n x n, lda) and b are not modified.
  * BEM2D_PREC_FP64: blocked complex128 LU with partial pivoting.
- * BEM2D_PREC_MIXED: complex64 LU with partial pivoting, then FP64 iterative
+ * BEM2D_PREC_MIXED: complex64 LU with partial pivoting (tournament
+ *   pivoting for panels taller than 4096 rows), then FP64 iterative
  *   refinement with the complex128 A until the backward error
  *   ||b - A x|| / (||A||_F ||x|| + ||b||) <= tol (tol <= 0 selects 1e-14);
- *   if progress stalls first, a backward error <= max(tol, 1e-12) is
- *   accepted, otherwise BEM2D_ERR_NOCONV.  At most 30 steps. */
+ *   at most 30 steps.  If plain refinement stalls or diverges above
+ *   max(tol, 1e-12) (cond(A) too large for the complex64 factor), GMRES-IR
+ *   takes over (GMRES in FP64 preconditioned by the complex64 factor, FP64
+ *   residuals); BEM2D_ERR_NOCONV if that stalls too.  info->iterations:
+ *   refinement steps, plus the factor's applications inside GMRES-IR. */
 int bem2d_solve_system(bem2d_ctx* ctx, int n, const void* A, int64_t lda,
                        const void* b, void* x, int precision, double tol,
                        bem2d_solve_info* info);

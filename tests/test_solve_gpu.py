@@ -152,3 +152,37 @@ def test_tall_panel_zero_column_reports_its_pivot(ctx):
         with pytest.raises(capi.LapackError) as e:
             ctx.solve(Acm, b, prec, out=x)
         assert e.value.code == 101, prec
+
+
+@pytest.mark.parametrize("n,cond", [(400, 1e9), (1500, 1e10)])
+def test_mixed_gmres_ir_fallback_on_ill_conditioned(ctx, n, cond):
+    """A = Q1 diag(s) Q2^H with singular values geometric from 1 to 1/cond:
+    cond(A) times the complex64 factor's error is far above one, so plain
+    refinement cannot converge; the mixed solve must fall back to GMRES-IR
+    and still reach the FP64 backward error |b - A x| / (|A|_F |x| + |b|)
+    <= 1e-14, with a solution within cond * 1e-14 of the FP64 path's."""
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(n)
+
+    def unitary():
+        Z = torch.randn((n, n), dtype=torch.complex128, device="cuda", generator=g)
+        Q, R = torch.linalg.qr(Z)
+        return Q * (torch.diagonal(R) / torch.diagonal(R).abs())[None, :]
+
+    s = torch.logspace(0, -np.log10(cond), n, dtype=torch.float64, device="cuda")
+    A = (unitary() * s[None, :]) @ unitary().conj().T
+    b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    Acm = A.T.contiguous().T
+    xs = {}
+    for prec in ("fp64", "mixed"):
+        x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+        ctx.solve(Acm, b, prec, out=x)
+        r = torch.linalg.vector_norm(b - A @ x)
+        berr = float(r / (torch.linalg.matrix_norm(A) * torch.linalg.vector_norm(x) +
+                          torch.linalg.vector_norm(b)))
+        assert berr <= 1e-14, (prec, berr, ctx.last_info)
+        xs[prec] = x
+    assert ctx.last_info[1] > 2  # more than plain refinement's two steps
+    err = float(torch.linalg.vector_norm(xs["mixed"] - xs["fp64"]) /
+                torch.linalg.vector_norm(xs["fp64"]))
+    assert err <= cond * 1e-14, err
