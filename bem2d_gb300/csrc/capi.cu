@@ -817,10 +817,10 @@ namespace bem2d_gpu {
 // three precisions", SIAM J. Sci. Comput. 40, 2018): the fallback of the
 // mixed solve when plain refinement with the complex64 factor stalls or
 // diverges (cond(A) times the factor's error above one).  Outer steps: r =
-// b - A x in FP64; d from GMRES on (M^{-1} A / |A|) d' = M^{-1} (r / |r|),
-// M = the complex64 factor (left preconditioning), Arnoldi basis and
-// Hessenberg matrix in FP64 (two Gram-Schmidt passes), restart length
-// kGmresM, inner tolerance 1e-6 relative; x += (|r| / |A|) d'.  Stops at
+// b - A x in FP64; d from GMRES on M^{-1} A d = M^{-1} r, M = the complex64
+// factor applied in FP64 arithmetic (left preconditioning), Arnoldi basis
+// and Hessenberg matrix in FP64 (two Gram-Schmidt passes), restart length
+// kGmresM, inner tolerance 1e-6 relative; x += d.  Stops at
 // backward error tol, or when an outer step no longer halves it (accepted
 // if at most `accept`).  *solves counts the applications of the factor.
 static constexpr int kGmresM = 40;
@@ -832,19 +832,17 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
   const int m = std::min(n, kGmresM);
   double2* V = static_cast<double2*>(ws(c, "gm_V", sizeof(double2) * (size_t)n * (m + 1), &rc));
   double2* wv = static_cast<double2*>(ws(c, "gm_w", sizeof(double2) * n, &rc));
-  float2* z = static_cast<float2*>(ws(c, "gm_z", sizeof(float2) * n, &rc));
   double2* hd = static_cast<double2*>(ws(c, "gm_h", sizeof(double2) * (m + 2) * 2, &rc));
   double* nd = static_cast<double*>(ws(c, "gm_n", sizeof(double) * 4, &rc));
   double2* mvp = static_cast<double2*>(ws(c, "mv_part", mv_part_bytes(n), &rc));
-  if (!V || !wv || !z || !hd || !nd || !mvp) return rc;
+  if (!V || !wv || !hd || !nd || !mvp) return rc;
   using cd = std::complex<double>;
-  // w = M^{-1} (scale v) in FP64
-  auto precond = [&](const double2* v, double scale, double2* out) -> int {
-    launch_scale_to_c64(n, v, scale, z, c->stream);
-    int e = lu_solve<float2>(LU, n, n, w, z, z, c->stream, &c->launches);
+  // out = M^{-1} v, the complex64 factor applied in FP64 arithmetic (GMRES
+  // needs a fixed operator: complex64 arithmetic would perturb it by
+  // cond(M) times single-precision roundoff)
+  auto precond = [&](const double2* v, double2* out) -> int {
+    int e = lu_solve_mixed(LU, n, n, w, v, out, c->stream, &c->launches);
     if (e) return fail(c, e, "triangular solve launch: %s", cudaGetErrorString(cudaGetLastError()));
-    launch_widen(n, z, n, out, n, 1, c->stream);
-    c->launches += 2;
     ++*solves;
     return BEM2D_OK;
   };
@@ -883,8 +881,8 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
       return fail(c, BEM2D_ERR_NOCONV, "GMRES-IR stalled at backward error %.3e", berr);
     }
     best = berr;
-    // v0 = M^{-1} (r / |r|) / beta
-    if ((rc = precond(r, 1.0 / rnorm, V))) return rc;
+    // v0 = M^{-1} r / beta
+    if ((rc = precond(r, V))) return rc;
     double beta = 0;
     if ((rc = host_norm(V, &beta))) return rc;
     if (!(beta > 0) || !std::isfinite(beta))
@@ -898,7 +896,7 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
       double2* vn = V + (size_t)(j + 1) * n;
       launch_mv(A, lda, n, vj, wv, mvp, c->stream);
       c->launches += 2;
-      if ((rc = precond(wv, 1.0 / normA, vn))) return rc;
+      if ((rc = precond(wv, vn))) return rc;
       std::vector<cd> h(j + 1, 0.0);
       for (int pass = 0; pass < 2; ++pass) {
         launch_batched_dots(V, 0, n, j + 1, vn, 0, hd, 0, 1, c->stream);
@@ -948,8 +946,7 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
       y[i] = std::abs(dgl) > 0 ? t / dgl : cd(0.0, 0.0);
     }
     std::vector<double2> yd(k);
-    const double f = rnorm / normA;
-    for (int i = 0; i < k; ++i) yd[i] = make_double2(-f * y[i].real(), -f * y[i].imag());
+    for (int i = 0; i < k; ++i) yd[i] = make_double2(-y[i].real(), -y[i].imag());
     CUDA_TRY(c, cudaMemcpyAsync(hd, yd.data(), sizeof(double2) * k, cudaMemcpyHostToDevice,
                                 c->stream));
     // x -= V (-f y)

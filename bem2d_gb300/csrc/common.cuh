@@ -472,6 +472,10 @@ template <typename T>
 int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
              cudaStream_t s, long long* launches);
 
+// x = A^{-1} b with a complex64 factor of lu_factor<float2>, the solves
+// arithmetic in complex128 (a fixed operator; b and x may alias).
+int lu_solve_mixed(const float2* LU, long long lda, int n, const LuWork& w, const double2* b,
+                   double2* x, cudaStream_t s, long long* launches);
 // x = A^{-H} b with the factor of lu_factor (b and x must differ).
 template <typename T>
 int lu_solve_h(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,

@@ -1759,6 +1759,13 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
 }
 
 // ---- triangular solves ----------------------------------------------------
+// The solves are templated on the arithmetic type T and the factor's
+// storage type TS (TS = complex64, T = complex128: the complex64 factor
+// applied exactly in FP64, a fixed operator, as GMRES-IR needs).
+template <typename T, typename TS>
+__device__ __forceinline__ T cvt(TS v) {
+  return CTraits<T>::make(v.x, v.y);
+}
 // x = U^{-1} L^{-1} P b in one cluster launch.  CTA r owns rows
 // [r rpb, (r+1) rpb) of b in shared memory (rpb a multiple of 64).  Step k of
 // the forward sweep: the owner of block k forms y_k = L_kk^{-1} b_k from the
@@ -1767,10 +1774,10 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
 // U_kk^{-1}.  One cluster barrier per block step.  bin and xout may be the
 // same vector (every read of bin precedes the first write of xout), so
 // neither is declared __restrict__.
-template <typename T>
+template <typename T, typename TS = T>
 __global__ void __launch_bounds__(256)
-trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
-                        const int* __restrict__ perm, const T* __restrict__ dinv,
+trisolve_cluster_kernel(const TS* __restrict__ LU, long long lda, int n,
+                        const int* __restrict__ perm, const TS* __restrict__ dinv,
                         const T* bin, T* xout, int rpb) {
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -1789,14 +1796,14 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
     const int owner = k0 / rpb;
     if (rank == owner) {
       // y = D_k^{-1} b_k: four column groups of 16 per row, partial sums in ps
-      const T* Di = dinv + (size_t)(2 * kb + (fwd ? 0 : 1)) * kNB * kNB;
+      const TS* Di = dinv + (size_t)(2 * kb + (fwd ? 0 : 1)) * kNB * kNB;
       const T* bk = bc + (k0 - r0);
       const int r = threadIdx.x & 63, g = threadIdx.x >> 6;
       T acc = CTraits<T>::make(0, 0);
       if (r < nb) {
         T l[16];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) l[u] = Di[(g * 16 + u) * kNB + r];
+        for (int u = 0; u < 16; ++u) l[u] = cvt<T>(Di[(g * 16 + u) * kNB + r]);
 #pragma unroll
         for (int u = 0; u < 16; ++u)
           if (g * 16 + u < nb) acc = cfma(l[u], bk[g * 16 + u], acc);
@@ -1822,11 +1829,11 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
     const int nrows = max(hi - lo, 0);
     for (int it = threadIdx.x; it < 4 * nrows; it += blockDim.x) {
       const int g = it / nrows, r = lo + (it - g * nrows);
-      const T* col = LU + (size_t)(k0 + g * 16) * lda + r;
+      const TS* col = LU + (size_t)(k0 + g * 16) * lda + r;
       T l[16];
 #pragma unroll
       for (int u = 0; u < 16; ++u)
-        l[u] = (g * 16 + u < nb) ? col[(size_t)u * lda] : CTraits<T>::make(0, 0);
+        l[u] = (g * 16 + u < nb) ? cvt<T>(col[(size_t)u * lda]) : CTraits<T>::make(0, 0);
       T acc = CTraits<T>::make(0, 0);
 #pragma unroll
       for (int u = 0; u < 16; ++u) acc = cfma(l[u], ys[(g * 16 + u) & (kNB - 1)], acc);
@@ -1864,9 +1871,9 @@ trisolve_cluster_kernel(const T* __restrict__ LU, long long lda, int n,
 constexpr int kWaveThreads = 256;
 constexpr int kWaveMinN = 8192;  // below: the single-cluster solve (fewer launches)
 
-template <typename T, bool FWD>
+template <typename T, bool FWD, typename TS = T>
 __global__ void __launch_bounds__(kWaveThreads)
-trisolve_wave_kernel(const T* __restrict__ LU, long long lda, int n, const T* __restrict__ dinv,
+trisolve_wave_kernel(const TS* __restrict__ LU, long long lda, int n, const TS* __restrict__ dinv,
                      const int* __restrict__ perm, const T* bin, T* xout, T* ybuf, int* flags,
                      int* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1889,17 +1896,17 @@ trisolve_wave_kernel(const T* __restrict__ LU, long long lda, int n, const T* __
   const int first = g, last = g + (nown - 1) * G;  // owned block range
   // entries of the diagonal-block inverse of block k for thread (r, q)
   auto load_dinv = [&](int kb, T* d) {
-    const T* Di = dinv + (size_t)(2 * kb + (FWD ? 0 : 1)) * kNB * kNB;
+    const TS* Di = dinv + (size_t)(2 * kb + (FWD ? 0 : 1)) * kNB * kNB;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) d[u] = Di[(q * 16 + u) * kNB + r];
+    for (int u = 0; u < 16; ++u) d[u] = cvt<T>(Di[(q * 16 + u) * kNB + r]);
   };
   // factor entries of block row `blk` in the columns of block kb
   auto load_l = [&](int blk, int kb, T* l) {
     const int row = blk * kNB + r, c0 = kb * kNB + q * 16;
-    const T* col = LU + (size_t)c0 * lda + row;
+    const TS* col = LU + (size_t)c0 * lda + row;
 #pragma unroll
     for (int u = 0; u < 16; ++u)
-      l[u] = (row < n && c0 + u < n) ? col[(size_t)u * lda] : zero;
+      l[u] = (row < n && c0 + u < n) ? cvt<T>(col[(size_t)u * lda]) : zero;
   };
   // first owned block strictly beyond kb in the sweep direction, or -1
   auto next_owned = [&](int kb) -> int {
@@ -1979,8 +1986,8 @@ trisolve_wave_kernel(const T* __restrict__ LU, long long lda, int n, const T* __
   }
 }
 
-template <typename T>
-static int lu_solve_wave(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
+template <typename T, typename TS = T>
+static int lu_solve_wave(const TS* LU, long long lda, int n, const LuWork& w, const T* b, T* x,
                          cudaStream_t s, long long* launches) {
   const int nk = (n + kNB - 1) / kNB;
   // scratch: forward result v [n], y slots [nk * kNB], flags [2 * nk]
@@ -1999,21 +2006,21 @@ static int lu_solve_wave(const T* LU, long long lda, int n, const LuWork& w, con
   const size_t smem = sizeof(T) * ((size_t)((nk + G - 1) / G) * kNB + 5 * kNB);
   if (smem > 48 * 1024) return BEM2D_ERR_ARG;
   cudaMemsetAsync(flags, 0, sizeof(int) * 2 * nk, s);
-  const T* dinv = reinterpret_cast<const T*>(w.dinv);
+  const TS* dinv = reinterpret_cast<const TS*>(w.dinv);
   const int* perm = w.perm;
   int* fl = flags;
   int* status = w.status;
   T* vo = v;
   void* af[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&dinv, (void*)&perm, (void*)&b,
                 (void*)&vo, (void*)&ybuf, (void*)&fl, (void*)&status};
-  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, true>, dim3(G),
+  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, true, TS>, dim3(G),
                                   dim3(kWaveThreads), af, smem, s) != cudaSuccess)
     return BEM2D_ERR_CUDA;
   const T* vin = v;
   int* fb = flags + nk;
   void* ab[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&dinv, (void*)&perm, (void*)&vin,
                 (void*)&x, (void*)&ybuf, (void*)&fb, (void*)&status};
-  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, false>, dim3(G),
+  if (cudaLaunchCooperativeKernel((void*)trisolve_wave_kernel<T, false, TS>, dim3(G),
                                   dim3(kWaveThreads), ab, smem, s) != cudaSuccess)
     return BEM2D_ERR_CUDA;
   *launches += 2;
@@ -2043,6 +2050,38 @@ int lu_solve(const T* LU, long long lda, int n, const LuWork& w, const T* b, T* 
     if (smem > kClusterSmem) return BEM2D_ERR_ARG;
     cudaError_t e = launch_cluster(trisolve_cluster_kernel<T>, C, 256, smem, s, LU, lda, n,
                                    (const int*)w.perm, (const T*)w.dinv, b, x, rpb);
+    if (e == cudaSuccess) break;
+    cudaGetLastError();
+    if (cmax == 8) return BEM2D_ERR_CUDA;
+    cmax = 8;
+  }
+  ++*launches;
+  return BEM2D_OK;
+}
+
+// x = A^{-1} b with a complex64 factor, the arithmetic in complex128.
+int lu_solve_mixed(const float2* LU, long long lda, int n, const LuWork& w, const double2* b,
+                   double2* x, cudaStream_t s, long long* launches) {
+  if (n >= kWaveMinN) return lu_solve_wave<double2, float2>(LU, lda, n, w, b, x, s, launches);
+  static std::atomic<int> cmax{kMaxCluster};
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    cudaFuncSetAttribute(trisolve_cluster_kernel<double2, float2>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmem);
+    if (cudaFuncSetAttribute(trisolve_cluster_kernel<double2, float2>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      cmax = 8;
+    }
+  });
+  for (;;) {
+    const int nk = (n + kNB - 1) / kNB;
+    const int C = std::max(1, std::min(cmax.load(), nk));
+    const int rpb = ((nk + C - 1) / C) * kNB;
+    const size_t smem = sizeof(double2) * ((size_t)rpb + kNB + 4 * (size_t)std::max(rpb, kNB));
+    if (smem > kClusterSmem) return BEM2D_ERR_ARG;
+    cudaError_t e = launch_cluster(trisolve_cluster_kernel<double2, float2>, C, 256, smem, s, LU,
+                                   lda, n, (const int*)w.perm, (const float2*)w.dinv, b, x, rpb);
     if (e == cudaSuccess) break;
     cudaGetLastError();
     if (cmax == 8) return BEM2D_ERR_CUDA;
