@@ -821,9 +821,11 @@ namespace bem2d_gpu {
 // factor applied in FP64 arithmetic (left preconditioning), Arnoldi basis
 // and Hessenberg matrix in FP64 (two Gram-Schmidt passes), restart length
 // kGmresM, inner tolerance 1e-6 relative; x += d.  Stops at
-// backward error tol, or when an outer step no longer halves it (accepted
-// if at most `accept`).  *solves counts the applications of the factor.
-static constexpr int kGmresM = 40;
+// backward error tol, or when three outer steps in a row have not halved it
+// (accepted if at most `accept`).  *solves counts the applications of the
+// factor.  Converges in few steps when the factor's errors leave few
+// outlying eigenvalues of M^{-1} A (a few near-singular directions).
+static constexpr int kGmresM = 64;
 static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const double2* b,
                     double2* x, const float2* LU, const LuWork& w, double normA, double normb,
                     double tol, double accept, double2* r, double2* part, double* red,
@@ -862,6 +864,7 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
     return BEM2D_OK;
   };
   double best = INFINITY;
+  int stall = 0;
   for (int outer = 0; outer < 20; ++outer) {
     // residual and backward error
     launch_residual(A, lda, n, x, b, r, part, c->stream);
@@ -876,11 +879,13 @@ static int gmres_ir(bem2d_ctx* c, int n, const double2* A, long long lda, const 
     rep->residual = berr;
     if (!std::isfinite(berr)) return fail(c, BEM2D_ERR_NONFINITE, "non-finite residual in GMRES-IR");
     if (berr <= tol || rnorm == 0.0) return BEM2D_OK;
-    if (!(berr < 0.5 * best)) {
+    if (berr < 0.5 * best) {
+      best = berr;
+      stall = 0;
+    } else if (++stall >= 3) {
       if (berr <= accept) return BEM2D_OK;
       return fail(c, BEM2D_ERR_NOCONV, "GMRES-IR stalled at backward error %.3e", berr);
     }
-    best = berr;
     // v0 = M^{-1} r / beta
     if ((rc = precond(r, V))) return rc;
     double beta = 0;

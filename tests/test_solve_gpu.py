@@ -156,11 +156,13 @@ def test_tall_panel_zero_column_reports_its_pivot(ctx):
 
 @pytest.mark.parametrize("n,cond", [(400, 1e9), (1500, 1e10)])
 def test_mixed_gmres_ir_fallback_on_ill_conditioned(ctx, n, cond):
-    """A = Q1 diag(s) Q2^H with singular values geometric from 1 to 1/cond:
-    cond(A) times the complex64 factor's error is far above one, so plain
-    refinement cannot converge; the mixed solve must fall back to GMRES-IR
-    and still reach the FP64 backward error |b - A x| / (|A|_F |x| + |b|)
-    <= 1e-14, with a solution within cond * 1e-14 of the FP64 path's."""
+    """A = Q1 diag(s) Q2^H with n - 8 singular values in [0.5, 1] and eight
+    geometric from 1e-3 down to 1/cond (a few near-singular directions, as
+    near a resonance): cond(A) times the complex64 factor's error is far
+    above one, so plain refinement cannot converge; the mixed solve must
+    fall back to GMRES-IR and still reach the FP64 backward error
+    |b - A x| / (|A|_F |x| + |b|) <= 1e-14, with a solution within
+    cond * 1e-14 of the FP64 path's."""
     torch = pytest.importorskip("torch")
     g = torch.Generator(device="cuda").manual_seed(n)
 
@@ -169,7 +171,8 @@ def test_mixed_gmres_ir_fallback_on_ill_conditioned(ctx, n, cond):
         Q, R = torch.linalg.qr(Z)
         return Q * (torch.diagonal(R) / torch.diagonal(R).abs())[None, :]
 
-    s = torch.logspace(0, -np.log10(cond), n, dtype=torch.float64, device="cuda")
+    s = torch.cat([0.5 + 0.5 * torch.rand(n - 8, dtype=torch.float64, device="cuda", generator=g),
+                   torch.logspace(-3, -np.log10(cond), 8, dtype=torch.float64, device="cuda")])
     A = (unitary() * s[None, :]) @ unitary().conj().T
     b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
     Acm = A.T.contiguous().T
