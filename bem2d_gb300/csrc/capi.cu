@@ -2365,6 +2365,13 @@ std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c) { return c->workers; }
 #ifndef BEM2D_SWEEP_TC_CTAS
 #define BEM2D_SWEEP_TC_CTAS 0
 #endif
+bool ctx_timers_on(const bem2d_ctx* c) { return c->timers; }
+void ctx_add_timers(bem2d_ctx* dst, const bem2d_ctx* src) {
+  for (int i = 0; i < 4; ++i) {
+    dst->phase_ms[i] += src->phase_ms[i];
+    dst->phase_n[i] += src->phase_n[i];
+  }
+}
 int ctx_make_sweep_worker(bem2d_ctx* c) {
   c->panel_min_rows = BEM2D_SWEEP_PANEL_ROWS;
   c->tc_ctas = BEM2D_SWEEP_TC_CTAS;

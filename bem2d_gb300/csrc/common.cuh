@@ -410,6 +410,10 @@ std::vector<bem2d_ctx*>& ctx_workers(bem2d_ctx* c);
 // Makes c a sweep worker: a high-priority stream for the factor/solve phase
 // of its scattering solves and throughput-sized LU panels.
 int ctx_make_sweep_worker(bem2d_ctx* c);
+// Phase timers of a sweep: whether `c` times its phases, and adding a
+// worker's phase totals (and counts) to `dst`.
+bool ctx_timers_on(const bem2d_ctx* c);
+void ctx_add_timers(bem2d_ctx* dst, const bem2d_ctx* src);
 // Records msg as the context's last error and returns code.
 int ctx_fail(bem2d_ctx* c, int code, const char* msg);
 

@@ -64,7 +64,11 @@ extern "C" int bem2d_sweep_solve(bem2d_ctx* c, int nk, const bem2d_geometry* geo
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return geoms[a].n_unk > geoms[b].n_unk; });
   std::vector<long long> launches0(W);
-  for (int w = 0; w < W; ++w) launches0[w] = bem2d_ctx_launch_count(workers[w]);
+  const bool timed = ctx_timers_on(c);  // phase timers: summed over the problems
+  for (int w = 0; w < W; ++w) {
+    launches0[w] = bem2d_ctx_launch_count(workers[w]);
+    bem2d_ctx_enable_timers(workers[w], timed ? 1 : 0);
+  }
 
   std::atomic<int> next{0};
   std::atomic<bool> stop{false};
@@ -100,7 +104,10 @@ extern "C" int bem2d_sweep_solve(bem2d_ctx* c, int nk, const bem2d_geometry* geo
   work(0);
   for (auto& t : pool) t.join();
   long long* total = ctx_launches(c);
-  for (int w = 0; w < W; ++w) *total += bem2d_ctx_launch_count(workers[w]) - launches0[w];
+  for (int w = 0; w < W; ++w) {
+    *total += bem2d_ctx_launch_count(workers[w]) - launches0[w];
+    if (timed) ctx_add_timers(c, workers[w]);
+  }
   if (err_rc != BEM2D_OK) {
     const std::string msg = "problem " + std::to_string(err_item) + ": " + err_msg;
     return ctx_fail(c, err_rc, msg.c_str());
