@@ -208,7 +208,10 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
       const int o1 = q1 * kTileF + lane;
       const float2 a0 = rs[o1], a1 = rs[SZ + o1], a2 = rs[2 * SZ + o1], a3 = rs[3 * SZ + o1],
                    a4 = rs[4 * SZ + o1];
-      const ff ox1 = ff_make(a0.x, a0.y), oy1 = ff_make(a1.x, a1.y);
+      // the row node's position relative to the column element's centre,
+      // once per row node: (c_row - c_col) + o_row
+      const ff Px = ff_add_fast(Dx, ff_make(a0.x, a0.y));
+      const ff Py = ff_add_fast(Dy, ff_make(a1.x, a1.y));
       const ff n1x = ff_make(a2.x, a2.y), n1y = ff_make(a3.x, a3.y), w1 = ff_make(a4.x, a4.y);
 #pragma unroll 1
       for (int q2 = 0; q2 < ng; ++q2) {
@@ -216,8 +219,8 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
         const float2 b0 = cs[o2], b1 = cs[SZ + o2], b2 = cs[2 * SZ + o2], b3 = cs[3 * SZ + o2],
                      b4 = cs[4 * SZ + o2];
         // w = x - y, x a node of the row element, y of the column element
-        const ff dx = ff_add_fast(Dx, ff_add_fast(ox1, ff_make(-b0.x, -b0.y)));
-        const ff dy = ff_add_fast(Dy, ff_add_fast(oy1, ff_make(-b1.x, -b1.y)));
+        const ff dx = ff_add_fast(Px, ff_make(-b0.x, -b0.y));
+        const ff dy = ff_add_fast(Py, ff_make(-b1.x, -b1.y));
         const HankelTermsFF h = hankel_terms_ff(dx, dy, kc, tab);
         const ff aw = ff_mul(h.amp, ff_mul(w1, ff_make(b4.x, b4.y)));  // amp w_x w_y
         if (KERNEL == BEM2D_KERNEL_SINGLE) {
