@@ -482,12 +482,16 @@ __global__ void batched_dots_kernel(const T* __restrict__ Q, long long qstride, 
   if (i >= j) return;
   const T* q = Q + (size_t)c * qstride + (size_t)i * n;
   const T* w = W + (size_t)c * wstride;
-  double sr = 0, si = 0;
+  // each thread's few terms in the vectors' own precision (complex64: the
+  // FP32 pipe; FP64 accumulation there would run on the FP64 pipe, 1/64 of
+  // the rate), the 256 partial sums in FP64
+  typename CTraits<T>::R pr = 0, pi = 0;
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
     const T a = q[r], b = w[r];
-    sr += (double)a.x * b.x + (double)a.y * b.y;
-    si += (double)a.x * b.y - (double)a.y * b.x;
+    pr = fma(a.x, b.x, fma(a.y, b.y, pr));
+    pi = fma(a.x, b.y, fma(-a.y, b.x, pi));
   }
+  const double sr = pr, si = pi;
   __shared__ double red[2][256];
   red[0][threadIdx.x] = sr;
   red[1][threadIdx.x] = si;
