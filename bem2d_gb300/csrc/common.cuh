@@ -504,16 +504,6 @@ int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda
                         const float2* B, long long ldb, int M, int N, int K, void* pack,
                         size_t pack_bytes, int* status, cudaStream_t s, int max_ctas = 0);
 
-// The same update with the A operand packed once (tc_pack_a: op(A) = sign A
-// or sign A^H, M x K) and reused: C -= op(A) B.
-size_t tc_pack_a_bytes(int M, int K);
-size_t tc_pack_b_bytes(int N, int K);
-int tc_pack_a(const float2* A, long long lda, int M, int K, bool herm, float sign, void* apack,
-              cudaStream_t s);
-int launch_tc_cgemm_packed(float2* C, long long ldc, const void* apack, const float2* B,
-                           long long ldb, int M, int N, int K, void* bpack, size_t bpack_bytes,
-                           int* status, cudaStream_t s);
-
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);
 size_t residual_part_bytes(int n);

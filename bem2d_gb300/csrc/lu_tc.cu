@@ -164,26 +164,14 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned b
 // ---- packing ---------------------------------------------------------------
 // A (M x K complex) -> Apk[mt][kc] = {hi, lo} chunks of kTcApart bytes each.
 // grid: (ceil(M / 64) * 64 / 128 x nkc * 16), 128 threads
-// herm: the operand is A^H (A read transposed and conjugated); sign scales
-// it (-1: the update computes C + A B)
 __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int nkc,
-                              unsigned char* __restrict__ Apk, bool herm = false,
-                              float sign = 1.f) {
+                              unsigned char* __restrict__ Apk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;  // complex row
   const int k = blockIdx.y;                             // 0 .. nkc * 16 - 1
   const int mt = i / kTcBM, il = i - mt * kTcBM;
   const int kc = k / kTcBK, kl = k - kc * kTcBK;
   if (i >= ((M + kTcBM - 1) / kTcBM) * kTcBM) return;
-  float2 v = make_float2(0.f, 0.f);
-  if (i < M && k < K) {
-    if (herm) {
-      const float2 t = A[(size_t)i * lda + k];
-      v = make_float2(sign * t.x, -sign * t.y);
-    } else {
-      const float2 t = A[(size_t)k * lda + i];
-      v = make_float2(sign * t.x, sign * t.y);
-    }
-  }
+  const float2 v = (i < M && k < K) ? A[(size_t)k * lda + i] : make_float2(0.f, 0.f);
   unsigned char* chunk = Apk + ((size_t)mt * nkc + kc) * kTcChunkA;
   float h, l;
   tf32_split(v.x, h, l);
@@ -429,43 +417,6 @@ size_t tc_pack_bytes(int M, int N, int K) {
   const size_t nkc = (size_t)(K + kTcBK - 1) / kTcBK;
   const size_t mt = (size_t)(M + kTcBM - 1) / kTcBM, nt = (size_t)(N + kTcBN - 1) / kTcBN;
   return align256(mt * nkc * kTcChunkA) + align256(nt * nkc * kTcChunkB);
-}
-
-size_t tc_pack_a_bytes(int M, int K) {
-  const size_t nkc = (size_t)(K + kTcBK - 1) / kTcBK, mt = (size_t)(M + kTcBM - 1) / kTcBM;
-  return align256(mt * nkc * kTcChunkA);
-}
-size_t tc_pack_b_bytes(int N, int K) {
-  const size_t nkc = (size_t)(K + kTcBK - 1) / kTcBK, nt = (size_t)(N + kTcBN - 1) / kTcBN;
-  return align256(nt * nkc * kTcChunkB);
-}
-
-int tc_pack_a(const float2* A, long long lda, int M, int K, bool herm, float sign, void* apack,
-              cudaStream_t s) {
-  if (M <= 0 || K <= 0) return BEM2D_OK;
-  if (!apack) return BEM2D_ERR_ARG;
-  const int nkc = (K + kTcBK - 1) / kTcBK, mt = (M + kTcBM - 1) / kTcBM;
-  pack_a_kernel<<<dim3((mt * kTcBM + 127) / 128, nkc * kTcBK), 128, 0, s>>>(
-      A, lda, M, K, nkc, static_cast<unsigned char*>(apack), herm, sign);
-  return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
-}
-
-int launch_tc_cgemm_packed(float2* C, long long ldc, const void* apack, const float2* B,
-                           long long ldb, int M, int N, int K, void* bpack, size_t bpack_bytes,
-                           int* status, cudaStream_t s) {
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      tc_cgemm_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-  if (attr != cudaSuccess) return BEM2D_ERR_CUDA;
-  if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
-  if (!apack || !bpack || tc_pack_b_bytes(N, K) > bpack_bytes) return BEM2D_ERR_ARG;
-  const int nkc = (K + kTcBK - 1) / kTcBK;
-  const int mt = (M + kTcBM - 1) / kTcBM, nt = (N + kTcBN - 1) / kTcBN;
-  unsigned char* Bpk = static_cast<unsigned char*>(bpack);
-  pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc, Bpk);
-  const int grid = std::min(mt * nt, num_sms());
-  tc_cgemm_sub_kernel<<<grid, kTcThreads, kTcSmem, s>>>(
-      C, ldc, static_cast<const unsigned char*>(apack), Bpk, M, N, nkc, mt, nt, status);
-  return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
 }
 
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
