@@ -1338,9 +1338,6 @@ struct LzNames<float2> {
 // in two consecutive steps.  start (complex128, n per angle): start vectors
 // (normalised here); else the deterministic start vector.  ritz (optional):
 // the Ritz vector of lambda_max per angle on return.
-// From this order on the complex64 phase's products run on the tensor cores.
-static constexpr int kNrTensorMinN = 512;
-
 template <typename T>
 static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int nang,
                             const double* dth, double tol, int mmax, const double2* start,
@@ -1403,28 +1400,6 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
   for (int m = 1; m <= nang; ++m) zwork_bytes = std::max(zwork_bytes, zgemm_work_bytes(n, m, sizeof(T)));
   void* zwork = zwork_bytes ? ws(c, LzNames<T>::Z, zwork_bytes, &rc) : nullptr;
   if (zwork_bytes && !zwork) return rc;
-  // complex64 products on the tensor cores (3xTF32, about FP32 accuracy):
-  // A and A^H packed once, negated (the update forms C - op(A) B with C = 0)
-  void* apk = nullptr;
-  void* ahpk = nullptr;
-  void* bpk = nullptr;
-  int* tst = nullptr;
-  size_t bpk_bytes = 0;
-  if constexpr (sizeof(T) == sizeof(float2)) {
-    if (n >= kNrTensorMinN) {
-      apk = ws(c, "nr_apk", tc_pack_a_bytes(n, n), &rc);
-      ahpk = ws(c, "nr_ahpk", tc_pack_a_bytes(n, n), &rc);
-      bpk_bytes = tc_pack_b_bytes(nang, n);
-      bpk = ws(c, "nr_bpk", bpk_bytes, &rc);
-      tst = static_cast<int*>(ws(c, "nr_tst", 256, &rc));
-      if (!apk || !ahpk || !bpk || !tst) return rc;
-      CUDA_TRY(c, cudaMemsetAsync(tst, 0, sizeof(int), c->stream));
-      if ((rc = tc_pack_a(dA, la, n, n, false, -1.f, apk, c->stream)) ||
-          (rc = tc_pack_a(dA, la, n, n, true, -1.f, ahpk, c->stream)))
-        return fail(c, rc, "operand packing failed");
-      c->launches += 2;
-    }
-  }
   std::vector<double> th_h(nang);
   CUDA_TRY(c, cudaMemcpyAsync(th_h.data(), dth, sizeof(double) * nang, cudaMemcpyDeviceToHost,
                               c->stream));
@@ -1474,17 +1449,6 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
         launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
         launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
       }
-    } else if (apk) {
-      CUDA_TRY(c, cudaMemsetAsync(Y1, 0, sizeof(T) * (size_t)n * na, c->stream));
-      CUDA_TRY(c, cudaMemsetAsync(Y2, 0, sizeof(T) * (size_t)n * na, c->stream));
-      if ((rc = launch_tc_cgemm_packed(reinterpret_cast<float2*>(Y1), n, apk,
-                                       reinterpret_cast<const float2*>(Qj), qs, n, na, n, bpk,
-                                       bpk_bytes, tst, c->stream)) ||
-          (rc = launch_tc_cgemm_packed(reinterpret_cast<float2*>(Y2), n, ahpk,
-                                       reinterpret_cast<const float2*>(Qj), qs, n, na, n, bpk,
-                                       bpk_bytes, tst, c->stream)))
-        return fail(c, rc, "tensor-core product launch failed");
-      c->launches += 4;
     } else {
       launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
       launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
@@ -1608,12 +1572,6 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
     CUDA_TRY(c, cudaMemcpyAsync(sc, inv.data(), sizeof(double) * na, cudaMemcpyHostToDevice, c->stream));
     launch_batched_scale(n, W, n, sc, Q + (size_t)(j + 1) * n, qs, na, c->stream);
     ++c->launches;
-  }
-  if (tst) {
-    int h = 0;
-    CUDA_TRY(c, cudaMemcpyAsync(&h, tst, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-    if (h) return fail(c, BEM2D_ERR_TIMEOUT, "tensor-core product wait timed out");
   }
   // mmax reached: the angles still iterating report their last values
   std::vector<int> rest;
