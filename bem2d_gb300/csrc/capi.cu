@@ -1400,6 +1400,11 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
   for (int m = 1; m <= nang; ++m) zwork_bytes = std::max(zwork_bytes, zgemm_work_bytes(n, m, sizeof(T)));
   void* zwork = zwork_bytes ? ws(c, LzNames<T>::Z, zwork_bytes, &rc) : nullptr;
   if (zwork_bytes && !zwork) return rc;
+  float2* ffb = nullptr;  // B's float-float split for the products
+  if (ffhi) {
+    ffb = static_cast<float2*>(ws(c, "nr_ffb", 2 * sizeof(float2) * (size_t)n * nang, &rc));
+    if (!ffb) return rc;
+  }
   std::vector<double> th_h(nang);
   CUDA_TRY(c, cudaMemcpyAsync(th_h.data(), dth, sizeof(double) * nang, cudaMemcpyDeviceToHost,
                               c->stream));
@@ -1443,8 +1448,10 @@ static int numrange_lanczos(bem2d_ctx* c, int n, const T* dA, long long la, int 
     const T* Qj = Q + (size_t)j * n;
     if constexpr (sizeof(T) == sizeof(double2)) {
       if (ffhi) {  // the products in float-float on the FP32 pipe
-        launch_zgemm_ff(false, ffhi, fflo, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
-        launch_zgemm_ff(true, ffhi, fflo, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);
+        launch_zgemm_ff(false, ffhi, fflo, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, ffb,
+                        c->stream);
+        launch_zgemm_ff(true, ffhi, fflo, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, ffb,
+                        c->stream);
       } else {
         launch_zgemm(false, dA, la, n, Qj, qs, na, Y1, n, zwork, zwork_bytes, c->stream);
         launch_zgemm(true, dA, la, n, Qj, qs, na, Y2, n, zwork, zwork_bytes, c->stream);

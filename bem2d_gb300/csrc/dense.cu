@@ -313,9 +313,11 @@ __device__ __forceinline__ void ffacc_add(FfAcc& a, float p) {
 template <bool HERM, int BN>
 __global__ void __launch_bounds__(256)
 zgemm_ff_kernel(const float2* __restrict__ Ahi, const float2* __restrict__ Alo, long long lda,
-                int n, const double2* __restrict__ B, long long ldb, int m,
-                double2* __restrict__ C, long long ldc, int kchunk, long long cz, int rows) {
+                int n, const float2* __restrict__ Bhi, const float2* __restrict__ Blo, long long ldb,
+                int m, double2* __restrict__ C, long long ldc, int kchunk, long long cz,
+                int rows) {
   constexpr int TY = BN >= 16 ? 16 : BN, TX = 256 / TY, RA = 64 / TX, RB = BN / TY;
+  constexpr int LA = 16 * 64 / 256, LB = (16 * BN + 255) / 256;  // staged entries per thread
   __shared__ float2 Ah[16][64 + 1], Al[16][64 + 1];
   __shared__ float2 Bh[16][BN + 1], Bl[16][BN + 1];
   const int i0 = blockIdx.x * 64, j0 = blockIdx.y * BN;
@@ -327,9 +329,12 @@ zgemm_ff_kernel(const float2* __restrict__ Ahi, const float2* __restrict__ Alo, 
   for (int a = 0; a < RA; ++a)
 #pragma unroll
     for (int b = 0; b < RB; ++b) re[a][b] = im[a][b] = FfAcc{0.f, 0.f, 0.f};
-  for (int k0 = kb; k0 < ke; k0 += 16) {
-    for (int v = threadIdx.x; v < 16 * 64; v += 256) {
-      const int kk = v / 64, ii = v - kk * 64;
+  // the next chunk's entries, loaded while the current chunk is computed
+  float2 nah[LA], nal[LA], nbh[LB], nbl[LB];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int u = 0; u < LA; ++u) {
+      const int v = threadIdx.x + 256 * u, kk = v / 64, ii = v - kk * 64;
       const int i = i0 + ii, k = k0 + kk;
       float2 h = make_float2(0.f, 0.f), l = h;
       if (i < rows && k < ke) {
@@ -341,18 +346,36 @@ zgemm_ff_kernel(const float2* __restrict__ Ahi, const float2* __restrict__ Alo, 
           l.y = -l.y;
         }
       }
-      Ah[kk][ii] = h;
-      Al[kk][ii] = l;
+      nah[u] = h;
+      nal[u] = l;
     }
-    for (int v = threadIdx.x; v < 16 * BN; v += 256) {
-      const int jj = v / 16, kk = v - jj * 16;
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int v = threadIdx.x + 256 * u, jj = v / 16, kk = v - jj * 16;
       const int j = j0 + jj, k = k0 + kk;
-      const double2 d = (j < m && k < ke) ? B[(size_t)j * ldb + k] : make_double2(0.0, 0.0);
-      const float hx = (float)d.x, hy = (float)d.y;
-      Bh[kk][jj] = make_float2(hx, hy);
-      Bl[kk][jj] = make_float2((float)(d.x - (double)hx), (float)(d.y - (double)hy));
+      const bool ok = v < 16 * BN && j < m && k < ke;
+      nbh[u] = ok ? Bhi[(size_t)j * ldb + k] : make_float2(0.f, 0.f);
+      nbl[u] = ok ? Blo[(size_t)j * ldb + k] : make_float2(0.f, 0.f);
+    }
+  };
+  load(kb);
+  for (int k0 = kb; k0 < ke; k0 += 16) {
+#pragma unroll
+    for (int u = 0; u < LA; ++u) {
+      const int v = threadIdx.x + 256 * u, kk = v / 64, ii = v - kk * 64;
+      Ah[kk][ii] = nah[u];
+      Al[kk][ii] = nal[u];
+    }
+#pragma unroll
+    for (int u = 0; u < LB; ++u) {
+      const int v = threadIdx.x + 256 * u, jj = v / 16, kk = v - jj * 16;
+      if (v < 16 * BN) {
+        Bh[kk][jj] = nbh[u];
+        Bl[kk][jj] = nbl[u];
+      }
     }
     __syncthreads();
+    if (k0 + 16 < ke) load(k0 + 16);
 #pragma unroll 2
     for (int kk = 0; kk < 16; ++kk) {
       float2 ah[RA], al[RA], bh[RB], bl[RB];
@@ -410,13 +433,15 @@ zgemm_ff_kernel(const float2* __restrict__ Ahi, const float2* __restrict__ Alo, 
   }
 }
 
-__global__ void split_ff_kernel(const double2* __restrict__ A, long long lda, int n,
+// hi / lo (rows x cols, ld rows) = the float-float split of S (complex128,
+// column-major, ld lds)
+__global__ void split_ff_kernel(const double2* __restrict__ S, long long lds, int rows, int cols,
                                 float2* __restrict__ hi, float2* __restrict__ lo) {
-  const long long tot = (long long)n * n;
+  const long long tot = (long long)rows * cols;
   for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < tot;
        v += (long long)gridDim.x * blockDim.x) {
-    const long long j = v / n, i = v - j * n;
-    const double2 d = A[j * lda + i];
+    const long long j = v / rows, i = v - j * rows;
+    const double2 d = S[j * lds + i];
     const float hx = (float)d.x, hy = (float)d.y;
     hi[v] = make_float2(hx, hy);
     lo[v] = make_float2((float)(d.x - (double)hx), (float)(d.y - (double)hy));
@@ -425,39 +450,46 @@ __global__ void split_ff_kernel(const double2* __restrict__ A, long long lda, in
 
 void launch_split_ff(const double2* A, long long lda, int n, float2* hi, float2* lo,
                      cudaStream_t s) {
-  split_ff_kernel<<<1024, 256, 0, s>>>(A, lda, n, hi, lo);
+  split_ff_kernel<<<1024, 256, 0, s>>>(A, lda, n, n, hi, lo);
 }
 
 template <int BN>
-static void zgemm_ff_bn(bool herm, const float2* Ahi, const float2* Alo, int n, const double2* B,
-                        long long ldb, int m, double2* C, long long ldc, double2* P, int z,
+static void zgemm_ff_bn(bool herm, const float2* Ahi, const float2* Alo, int n, const float2* Bhi,
+                        const float2* Blo, int m, double2* C, long long ldc, double2* P, int z,
                         cudaStream_t s) {
   const int kchunk = ((n + z - 1) / z + 15) / 16 * 16;
   dim3 g((n + 63) / 64, (m + BN - 1) / BN, z);
   double2* out = z > 1 ? P : C;
   const long long lo = z > 1 ? n : ldc, cz = z > 1 ? (long long)n * m : 0;
   if (herm)
-    zgemm_ff_kernel<true, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, B, ldb, m, out, lo, kchunk, cz, n);
+    zgemm_ff_kernel<true, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, Bhi, Blo, n, m, out, lo, kchunk,
+                                                cz, n);
   else
-    zgemm_ff_kernel<false, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, B, ldb, m, out, lo, kchunk, cz, n);
+    zgemm_ff_kernel<false, BN><<<g, 256, 0, s>>>(Ahi, Alo, n, n, Bhi, Blo, n, m, out, lo, kchunk,
+                                                 cz, n);
   if (z > 1)
     zgemm_reduce_kernel<double2><<<dim3((n + 255) / 256, m), 256, 0, s>>>(P, cz, z, n, m, C, ldc);
 }
 
 void launch_zgemm_ff(bool herm, const float2* Ahi, const float2* Alo, int n, const double2* B,
                      long long ldb, int m, double2* C, long long ldc, void* work,
-                     size_t work_bytes, cudaStream_t s) {
+                     size_t work_bytes, float2* bsplit, cudaStream_t s) {
   if (m <= 0 || n <= 0) return;
+  // B split once here, not once per row tile of the product
+  float2* Bhi = bsplit;
+  float2* Blo = bsplit + (size_t)n * m;
+  split_ff_kernel<<<std::min(1024, (int)(((long long)n * m + 255) / 256)), 256, 0, s>>>(
+      B, ldb, n, m, Bhi, Blo);
   const int bn = zgemm_bn(m);
   int z = zgemm_splits(n, m, bn);
   if (z > 1 && work_bytes < sizeof(double2) * (size_t)z * n * m) z = 1;
   double2* P = static_cast<double2*>(work);
   if (bn == 4)
-    zgemm_ff_bn<4>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+    zgemm_ff_bn<4>(herm, Ahi, Alo, n, Bhi, Blo, m, C, ldc, P, z, s);
   else if (bn == 16)
-    zgemm_ff_bn<16>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+    zgemm_ff_bn<16>(herm, Ahi, Alo, n, Bhi, Blo, m, C, ldc, P, z, s);
   else
-    zgemm_ff_bn<64>(herm, Ahi, Alo, n, B, ldb, m, C, ldc, P, z, s);
+    zgemm_ff_bn<64>(herm, Ahi, Alo, n, Bhi, Blo, m, C, ldc, P, z, s);
 }
 
 void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,

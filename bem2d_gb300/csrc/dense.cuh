@@ -27,10 +27,11 @@ void launch_zgemm(bool herm, const float2* A, long long lda, int n, const float2
 size_t zgemm_work_bytes(int n, int m, size_t elem);
 // C (n x m, ldc) = op(A) B in float-float on the FP32 pipe (~1e-13 relative
 // to |A| |B|): A (n x n) given as hi = fl32(A), lo = fl32(A - hi), ld n;
-// B, C complex128.  work: zgemm_work_bytes(n, m, sizeof(double2)).
+// B, C complex128.  work: zgemm_work_bytes(n, m, sizeof(double2));
+// bsplit: 2 n m float2 of scratch for B's split.
 void launch_zgemm_ff(bool herm, const float2* Ahi, const float2* Alo, int n, const double2* B,
                      long long ldb, int m, double2* C, long long ldc, void* work,
-                     size_t work_bytes, cudaStream_t s);
+                     size_t work_bytes, float2* bsplit, cudaStream_t s);
 // hi / lo (n x n, ld n) = the float-float split of A (complex128, ld lda)
 void launch_split_ff(const double2* A, long long lda, int n, float2* hi, float2* lo,
                      cudaStream_t s);
