@@ -1513,8 +1513,10 @@ static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N
                       const LuWork& w, cudaStream_t s, long long* launches) {
   if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
   if constexpr (sizeof(T) == sizeof(float2)) {
-    // tall and narrow updates (the columns inside an outer block) too
-    if ((M >= kTensorMinN && N >= kTensorMinN) || (M >= 4 * kTensorMinN && N >= kNB)) {
+    // tall and narrow updates (the columns inside an outer block), and short
+    // wide ones (the rows of an outer block right of it) too
+    if ((M >= kTensorMinN && N >= kTensorMinN) || (M >= 4 * kTensorMinN && N >= kNB) ||
+        (N >= 4 * kTensorMinN && M >= kNB)) {
       ++*launches;
       if (w.pack && tc_pack_bytes(M, N, K) <= w.pack_bytes) {
         *launches += 2;  // + the two packing kernels
