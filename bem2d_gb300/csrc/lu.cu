@@ -137,7 +137,7 @@ panel_kernel(T* __restrict__ A, long long lda, int n, int k0, int nb, int rpb,
   __shared__ int s_p, s_bw, s_ok;
   __shared__ R s_pv;
 
-  const int nblk = gridDim.x, b = blockIdx.x;
+  const int b = blockIdx.x;
   const int r0 = k0 + b * rpb;
   const int r1 = min(r0 + rpb, n);
   const int nr = max(r1 - r0, 0);
