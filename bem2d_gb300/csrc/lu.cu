@@ -1638,10 +1638,6 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
         if (cmax > 8) cluster16 = false;
       }
     }
-    if (!done && sizeof(T) == sizeof(float2)) {  // taller: tournament pivoting
-      done = tslu_panel(reinterpret_cast<float2*>(A), lda, n, k0, nb, w,
-                        cluster16 ? kMaxClusterPanel : 8, s, launches);
-    }
     if (!done && sizeof(T) == sizeof(float2)) {  // taller: shared-memory rows panel
       for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
         int C = std::max(1, std::min(cmax, (H + kRowsMinRpb - 1) / kRowsMinRpb));
@@ -1659,6 +1655,13 @@ int lu_factor(T* A, long long lda, int n, const LuWork& w, cudaStream_t s,
         cudaGetLastError();
         if (cmax > 8) cluster16 = false;
       }
+    }
+    if (!done && sizeof(T) == sizeof(float2)) {
+      // taller still: tournament pivoting (measured against the shared-memory
+      // rows panel above: ~200 us per 64 columns for it up to 16 x 416 rows,
+      // ~260 us for the tournament there; beyond, the grid panel: ~370 us)
+      done = tslu_panel(reinterpret_cast<float2*>(A), lda, n, k0, nb, w,
+                        cluster16 ? kMaxClusterPanel : 8, s, launches);
     }
     for (int cmax : {cluster16 ? kMaxClusterPanel : 8, 8}) {
       if (done) break;
