@@ -113,10 +113,11 @@ def _device_system(n, seed, row_scale=False):
     return A, A.T.contiguous().T, b
 
 
-@pytest.mark.parametrize("n,row_scale", [(4200, False), (6000, True), (9000, False)])
+@pytest.mark.parametrize("n,row_scale", [(4200, False), (7000, True), (9000, False)])
 def test_tall_panels_tournament_pivoting(ctx, n, row_scale):
     """Orders above 4096 factor their tall complex64 panels (more rows than
-    a 16-CTA cluster holds in registers) with tournament pivoting.  The mixed
+    a 16-CTA cluster holds in registers) with the shared-memory rows panel
+    up to 16 x 416 rows and with tournament pivoting beyond.  The mixed
     solve must still reach FP64 backward error, |b - A x| / (|A|_F |x| +
     |b|) < 1e-14, and agree with the FP64 path (partial pivoting) to the
     conditioning: |x_mixed - x_fp64| / |x_fp64| <= cond_est * 1e-14, with
@@ -140,15 +141,16 @@ def test_tall_panels_tournament_pivoting(ctx, n, row_scale):
 
 
 def test_tall_panel_zero_column_reports_its_pivot(ctx):
-    """A zero column inside a tall panel (n = 5000, column 101 of the panel
-    starting at row 64, 4936 rows): the tournament's candidates are all zero
-    there, and both paths report LAPACK's info = 101 as LapackError."""
+    """A zero column inside a tall panel (n = 8000, column 101 of the panel
+    starting at row 64, 7936 rows: tournament pivoting): the tournament's
+    candidates are all zero there, and both paths report LAPACK's info = 101
+    as LapackError."""
     torch = pytest.importorskip("torch")
     from bem2d_gb300 import capi
-    A, Acm, b = _device_system(5000, 77)
+    A, Acm, b = _device_system(8000, 77)
     Acm[:, 100] = 0
     for prec in ("fp64", "mixed"):
-        x = torch.zeros(5000, dtype=torch.complex128, device="cuda")
+        x = torch.zeros(8000, dtype=torch.complex128, device="cuda")
         with pytest.raises(capi.LapackError) as e:
             ctx.solve(Acm, b, prec, out=x)
         assert e.value.code == 101, prec
