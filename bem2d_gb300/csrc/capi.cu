@@ -1863,6 +1863,7 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
   if (!w.scratch || !aux || !LU) return rc;
   w.dinv = aux;
   w.perm = reinterpret_cast<int*>(aux + (lu_aux_bytes(n, esz) - 256 - sizeof(int) * (size_t)n));
+  const int tl = tic(c, BEM2D_PHASE_LU);
   if (mixed) {
     w.pack_bytes = lu_pack_bytes(n);
     w.pack = ws(c, "lu_pack", w.pack_bytes, &rc);
@@ -1876,6 +1877,7 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
                                   sizeof(double2) * n, n, cudaMemcpyDeviceToDevice, c->stream));
     rc = lu_factor<double2>(static_cast<double2*>(LU), n, n, w, c->stream, &c->launches);
   }
+  toc(c, tl);
   if (rc) return fail(c, rc, "LU launch failed: %s", cudaGetErrorString(cudaGetLastError()));
   int hinfo[2];
   CUDA_TRY(c, cudaMemcpyAsync(hinfo, w.info, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -1902,6 +1904,8 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
     if ((rc = gk_sigma_max(c, n, iop, ioph, tol, "gkb", &inv_smin))) return rc;
     *norm = smax;
     *cond = smax * inv_smin;
+    CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    resolve_timers(c);
     return BEM2D_OK;
   }
   float2* LU32 = static_cast<float2*>(LU);
@@ -1920,12 +1924,20 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
     Winv = static_cast<float2*>(ws(c, "lu_inv32", sizeof(float2) * (size_t)n * n, &rc));
     zw = ws(c, "inv_zw", zw_bytes + 256, &rc);
     if (!Winv || !zw) return rc;
+    const int ti = tic(c, BEM2D_PHASE_LU);
     if ((rc = lu_inverse_c64(LU32, n, n, w, Winv, n, c->stream, &c->launches)))
       return fail(c, rc, "inverse launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    toc(c, ti);
     CHECK_LAUNCH(c);
   }
   // out = op(A)^{-1} (scale x) in complex64 (out: d + n; d, d + 2n: scratch)
   auto inv32 = [&](bool herm, const double2* x, double scale) -> int {
+    const int ts = tic(c, BEM2D_PHASE_SOLVE);
+    struct Toc {
+      bem2d_ctx* c;
+      int t;
+      ~Toc() { toc(c, t); }
+    } toc_on_return{c, ts};
     if (Winv) {
       if (herm) {
         launch_scale_to_c64(n, x, scale, d, c->stream);
@@ -2022,6 +2034,8 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
     return rc;
   *norm = smax;
   *cond = smax * inv_smin;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  resolve_timers(c);
   return BEM2D_OK;
 }
 
