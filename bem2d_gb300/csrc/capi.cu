@@ -1919,7 +1919,7 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
   // hundreds of such products.
   float2* Winv = nullptr;
   void* zw = nullptr;
-  const size_t zw_bytes = zgemm_work_bytes(n, 1, sizeof(float2));
+  const size_t zw_bytes = mv_part_bytes(n);
   if (n >= kInverseMinN) {
     Winv = static_cast<float2*>(ws(c, "lu_inv32", sizeof(float2) * (size_t)n * n, &rc));
     zw = ws(c, "inv_zw", zw_bytes + 256, &rc);
@@ -1941,13 +1941,14 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
     if (Winv) {
       if (herm) {
         launch_scale_to_c64(n, x, scale, d, c->stream);
-        launch_zgemm(true, Winv, n, n, d, n, 1, d + 2 * n, n, zw, zw_bytes, c->stream);
+        launch_mvh(Winv, n, n, d, d + 2 * n, c->stream);
         launch_scatter_c64(n, d + 2 * n, w.perm, d + n, c->stream);
+        c->launches += 3;
       } else {
         launch_gather_to_c64(n, x, w.perm, scale, d, c->stream);
-        launch_zgemm(false, Winv, n, n, d, n, 1, d + n, n, zw, zw_bytes, c->stream);
+        launch_mv(Winv, n, n, d, d + n, static_cast<float2*>(zw), c->stream);
+        c->launches += 3;
       }
-      c->launches += 3;
       return BEM2D_OK;
     }
     launch_scale_to_c64(n, x, scale, d, c->stream);

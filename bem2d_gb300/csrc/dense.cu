@@ -72,29 +72,31 @@ void launch_gather_blocks(int n, const double2* M, long long ldm, const int* bst
 }
 
 // ---- matrix-vector products ---------------------------------------------
-// y = A x (n x n), column chunks of 256 with per-row partial sums, then sum.
+// y = A x (n x n), column chunks of 256 with per-row partial sums, then sum;
+// complex128 or complex64 (the latter summed on the FP32 pipe).
 constexpr int kMvChunk = 256;
-__global__ void mv_partial_kernel(const double2* __restrict__ A, long long lda, int n,
-                                  const double2* __restrict__ x, double2* part) {
-  __shared__ double2 xs[kMvChunk];
+template <typename T>
+__global__ void mv_partial_kernel(const T* __restrict__ A, long long lda, int n,
+                                  const T* __restrict__ x, T* part) {
+  __shared__ T xs[kMvChunk];
   const int c0 = blockIdx.y * kMvChunk;
   const int nc = min(kMvChunk, n - c0);
   for (int v = threadIdx.x; v < nc; v += blockDim.x) xs[v] = x[c0 + v];
   __syncthreads();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  double2 acc = make_double2(0, 0);
-  const double2* col = A + (size_t)c0 * lda + r;
+  T acc = CTraits<T>::make(0, 0);
+  const T* col = A + (size_t)c0 * lda + r;
 #pragma unroll 4
   for (int c = 0; c < nc; ++c) acc = cfma(col[(size_t)c * lda], xs[c], acc);
   part[(size_t)blockIdx.y * n + r] = acc;
 }
 
-__global__ void mv_final_kernel(int n, int nchunk, const double2* __restrict__ part,
-                                double2* __restrict__ y) {
+template <typename T>
+__global__ void mv_final_kernel(int n, int nchunk, const T* __restrict__ part, T* __restrict__ y) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double2 acc = make_double2(0, 0);
+  T acc = CTraits<T>::make(0, 0);
   for (int c = 0; c < nchunk; ++c) {
     acc.x += part[(size_t)c * n + i].x;
     acc.y += part[(size_t)c * n + i].y;
@@ -103,15 +105,16 @@ __global__ void mv_final_kernel(int n, int nchunk, const double2* __restrict__ p
 }
 
 // y = A^H x: one warp per column, lanes over rows (coalesced), shuffle sum.
-__global__ void mvh_kernel(const double2* __restrict__ A, long long lda, int n,
-                           const double2* __restrict__ x, double2* __restrict__ y) {
+template <typename T>
+__global__ void mvh_kernel(const T* __restrict__ A, long long lda, int n, const T* __restrict__ x,
+                           T* __restrict__ y) {
   const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= n) return;
-  const double2* col = A + (size_t)j * lda;
-  double sr = 0, si = 0;
+  const T* col = A + (size_t)j * lda;
+  typename CTraits<T>::R sr = 0, si = 0;
   for (int r = lane; r < n; r += 32) {
-    const double2 a = col[r], b = x[r];
+    const T a = col[r], b = x[r];
     sr += a.x * b.x + a.y * b.y;  // conj(a) b
     si += a.x * b.y - a.y * b.x;
   }
@@ -120,23 +123,36 @@ __global__ void mvh_kernel(const double2* __restrict__ A, long long lda, int n,
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
     si += __shfl_xor_sync(0xffffffffu, si, o);
   }
-  if (lane == 0) y[j] = make_double2(sr, si);
+  if (lane == 0) y[j] = CTraits<T>::make(sr, si);
 }
 
 size_t mv_part_bytes(int n) {
   return sizeof(double2) * (size_t)n * ((n + kMvChunk - 1) / kMvChunk);
 }
 
+template <typename T>
+static void mv_t(const T* A, long long lda, int n, const T* x, T* y, T* part, cudaStream_t s) {
+  const int nchunk = (n + kMvChunk - 1) / kMvChunk;
+  mv_partial_kernel<T><<<dim3((n + 127) / 128, nchunk), 128, 0, s>>>(A, lda, n, x, part);
+  mv_final_kernel<T><<<(n + 255) / 256, 256, 0, s>>>(n, nchunk, part, y);
+}
+
 void launch_mv(const double2* A, long long lda, int n, const double2* x, double2* y,
                double2* part, cudaStream_t s) {
-  const int nchunk = (n + kMvChunk - 1) / kMvChunk;
-  mv_partial_kernel<<<dim3((n + 127) / 128, nchunk), 128, 0, s>>>(A, lda, n, x, part);
-  mv_final_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, nchunk, part, y);
+  mv_t(A, lda, n, x, y, part, s);
+}
+void launch_mv(const float2* A, long long lda, int n, const float2* x, float2* y, float2* part,
+               cudaStream_t s) {
+  mv_t(A, lda, n, x, y, part, s);
 }
 
 void launch_mvh(const double2* A, long long lda, int n, const double2* x, double2* y,
                 cudaStream_t s) {
-  mvh_kernel<<<(n + 7) / 8, 256, 0, s>>>(A, lda, n, x, y);
+  mvh_kernel<double2><<<(n + 7) / 8, 256, 0, s>>>(A, lda, n, x, y);
+}
+void launch_mvh(const float2* A, long long lda, int n, const float2* x, float2* y,
+                cudaStream_t s) {
+  mvh_kernel<float2><<<(n + 7) / 8, 256, 0, s>>>(A, lda, n, x, y);
 }
 
 // ---- matrix-matrix products: C (n x m) = op(A) (n x n) B (n x m) -------------

@@ -16,6 +16,11 @@ void launch_mv(const double2* A, long long lda, int n, const double2* x, double2
                double2* part, cudaStream_t s);
 void launch_mvh(const double2* A, long long lda, int n, const double2* x, double2* y,
                 cudaStream_t s);
+// complex64 versions (part: mv_part_bytes(n) bytes suffice)
+void launch_mv(const float2* A, long long lda, int n, const float2* x, float2* y, float2* part,
+               cudaStream_t s);
+void launch_mvh(const float2* A, long long lda, int n, const float2* x, float2* y,
+                cudaStream_t s);
 // C (n x m, ldc) = op(A) B, op = A or A^H (herm).  work: room for the K-split
 // partial products (zgemm_work_bytes); with less, one pass over K.
 void launch_zgemm(bool herm, const double2* A, long long lda, int n, const double2* B,
