@@ -2328,12 +2328,15 @@ __global__ void axpy_c64_kernel(int n, double scale, const float2* __restrict__ 
 // ---- explicit inverse of a complex64 factor ---------------------------------
 // W = U^{-1} L^{-1} from the factor P A = L U of lu_factor<float2>, so that
 // A^{-1} x = W (P x) and A^{-H} x = P^T (W^H x).  Blocked substitution on
-// the identity, 64 rows at a time:
-//   forward  Y_k = L_kk^{-1} Y_k, then Y_below -= L_below,k Y_k (Y stays lower
-//            triangular: only columns 0 .. k64 + 63 are touched);
-//   backward W_k = U_kk^{-1} W_k, then W_above -= U_above,k W_k.
-// The diagonal-block inverses are lu_factor's (w.dinv); the rank-64 updates
-// run on the tensor cores (the trailing-update kernel).  About 2.7 N^3
+// the identity, 64 rows at a time inside outer blocks of 256 rows (64 when
+// the packing buffer only holds rank-64 operands):
+//   forward  Y_k = L_kk^{-1} Y_k, then the outer block's rows below k, and
+//            after the outer block the rows below it (Y stays lower
+//            triangular: only the columns left of the block are touched);
+//   backward W_k = U_kk^{-1} W_k, then the outer block's rows above k, and
+//            after the outer block the rows above it.
+// The diagonal-block inverses are lu_factor's (w.dinv); the updates run on
+// the tensor cores (the trailing-update kernel).  About 2.7 N^3
 // complex flops; an inverse pays for itself once an iteration needs more
 // than a few dozen solves with the factor (a product with W streams N^2
 // entries; the substitution is a chain of 2 N / 64 dependent steps).
@@ -2379,37 +2382,47 @@ int lu_inverse_c64(const float2* LU, long long lda, int n, const LuWork& w, floa
                    long long ldw, cudaStream_t s, long long* launches) {
   if (n <= 0) return BEM2D_OK;
   if (!w.pack || !w.dinv) return BEM2D_ERR_ARG;
-  const int nk = (n + kNB - 1) / kNB;
   if (tc_pack_bytes(n, n, kNB) > w.pack_bytes) return BEM2D_ERR_ARG;
+  // outer blocks of kOuterNB rows where the packing buffer holds rank-256
+  // operands (one pass over the rest of W per outer block, not per 64 rows)
+  const int ob = tc_pack_bytes(n, n, kOuterNB) <= w.pack_bytes ? kOuterNB : kNB;
+  auto upd = [&](float2* C, const float2* Am, const float2* Bm, int M, int N, int K) -> int {
+    if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
+    if (launch_tc_cgemm_sub(C, ldw, Am, lda, Bm, ldw, M, N, K, w.pack, w.pack_bytes, w.status, s))
+      return BEM2D_ERR_CUDA;
+    *launches += 3;
+    return BEM2D_OK;
+  };
   if (cudaMemset2DAsync(W, sizeof(float2) * ldw, 0, sizeof(float2) * n, n, s) != cudaSuccess)
     return BEM2D_ERR_CUDA;
   identity_c64_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, W, ldw);
   ++*launches;
   const float2* dinv = static_cast<const float2*>(w.dinv);
-  for (int k = 0; k < nk; ++k) {  // forward: Y = L^{-1}
-    const int r0 = k * kNB, bs = std::min(kNB, n - r0), nc = r0 + bs;
-    block_apply_kernel<<<(nc + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * k) * kNB * kNB,
-                                                      W + r0, ldw, bs, nc);
-    ++*launches;
-    const int M = n - nc;
-    if (M > 0) {
-      if (launch_tc_cgemm_sub(W + nc, ldw, LU + (size_t)r0 * lda + nc, lda, W + r0, ldw, M, nc,
-                              bs, w.pack, w.pack_bytes, w.status, s))
-        return BEM2D_ERR_CUDA;
-      *launches += 3;
+  int rc = 0;
+  for (int R0 = 0; R0 < n; R0 += ob) {  // forward: Y = L^{-1} (lower triangular)
+    const int R1 = std::min(n, R0 + ob);
+    for (int k0 = R0; k0 < R1; k0 += kNB) {
+      const int kb = k0 / kNB, bs = std::min(kNB, n - k0), nc = k0 + bs;
+      block_apply_kernel<<<(nc + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * kb) * kNB * kNB,
+                                                        W + k0, ldw, bs, nc);
+      ++*launches;
+      // the rest of this outer block's rows
+      if ((rc = upd(W + nc, LU + (size_t)k0 * lda + nc, W + k0, R1 - nc, nc, bs))) return rc;
     }
+    // the rows below the outer block, columns 0 .. R1 - 1 (Y is zero beyond)
+    if ((rc = upd(W + R1, LU + (size_t)R0 * lda + R1, W + R0, n - R1, R1, R1 - R0))) return rc;
   }
-  for (int k = nk - 1; k >= 0; --k) {  // backward: W = U^{-1} Y
-    const int r0 = k * kNB, bs = std::min(kNB, n - r0);
-    block_apply_kernel<<<(n + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * k + 1) * kNB * kNB,
-                                                     W + r0, ldw, bs, n);
-    ++*launches;
-    if (r0 > 0) {
-      if (launch_tc_cgemm_sub(W, ldw, LU + (size_t)r0 * lda, lda, W + r0, ldw, r0, n, bs, w.pack,
-                              w.pack_bytes, w.status, s))
-        return BEM2D_ERR_CUDA;
-      *launches += 3;
+  const int nob = (n + ob - 1) / ob;
+  for (int q = nob - 1; q >= 0; --q) {  // backward: W = U^{-1} Y
+    const int R0 = q * ob, R1 = std::min(n, R0 + ob);
+    for (int k0 = ((R1 - 1) / kNB) * kNB; k0 >= R0; k0 -= kNB) {
+      const int kb = k0 / kNB, bs = std::min(kNB, n - k0);
+      block_apply_kernel<<<(n + 15) / 16, 256, 0, s>>>(dinv + (size_t)(2 * kb + 1) * kNB * kNB,
+                                                       W + k0, ldw, bs, n);
+      ++*launches;
+      if ((rc = upd(W + R0, LU + (size_t)k0 * lda + R0, W + k0, k0 - R0, n, bs))) return rc;
     }
+    if ((rc = upd(W, LU + (size_t)R0 * lda, W + R0, R0, n, R1 - R0))) return rc;
   }
   return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
 }
