@@ -229,8 +229,9 @@ int bem2d_change_basis(bem2d_ctx* ctx, int n, const void* K, int64_t ldk, const 
 /* norm = sigma_max(A), cond = sigma_max / sigma_min: replaces L2NormCond
  * (lib/bem2d_mathroutines.cpp:208-266, zgesvd).  Golub-Kahan-Lanczos
  * bidiagonalisation with full reorthogonalisation, on A for sigma_max and on
- * A^{-1} (complex128 LU, solves with A and A^H) for sigma_min, until the
- * estimates change by less than tol (tol <= 0 selects 1e-13). */
+ * A^{-1} (complex128 LU, solves with A and A^H) for sigma_min, each until
+ * the Ritz residual bound min(r, r^2 / gap) of the largest Ritz value bounds
+ * its relative error by tol (tol <= 0 selects 1e-13; at most 300 steps). */
 int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
                        double* norm, double* cond);
 
@@ -238,12 +239,14 @@ int bem2d_l2_norm_cond(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double
  * routine of the reference, lib/bem2d_mathroutines.cpp:208-266):
  * BEM2D_PREC_FP64: as bem2d_l2_norm_cond (complex128 LU);
  * BEM2D_PREC_MIXED: complex64 LU (tensor-core trailing updates); the Lanczos
- *   iteration on A^{-1} first runs with unrefined complex64 solves until its
- *   estimate settles, then again from that Ritz vector with every product
- *   with A^{-1} or A^{-H} refined with FP64 residuals of A until its backward
- *   error reaches FP64 roundoff or stops halving, so the final iteration sees
- *   the operator to FP64 accuracy.  The Lanczos arithmetic is FP64 in both
- *   modes. */
+ *   iteration on A^{-1} first runs with unrefined complex64 solves (to
+ *   1e-10), then again from that Ritz vector with every product with A^{-1}
+ *   or A^{-H} refined with FP64 residuals of A until its backward error
+ *   reaches FP64 roundoff or stops halving, so the final iteration sees the
+ *   operator to FP64 accuracy.  From n = 1024 on the complex64 solves are
+ *   products with the explicit inverse U^{-1} L^{-1} (formed once from the
+ *   factor, n^2 complex64 of device memory more).  The Lanczos arithmetic
+ *   is FP64 in both modes. */
 int bem2d_l2_norm_cond_prec(bem2d_ctx* ctx, int n, const void* A, int64_t lda, double tol,
                             int precision, double* norm, double* cond);
 
