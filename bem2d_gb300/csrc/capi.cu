@@ -1834,21 +1834,48 @@ int bem2d_l2_norm_cond_prec(bem2d_ctx* c, int n, const void* A, int64_t lda, dou
   if (!dA) return rc;
   double2* part = static_cast<double2*>(ws(c, "mv_part", mv_part_bytes(n), &rc));
   if (!part) return rc;
+  const bool mixed = precision == BEM2D_PREC_MIXED;
+  // sigma_max: products with A in FP64 (the FP64 pipe), or, in mixed
+  // precision, in float-float on the FP32 pipe (~1e-13 relative to |A| |x|:
+  // A split once, 16 n^2 bytes)
+  float2* Ahi = nullptr;
+  float2* Alo = nullptr;
+  float2* ffb = nullptr;
+  void* ffw = nullptr;
+  const size_t ffw_bytes = zgemm_work_bytes(n, 1, sizeof(double2));
+  if (mixed) {
+    Ahi = static_cast<float2*>(ws(c, "nc_Ahi", sizeof(float2) * (size_t)n * n, &rc));
+    Alo = static_cast<float2*>(ws(c, "nc_Alo", sizeof(float2) * (size_t)n * n, &rc));
+    ffb = static_cast<float2*>(ws(c, "nc_ffb", 2 * sizeof(float2) * (size_t)n, &rc));
+    ffw = ws(c, "nc_ffw", ffw_bytes + 256, &rc);
+    if (!Ahi || !Alo || !ffb || !ffw) return rc;
+    launch_split_ff(dA, la, n, Ahi, Alo, c->stream);
+    ++c->launches;
+  }
   auto op = [&](const double2* x, double2* y) -> int {
-    launch_mv(dA, la, n, x, y, part, c->stream);
-    c->launches += 2;
+    if (mixed) {
+      launch_zgemm_ff(false, Ahi, Alo, n, x, n, 1, y, n, ffw, ffw_bytes, ffb, c->stream);
+      c->launches += 3;
+    } else {
+      launch_mv(dA, la, n, x, y, part, c->stream);
+      c->launches += 2;
+    }
     return BEM2D_OK;
   };
   auto oph = [&](const double2* x, double2* y) -> int {
-    launch_mvh(dA, la, n, x, y, c->stream);
-    c->launches += 1;
+    if (mixed) {
+      launch_zgemm_ff(true, Ahi, Alo, n, x, n, 1, y, n, ffw, ffw_bytes, ffb, c->stream);
+      c->launches += 3;
+    } else {
+      launch_mvh(dA, la, n, x, y, c->stream);
+      c->launches += 1;
+    }
     return BEM2D_OK;
   };
   double smax = 0, inv_smin = 0;
   if ((rc = gk_sigma_max(c, n, op, oph, tol, "gka", &smax))) return rc;
   // sigma_min = 1 / sigma_max(A^{-1}): complex128 LU, or complex64 LU with
   // FP64 refinement of every product with A^{-1} / A^{-H}
-  const bool mixed = precision == BEM2D_PREC_MIXED;
   const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
   LuWork w;
   int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));

@@ -113,10 +113,11 @@ __global__ void mvh_kernel(const T* __restrict__ A, long long lda, int n, const 
   if (j >= n) return;
   const T* col = A + (size_t)j * lda;
   typename CTraits<T>::R sr = 0, si = 0;
+#pragma unroll 4
   for (int r = lane; r < n; r += 32) {
     const T a = col[r], b = x[r];
-    sr += a.x * b.x + a.y * b.y;  // conj(a) b
-    si += a.x * b.y - a.y * b.x;
+    sr = fma(a.x, b.x, fma(a.y, b.y, sr));  // conj(a) b
+    si = fma(a.x, b.y, fma(-a.y, b.x, si));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
