@@ -164,6 +164,32 @@ def test_oracle_at_kite_config_size(ctx):
     assert rel(b, O.rhs(g, 100.0, d, 100.0)) < TOL_MAT
 
 
+@pytest.mark.parametrize("n", [400, 1500])
+def test_fine_ellipse_arc_matches_oracle(ctx, n):
+    """Elliptic-arc elements narrower than 0.05 rad (the sweep's meshes): the
+    self pairs' trial points come from the addition theorem and short Taylor
+    series instead of a sincos per point.  FP64 and mixed assembly of the
+    ellipse (2, 1), k = 40, against the CPU oracle on 48 full rows, to
+    1e-12 relative (or 3x the rounding floor of the FP64 formulation, as
+    in test_oracle_at_kite_config_size)."""
+    from bem2d_gb300 import geometry as G
+    from oracle import oracle as O
+    g = G.ellipse_arc_closed(n).add_poly_basis(0)
+    k = 40.0
+    rows = np.random.default_rng(n).choice(n, 48, replace=False)
+    R = O.discrete_kernel_rows(g, rows, "combined", k, k, QUAD, alpha=2.0, beta=1.0)
+    g2 = G.ellipse_arc_closed(n).add_poly_basis(0)
+    rng = np.random.default_rng(2)
+    for p in g2.param:
+        p[0] = float(np.nextafter(p[0], 10.0 if rng.random() < 0.5 else -10.0))
+    floor = rel(O.discrete_kernel_rows(g2, rows[:12], "combined", k, k, QUAD, alpha=2.0,
+                                       beta=1.0), R[:12])
+    A = ctx.discrete_kernel(g, "combined", k, k, QUAD, alpha=2.0, beta=1.0)
+    assert rel(A[rows, :], R) < max(TOL_MAT, 3 * floor), floor
+    Am, _ = ctx.discrete_kernel_mixed(g, "combined", k, k, QUAD, alpha=2.0, beta=1.0)
+    assert rel(Am[rows, :], R) < max(TOL_MAT, 3 * floor), floor
+
+
 MIXED_CASES = ["disk160", "kite128", "ellipsearc100", "trefoil48", "invellipse48",
                "square_graded", "lshape_graded", "square_poly2", "triangle_lin", "two_squares"]
 
