@@ -247,9 +247,10 @@ struct GeoTab {
 __device__ __forceinline__ void geo_fill(const DevGeom& g, int e, int u, const double* vals, int n,
                                          bool mirror, const GeoTab& tb, int off, int lane) {
   const double* prm = g.param + 8 * (size_t)e;
+  const ArcBase arc = arc_base(g.kind[e], prm);
   for (int v = lane; v < n; v += 32) {
     const double s = mirror ? 1 - vals[v] : vals[v];
-    const ElemPt p = elem_eval(g.kind[e], prm, s);
+    const ElemPt p = arc.ok ? arc_eval(arc, s) : elem_eval(g.kind[e], prm, s);
     double nx, ny;
     elem_normal(p, &nx, &ny);
     tb.x[off + v] = p.mx;
