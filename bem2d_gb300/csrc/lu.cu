@@ -869,7 +869,6 @@ panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, i
   __shared__ unsigned ckv[2], ckl[2];
   __shared__ unsigned skv[kMaxClusterPanel], skl[kMaxClusterPanel];
   __shared__ unsigned wkv[kWinMaxThreads / 32], wkl[kWinMaxThreads / 32];
-  __shared__ unsigned s_cl;
   __shared__ int s_ipiv[kNB];
   __shared__ int s_info;
   const int lw = threadIdx.x >> 5, ln = threadIdx.x & 31;
@@ -911,19 +910,22 @@ panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, i
           wkl[lw] = lab;
         }
         __syncthreads();
-        if (lw == 0) {
+        // every warp forms the CTA candidate from the warp maxima (no second
+        // barrier: the next column rewrites them only after the cluster
+        // barrier below, which every thread reaches after reading them)
+        unsigned cand;
+        {
           const unsigned wv = ln < nw ? wkv[ln] : 0u;
           const unsigned wl = ln < nw ? wkl[ln] : 0xffffffffu;
           m = __reduce_max_sync(0xffffffffu, wv);
           lab = __reduce_min_sync(0xffffffffu, (wv == m && m) ? wl : 0xffffffffu);
-          if (ln == 0) {
-            s_cl = m ? lab : 0xfffffffeu;
+          cand = m ? lab : 0xfffffffeu;
+          if (lw == 0 && ln == 0) {
             ckv[par] = m;
             ckl[par] = lab;
           }
         }
-        __syncthreads();
-        if (label == s_cl) {  // this row is the CTA candidate: stage pairs >= c/2
+        if (label == cand) {  // this row is the CTA candidate: stage pairs >= c/2
           float4* dst = cand4 + par * (kNB / 2) + 2 * b + h;
 #pragma unroll
           for (int i = 0; i < kW; ++i)
