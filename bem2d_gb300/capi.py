@@ -21,7 +21,7 @@ ERR = {-1: "ARG", -2: "CUDA", -3: "NOMEM", -4: "NONFINITE", -5: "NOCONV",
        -6: "TIMEOUT", -7: "UNSUPPORTED"}
 KERNEL = {"single": 0, "double": 1, "conjdouble": 2, "combined": 3}
 FUN = {"planewave": 0, "normalplanewave": 1, "combinedplanewave": 2}
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "mixed_tf32": 2}
 
 # symbols declared in include/bem2d_gpu.h
 EXPORTS = ["bem2d_ctx_create", "bem2d_ctx_destroy", "bem2d_ctx_last_error",

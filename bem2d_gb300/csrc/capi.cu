@@ -994,6 +994,10 @@ static int solve_dev(bem2d_ctx* c, int n, const double2* A, long long lda, const
   LuWork w;
   w.min_rows = c->panel_min_rows;
   w.tc_ctas = c->tc_ctas;
+  if (precision == BEM2D_PREC_MIXED_TF32) {
+    w.tc_passes = 1;
+    precision = BEM2D_PREC_MIXED;
+  }
   // ints: [0] info [1] status [8, 8+n) ipiv
   int* ints = static_cast<int*>(ws(c, "lu_ints", sizeof(int) * (n + 8), &rc));
   if (!ints) return rc;
@@ -1228,13 +1232,13 @@ int bem2d_scattering_solve(bem2d_ctx* c, const bem2d_geometry* geom, const bem2d
   if (rc) return rc;
   cudaSetDevice(c->device);
   Staged st;
-  if ((rc = stage(c, geom, quad, true, true, &st, precision == BEM2D_PREC_MIXED))) return rc;
+  const bool mixed = precision == BEM2D_PREC_MIXED || precision == BEM2D_PREC_MIXED_TF32;
+  if ((rc = stage(c, geom, quad, true, true, &st, mixed))) return rc;
   const int n = geom->n_unk;
   double2* A = static_cast<double2*>(ws(c, "sys_A", sizeof(double2) * (size_t)n * n, &rc));
   if (!A) return rc;
   double2* b = static_cast<double2*>(ws(c, "sys_b", sizeof(double2) * n, &rc));
   if (!b) return rc;
-  const bool mixed = precision == BEM2D_PREC_MIXED;
   // complex wavenumbers: FP64 assembly; the mixed solver converts A itself
   const bool mixed_asm = mixed && k_im == 0.0;
   if ((rc = nf_clear(c))) return rc;

@@ -475,6 +475,8 @@ struct LuWork {
   // persistent CTAs of the tensor-core update (0: one per SM); fewer leave
   // SMs to concurrent factorisations
   int tc_ctas = 0;
+  // products per term of the tensor-core update: 3 (3xTF32) or 1 (1xTF32)
+  int tc_passes = 3;
   // look-ahead of the blocked complex64 factorisation (all set, or none):
   // the trailing update of the columns beyond the next block runs on `aux`
   // (packing buffer pack2, aux_ctas persistent CTAs) while the next block's
@@ -533,13 +535,16 @@ void launch_gather_to_c64(int n, const double2* src, const int* perm, double sca
 void launch_scatter_c64(int n, const float2* src, const int* perm, float2* dst, cudaStream_t s);
 
 // C -= A B for complex64 column-major operands on the tensor cores
-// (tcgen05 kind::tf32, 3xTF32 split; lu_tc.cu).  C is M x N, A M x K, B K x N.
+// (tcgen05 kind::tf32; lu_tc.cu).  C is M x N, A M x K, B K x N.
+// passes = 3: 3xTF32 split (FP32-accurate products); 1: 1xTF32 (operands
+// rounded to TF32, a third of the tensor work).
 // Sets *status on a device-side wait timeout.
 // `pack` (tc_pack_bytes(M, N, K) bytes) holds the split, re-laid-out operands.
 size_t tc_pack_bytes(int M, int N, int K);
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
                         const float2* B, long long ldb, int M, int N, int K, void* pack,
-                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas = 0);
+                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas = 0,
+                        int passes = 3);
 
 void launch_residual(const double2* A, long long lda, int n, const double2* x,
                      const double2* b, double2* r, double2* part, cudaStream_t s);

@@ -1525,7 +1525,7 @@ static int update_sub(T* C, const T* Am, const T* Bm, long long ld, int M, int N
         return launch_tc_cgemm_sub(reinterpret_cast<float2*>(C), ld,
                                    reinterpret_cast<const float2*>(Am), ld,
                                    reinterpret_cast<const float2*>(Bm), ld, M, N, K, w.pack,
-                                   w.pack_bytes, w.status, s, w.tc_ctas)
+                                   w.pack_bytes, w.status, s, w.tc_ctas, w.tc_passes)
                    ? BEM2D_ERR_CUDA
                    : BEM2D_OK;
       }

@@ -13,11 +13,14 @@
 // A tile is 64 complex rows (128 real rows = the MMA's M) by 128 complex
 // columns: 256 tensor-memory columns per accumulator.
 //
-// Accuracy (3xTF32): every FP32 operand x is split into hi = x with its low
-// 13 mantissa bits cleared (exactly a TF32 value) and lo = x - hi; each
+// Accuracy (3xTF32): every FP32 operand x is split into hi = x rounded to
+// the nearest TF32 value (10 mantissa bits) and lo = x - hi (exact); each
 // product is accumulated as hi*hi + hi*lo + lo*hi, which keeps about 21 bits
 // per product - the accuracy of the FP32 update it replaces, so the LU keeps
-// the quality the FP64 refinement expects.
+// the quality the FP64 refinement expects.  With passes = 1 (1xTF32) only
+// hi*hi is issued: a third of the tensor work, products to about 2^-11
+// relative, for systems whose condition number the refinement tolerates at
+// that precision.
 //
 // Operands are packed once per update (pack_a_kernel, pack_b_kernel): split
 // into hi/lo and laid out, per tile and per chunk of 16 along K, exactly as
@@ -85,8 +88,9 @@ __device__ __forceinline__ unsigned long long smem_desc(unsigned addr) {
 __host__ __device__ __forceinline__ int kmajor_off(int r, int k) {
   return (r >> 3) * kTcSBO + (k >> 2) * kCoreBytes + (r & 7) * 16 + (k & 3) * 4;
 }
+// hi = x rounded to 10 mantissa bits (ties away from zero), lo = x - hi
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
-  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+  hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
   lo = x - hi;
 }
 
@@ -165,7 +169,7 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned b
 // A (M x K complex) -> Apk[mt][kc] = {hi, lo} chunks of kTcApart bytes each.
 // grid: (ceil(M / 64) * 64 / 128 x nkc * 16), 128 threads
 __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M, int K, int nkc,
-                              unsigned char* __restrict__ Apk) {
+                              int passes, unsigned char* __restrict__ Apk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;  // complex row
   const int k = blockIdx.y;                             // 0 .. nkc * 16 - 1
   const int mt = i / kTcBM, il = i - mt * kTcBM;
@@ -174,19 +178,22 @@ __global__ void pack_a_kernel(const float2* __restrict__ A, long long lda, int M
   const float2 v = (i < M && k < K) ? A[(size_t)k * lda + i] : make_float2(0.f, 0.f);
   unsigned char* chunk = Apk + ((size_t)mt * nkc + kc) * kTcChunkA;
   float h, l;
+  float h2, l2;
   tf32_split(v.x, h, l);
+  tf32_split(v.y, h2, l2);
   *reinterpret_cast<float*>(chunk + kmajor_off(2 * il, kl)) = h;
-  *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il, kl)) = l;
-  tf32_split(v.y, h, l);
-  *reinterpret_cast<float*>(chunk + kmajor_off(2 * il + 1, kl)) = h;
-  *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il + 1, kl)) = l;
+  *reinterpret_cast<float*>(chunk + kmajor_off(2 * il + 1, kl)) = h2;
+  if (passes > 1) {
+    *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il, kl)) = l;
+    *reinterpret_cast<float*>(chunk + kTcApart + kmajor_off(2 * il + 1, kl)) = l2;
+  }
 }
 
 // B (K x N complex) -> Bpk[nt][kc] = {hi, lo} chunks of kTcBpart bytes, each
 // with rows 0..127 = re and rows 128..255 = im of the tile's 128 columns.
 // grid: (ceil(N / 128) * 128 x ceil(nkc * 16 / 64)), 64 threads
 __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K, int N, int nkc,
-                              unsigned char* __restrict__ Bpk) {
+                              int passes, unsigned char* __restrict__ Bpk) {
   const int n = blockIdx.x;                             // complex column
   const int k = blockIdx.y * blockDim.x + threadIdx.x;  // 0 .. nkc * 16 - 1
   if (k >= nkc * kTcBK) return;
@@ -196,12 +203,15 @@ __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K
   unsigned char* chunk = Bpk + ((size_t)nt * nkc + kc) * kTcChunkB;
   const int ore = kmajor_off(nl, kl), oim = kmajor_off(kTcBN + nl, kl);
   float h, l;
+  float h2, l2;
   tf32_split(v.x, h, l);
+  tf32_split(v.y, h2, l2);
   *reinterpret_cast<float*>(chunk + ore) = h;
-  *reinterpret_cast<float*>(chunk + kTcBpart + ore) = l;
-  tf32_split(v.y, h, l);
-  *reinterpret_cast<float*>(chunk + oim) = h;
-  *reinterpret_cast<float*>(chunk + kTcBpart + oim) = l;
+  *reinterpret_cast<float*>(chunk + oim) = h2;
+  if (passes > 1) {
+    *reinterpret_cast<float*>(chunk + kTcBpart + ore) = l;
+    *reinterpret_cast<float*>(chunk + kTcBpart + oim) = l2;
+  }
 }
 
 // ---- the update --------------------------------------------------------------
@@ -210,7 +220,7 @@ __global__ void pack_b_kernel(const float2* __restrict__ B, long long ldb, int K
 __global__ void __launch_bounds__(kTcThreads, 1)
 tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* __restrict__ Apk,
                     const unsigned char* __restrict__ Bpk, int M, int N, int nkc, int mtiles,
-                    int ntiles, int* status) {
+                    int ntiles, int passes, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
   unsigned long long* full = reinterpret_cast<unsigned long long*>(sm + kTcBarOff);
   unsigned long long* empty = full + kTcStages;
@@ -263,9 +273,12 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* 
             break;
           }
           unsigned char* st = sm + s * kTcStage;
-          mbar_expect_tx(&full[s], kTcStage);
-          bulk_copy(st, asrc + (size_t)c * kTcChunkA, kTcChunkA, &full[s]);
-          bulk_copy(st + kTcChunkA, bsrc + (size_t)c * kTcChunkB, kTcChunkB, &full[s]);
+          // 1xTF32: the hi halves only (the first half of each packed chunk)
+          const unsigned abytes = passes > 1 ? kTcChunkA : kTcApart;
+          const unsigned bbytes = passes > 1 ? kTcChunkB : kTcBpart;
+          mbar_expect_tx(&full[s], abytes + bbytes);
+          bulk_copy(st, asrc + (size_t)c * kTcChunkA, abytes, &full[s]);
+          bulk_copy(st + kTcChunkA, bsrc + (size_t)c * kTcChunkB, bbytes, &full[s]);
         }
       }
       if (!ok) {
@@ -302,8 +315,10 @@ tc_cgemm_sub_kernel(float2* __restrict__ C, long long ldc, const unsigned char* 
           for (int ks = 0; ks < kTcBK / 8; ++ks) {
             const unsigned o = 256u * ks;  // K = 8 tf32 = two core matrices
             mma_tf32(d, ah + o, bh + o, idesc, (c == 0 && ks == 0) ? 0u : 1u);
-            mma_tf32(d, ah + o, bl + o, idesc, 1u);
-            mma_tf32(d, al + o, bh + o, idesc, 1u);
+            if (passes > 1) {
+              mma_tf32(d, ah + o, bl + o, idesc, 1u);
+              mma_tf32(d, al + o, bh + o, idesc, 1u);
+            }
           }
           mma_commit(&empty[s]);  // the stage may be refilled once these MMAs read it
         }
@@ -421,22 +436,25 @@ size_t tc_pack_bytes(int M, int N, int K) {
 
 int launch_tc_cgemm_sub(float2* C, long long ldc, const float2* A, long long lda,
                         const float2* B, long long ldb, int M, int N, int K, void* pack,
-                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas) {
+                        size_t pack_bytes, int* status, cudaStream_t s, int max_ctas,
+                        int passes) {
   static const cudaError_t attr = cudaFuncSetAttribute(
       tc_cgemm_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (attr != cudaSuccess) return BEM2D_ERR_CUDA;
   if (M <= 0 || N <= 0 || K <= 0) return BEM2D_OK;
   if (!pack || tc_pack_bytes(M, N, K) > pack_bytes) return BEM2D_ERR_ARG;
+  if (passes != 1 && passes != 3) return BEM2D_ERR_ARG;
   const int nkc = (K + kTcBK - 1) / kTcBK;
   const int mt = (M + kTcBM - 1) / kTcBM, nt = (N + kTcBN - 1) / kTcBN;
   unsigned char* Apk = static_cast<unsigned char*>(pack);
   unsigned char* Bpk = Apk + align256((size_t)mt * nkc * kTcChunkA);
   pack_a_kernel<<<dim3((mt * kTcBM + 127) / 128, nkc * kTcBK), 128, 0, s>>>(A, lda, M, K, nkc,
-                                                                            Apk);
-  pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc, Bpk);
+                                                                            passes, Apk);
+  pack_b_kernel<<<dim3(nt * kTcBN, (nkc * kTcBK + 63) / 64), 64, 0, s>>>(B, ldb, K, N, nkc,
+                                                                        passes, Bpk);
   const int grid = std::min(mt * nt, max_ctas > 0 ? max_ctas : num_sms());
   tc_cgemm_sub_kernel<<<grid, kTcThreads, kTcSmem, s>>>(C, ldc, Apk, Bpk, M, N, nkc, mt, nt,
-                                                        status);
+                                                        passes, status);
   return cudaPeekAtLastError() == cudaSuccess ? BEM2D_OK : BEM2D_ERR_CUDA;
 }
 

@@ -44,7 +44,8 @@ extern "C" int bem2d_sweep_solve(bem2d_ctx* c, int nk, const bem2d_geometry* geo
   if (nk < 0 || (nk > 0 && (!geoms || !quad || !k || !x)))
     return ctx_fail(c, BEM2D_ERR_ARG, "bad arguments");
   if (nk == 0) return BEM2D_OK;
-  if (precision != BEM2D_PREC_FP64 && precision != BEM2D_PREC_MIXED)
+  if (precision != BEM2D_PREC_FP64 && precision != BEM2D_PREC_MIXED &&
+      precision != BEM2D_PREC_MIXED_TF32)
     return ctx_fail(c, BEM2D_ERR_ARG, "unknown precision");
   for (int i = 0; i < nk; ++i)
     if (!x[i]) return ctx_fail(c, BEM2D_ERR_ARG, "an output pointer is NULL");

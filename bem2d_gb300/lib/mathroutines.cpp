@@ -104,7 +104,9 @@ void SetSolverPrecision(int p) { g_precision = p; }
 int GetSolverPrecision() {
   if (g_precision < 0) {
     const char* e = std::getenv("BEM2D_PRECISION");
-    g_precision = (e && std::strcmp(e, "mixed") == 0) ? BEM2D_PREC_MIXED : BEM2D_PREC_FP64;
+    g_precision = (e && std::strcmp(e, "mixed") == 0)        ? BEM2D_PREC_MIXED
+                  : (e && std::strcmp(e, "mixed_tf32") == 0) ? BEM2D_PREC_MIXED_TF32
+                                                             : BEM2D_PREC_FP64;
   }
   return g_precision;
 }
@@ -190,7 +192,9 @@ void NumRange(const Matrix& m, int n, std::string filename) {
     th[n + i] = i * step + PI;
   }
   detail::check(bem2d_num_range(detail::ctx(), N, &(*m.data)[0], N, 2 * n, th.data(), 0.0,
-                                GetSolverPrecision(), lmax.data()),
+                                GetSolverPrecision() == BEM2D_PREC_FP64 ? BEM2D_PREC_FP64
+                                                                        : BEM2D_PREC_MIXED,
+                                lmax.data()),
                 "NumRange");
   dvector eigs(2 * n), steps(2 * n);
   for (int i = 0; i < n; ++i) {

@@ -598,7 +598,8 @@ def solve_record(ctx, args, wname, steps, warmup, ws=1, rank=0, sub=False):
         "data": "synthetic",
         "config": {"workload": w["desc"], "problems_per_step": P,
                    "n_unknowns": ns[0] if P == 1 else [min(ns), max(ns)],
-                   "precision": "mixed", "sweep_workers": args.workers if P > 1 else None,
+                   "precision": "mixed", "lu_update": "3xTF32 (tcgen05 kind::tf32)",
+                   "sweep_workers": args.workers if P > 1 else None,
                    "l2": "256 MB write between timed steps, outside the step events",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": ws * P * 1e3 / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": h2d,
@@ -638,6 +639,27 @@ def solve_record(ctx, args, wname, steps, warmup, ws=1, rank=0, sub=False):
 
         res["backward_error"] = {"mixed": berr(x_dev[0]), "fp64": berr(x_fp64[0]),
                                  "measure": "|b - A x| / (|A|_F |x| + |b|), FP64 A"}
+        # the LU's trailing-update precision options on the same system: the
+        # value above runs 3xTF32; 1xTF32 issues a third of the tensor work
+        # and leaves more to the refinement
+        x_t = torch.zeros(nb, dtype=torch.complex128, device="cuda")
+        ms_t = st.run(lambda: ctx.scattering_solve(holds[0].arrays, k, w["d"], eta, QUAD,
+                                                   precision="mixed_tf32", out=x_t),
+                      steps, warmup)
+        info_t = ctx.last_info
+        ph_t = phases("mixed_tf32")
+        t_t = max_over_ranks([sum(ms_t) / len(ms_t)], ws, "cuda")[0]
+        res["update_options"] = {
+            "ran": "3xTF32 (value, e2e)",
+            "3xTF32": {"ms_per_step": t_mixed, "lu_ms": ph_mixed["lu"],
+                       "solve_ms": ph_mixed["solve"], "iterations": infos[0][1],
+                       "backward_error": res["backward_error"]["mixed"],
+                       "rel_err_vs_fp64": errs[0]},
+            "1xTF32": {"ms_per_step": t_t, "lu_ms": ph_t["lu"], "solve_ms": ph_t["solve"],
+                       "iterations": info_t[1], "backward_error": berr(x_t),
+                       "rel_err_vs_fp64": float(torch.linalg.vector_norm(x_t - x_fp64[0]) /
+                                                torch.linalg.vector_norm(x_fp64[0]))}}
+        del x_t
         if not args.no_cpu and rank == 0:
             threads = os.cpu_count() or 1
             res["cpu_baseline"], res["rows_rel_err_vs_oracle"] = lshape_cpu_leg(

@@ -78,6 +78,14 @@ extern "C" {
 /* ---- solver precision -------------------------------------------------- */
 #define BEM2D_PREC_FP64 0  /* complex128 LU, FP64 throughout                 */
 #define BEM2D_PREC_MIXED 1 /* complex64 LU + FP64 iterative refinement      */
+/* As BEM2D_PREC_MIXED, with the LU's tensor-core trailing updates as one
+ * TF32 product per term (1xTF32: operands rounded to 10 mantissa bits, a
+ * third of the 3xTF32 tensor work).  The factor is then accurate to about
+ * 1e-3 relative instead of 1e-6, so refinement contracts the error by about
+ * cond(A) 1e-3 per step: for systems with cond(A) up to ~100; beyond that
+ * GMRES-IR takes over (see bem2d_solve_system).  Accepted by
+ * bem2d_solve_system, bem2d_scattering_solve and bem2d_sweep_solve. */
+#define BEM2D_PREC_MIXED_TF32 2
 
 /* QuadOption (lib/bem2d_quadrature.h:26-30). */
 typedef struct {

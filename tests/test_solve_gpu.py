@@ -191,3 +191,55 @@ def test_mixed_gmres_ir_fallback_on_ill_conditioned(ctx, n, cond):
     err = float(torch.linalg.vector_norm(xs["mixed"] - xs["fp64"]) /
                 torch.linalg.vector_norm(xs["fp64"]))
     assert err <= cond * 1e-14, err
+
+
+def _berr(A, x, b):
+    torch = pytest.importorskip("torch")
+    r = torch.linalg.vector_norm(b - A @ x)
+    return float(r / (torch.linalg.matrix_norm(A) * torch.linalg.vector_norm(x) +
+                      torch.linalg.vector_norm(b)))
+
+
+@pytest.mark.parametrize("n", [3000, 9000])
+def test_update_precision_options(ctx, n):
+    """The LU's tensor-core trailing update with 3xTF32 ("mixed") and 1xTF32
+    ("mixed_tf32") products on a well-conditioned system (complex Gaussian
+    plus 2 sqrt(n) I, cond(A) ~ 3): both reach the FP64 backward error
+    |b - A x| / (|A|_F |x| + |b|) <= 1e-14 and agree with the FP64 path to
+    cond_est * 1e-14 (cond_est = 10 |A|_F |x| / |b|, as above).  The 1xTF32
+    factor is accurate to ~1e-3 instead of ~1e-6, so its refinement takes
+    more steps; the line printed gives steps and errors per option."""
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda").manual_seed(n + 1)
+    A = torch.randn((n, n), dtype=torch.complex128, device="cuda", generator=g)
+    A += 2.0 * np.sqrt(n) * torch.eye(n, dtype=torch.complex128, device="cuda")
+    b = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+    Acm = A.T.contiguous().T
+    xs, its = {}, {}
+    for prec in ("fp64", "mixed", "mixed_tf32"):
+        x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+        ctx.solve(Acm, b, prec, out=x)
+        assert _berr(A, x, b) <= 1e-14, (prec, ctx.last_info)
+        xs[prec], its[prec] = x, ctx.last_info[1]
+    cond_est = 10.0 * float(torch.linalg.matrix_norm(A) * torch.linalg.vector_norm(xs["fp64"]) /
+                            torch.linalg.vector_norm(b))
+    errs = {p: float(torch.linalg.vector_norm(xs[p] - xs["fp64"]) /
+                     torch.linalg.vector_norm(xs["fp64"])) for p in ("mixed", "mixed_tf32")}
+    print("n=%d cond_est=%.1f iterations %s rel_err_vs_fp64 %s" % (n, cond_est, its, errs))
+    for p, e in errs.items():
+        assert e <= cond_est * 1e-14, (p, e)
+    assert its["mixed_tf32"] >= its["mixed"]
+
+
+def test_update_1xtf32_falls_back_to_gmres_ir(ctx):
+    """1xTF32 factor on a complex Gaussian matrix without a diagonal shift
+    (n = 4200, cond(A) ~ 1e4): cond(A) times the factor's ~1e-3 error is
+    above one, so plain refinement stalls; GMRES-IR with that factor must
+    still reach |b - A x| / (|A|_F |x| + |b|) <= 1e-14."""
+    torch = pytest.importorskip("torch")
+    A, Acm, b = _device_system(4200, 4201)
+    x = torch.zeros(4200, dtype=torch.complex128, device="cuda")
+    ctx.solve(Acm, b, "mixed_tf32", out=x)
+    assert _berr(A, x, b) <= 1e-14, ctx.last_info
+    print("n=4200 mixed_tf32 steps (refinement + GMRES-IR factor applications):",
+          ctx.last_info[1])
