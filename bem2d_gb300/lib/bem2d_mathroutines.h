@@ -48,7 +48,7 @@ void L2NormCond(const Matrix& stiff, double& norm, double& cond);
 // All singular values, descending (GPU Householder tridiagonalisation of
 // [0 A; A^H 0] and bisection).
 void SingularValues(const Matrix& stiff, pdvector& singvals);
-// x = m^{-1} rhs (GPU LU; precision from BEM2D_PRECISION=fp64|mixed).
+// x = m^{-1} rhs (GPU LU; precision from BEM2D_PRECISION=fp64|mixed|mixed_tf32).
 pMatrix SolveSystem(Matrix& m, Matrix& rhs);
 // All eigenvalues of the Hermitian matrix the upper triangle of k defines,
 // ascending (GPU Householder tridiagonalisation and bisection).
