@@ -74,7 +74,8 @@ void InPolygon(const pGeometry polygon, const std::vector<Point>& testpoints,
                std::vector<int>& inpoly);
 
 // Solver precision of SolveSystem / SoundSoftScattering::Solve:
-// 0 = complex128 LU (default), 1 = complex64 LU + FP64 refinement.
+// 0 = complex128 LU (default), 1 = complex64 LU + FP64 refinement,
+// 2 = as 1 with 1xTF32 tensor-core updates in the LU.
 void SetSolverPrecision(int precision);
 int GetSolverPrecision();
 
