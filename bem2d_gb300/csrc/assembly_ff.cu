@@ -38,7 +38,7 @@ __device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KCo
   const ff x = ff_mul(d, kc.k);
   const ff ix = ff_mul(h.y, kc.invk);
   pq_ff(x.hi, ix, &h.p0, &h.q0, &h.p1, &h.q1);
-  h.amp = ff_mul(kc.amp0, ff_sqrt(ix));
+  h.amp = ff_mul(kc.amp0, ff_rsqrt(x));  // amp0 / sqrt(x)
   h.e = expi_ff(x, tab);
   return h;
 }
@@ -50,6 +50,16 @@ __device__ __forceinline__ ffc ffc_mul_pq(const ffc& e, ff p, ff q) {
   r.im = ff_add_fast(ff_mul(e.re, q), ff_mul(e.im, p));
   return r;
 }
+
+// acc += v without renormalising acc: acc.lo gathers the hi sums' rounding
+// errors and the lo parts (ff_acc_norm restores |lo| <= ulp(hi)/2 after a
+// few steps, so that the FP32 sum in lo stays ~2^-48 |acc| accurate)
+__device__ __forceinline__ void ff_acc(ff& acc, ff v) {
+  const ff s = two_sum(acc.hi, v.hi);
+  acc.hi = s.hi;
+  acc.lo += s.lo + v.lo;
+}
+__device__ __forceinline__ void ff_acc_norm(ff& acc) { acc = fast_two_sum(acc.hi, acc.lo); }
 
 __device__ __forceinline__ ffc ffc_scale(const ffc& z, ff a) {
   ffc r;
@@ -201,8 +211,10 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
       continue;
     }
     const ff Dx = ff_from_double(dxc), Dy = ff_from_double(dyc);
-    ffc arc, acr;
-    arc.re = arc.im = acr.re = acr.im = ff_make(0.0f, 0.0f);
+    // s0: the terms both orientations share (the single-layer part), t_rc /
+    // t_cr: the normal-factor terms of entry (row, col) / (col, row)
+    ffc s0, trc, tcr;
+    s0.re = s0.im = trc.re = trc.im = tcr.re = tcr.im = ff_make(0.0f, 0.0f);
 #pragma unroll 1
     for (int q1 = 0; q1 < ng; ++q1) {
       const int o1 = q1 * kTileF + lane;
@@ -226,24 +238,19 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
         if (KERNEL == BEM2D_KERNEL_SINGLE) {
           // K w_x w_y = (i/4) aw E (P0 + i Q0), the same in both orientations
           const ffc Z = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_scale2(aw, 0.25f));
-          if (rc) {
-            arc.re = ff_add_fast(arc.re, ff_neg(Z.im));
-            arc.im = ff_add_fast(arc.im, Z.re);
-          }
-          if (cr) {
-            acr.re = ff_add_fast(acr.re, ff_neg(Z.im));
-            acr.im = ff_add_fast(acr.im, Z.re);
-          }
+          ff_acc(s0.re, ff_neg(Z.im));
+          ff_acc(s0.im, Z.re);
         } else {
           // K w_x w_y = Z0 - dot Z1 with Z1 = aw (k/4)/d E (P1 + i Q1) and, for
           // the combined operator, Z0 = aw (eta/4) E (P0 + i Q0); dot is the
           // orientation's normal factor (n_y . (y - x) for the double layer
           // at (x, y), n_x . (x - y) otherwise)
           const ffc Z1 = ffc_scale(ffc_mul_pq(h.e, h.p1, h.q1), ff_mul(aw, ff_mul(kc.kq, h.y)));
-          ffc Z0;
-          Z0.re = Z0.im = ff_make(0.0f, 0.0f);
-          if (KERNEL == BEM2D_KERNEL_COMBINED)
-            Z0 = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(aw, kc.eq));
+          if (KERNEL == BEM2D_KERNEL_COMBINED) {
+            const ffc Z0 = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(aw, kc.eq));
+            ff_acc(s0.re, Z0.re);
+            ff_acc(s0.im, Z0.im);
+          }
           const ff n1w = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));  // n_x . (x - y)
           const ff n2w = ff_add_fast(ff_mul(ff_make(b2.x, b2.y), dx),
                                      ff_mul(ff_make(b3.x, b3.y), dy));  // n_y . (x - y)
@@ -251,16 +258,27 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
           const ff m_rc = KERNEL == BEM2D_KERNEL_DOUBLE ? n2w : ff_neg(n1w);
           const ff m_cr = KERNEL == BEM2D_KERNEL_DOUBLE ? ff_neg(n1w) : n2w;
           if (rc) {
-            arc.re = ff_add_fast(arc.re, ff_add_fast(Z0.re, ff_mul(m_rc, Z1.re)));
-            arc.im = ff_add_fast(arc.im, ff_add_fast(Z0.im, ff_mul(m_rc, Z1.im)));
+            ff_acc(trc.re, ff_mul(m_rc, Z1.re));
+            ff_acc(trc.im, ff_mul(m_rc, Z1.im));
           }
           if (cr) {
-            acr.re = ff_add_fast(acr.re, ff_add_fast(Z0.re, ff_mul(m_cr, Z1.re)));
-            acr.im = ff_add_fast(acr.im, ff_add_fast(Z0.im, ff_mul(m_cr, Z1.im)));
+            ff_acc(tcr.re, ff_mul(m_cr, Z1.re));
+            ff_acc(tcr.im, ff_mul(m_cr, Z1.im));
           }
         }
       }
+      ff_acc_norm(s0.re);
+      ff_acc_norm(s0.im);
+      ff_acc_norm(trc.re);
+      ff_acc_norm(trc.im);
+      ff_acc_norm(tcr.re);
+      ff_acc_norm(tcr.im);
     }
+    ffc arc, acr;
+    arc.re = ff_add(s0.re, trc.re);
+    arc.im = ff_add(s0.im, trc.im);
+    acr.re = ff_add(s0.re, tcr.re);
+    acr.im = ff_add(s0.im, tcr.im);
     if (rc) {
       const double re = alpha * ff_to_double(arc.re), im = alpha * ff_to_double(arc.im);
       out[(size_t)col * ld + row] = make_double2(re, im);

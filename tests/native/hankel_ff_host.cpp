@@ -23,7 +23,7 @@ extern "C" void hankel01_ff_host(int n, const double* x, double* out) {
     const ff ix = ff_rcp(xf);
     ff p0, q0, p1, q1;
     pq_ff(xf.hi, ix, &p0, &q0, &p1, &q1);
-    const ff amp = ff_mul(ff_make(0.7978845834732056f, -2.2670340271702116e-08f), ff_sqrt(ix));
+    const ff amp = ff_mul(ff_make(0.7978845834732056f, -2.2670340271702116e-08f), ff_rsqrt(xf));
     const ffc e = expi_ff(xf, tab);
     ffc h0 = cmul_ff(ffc{p0, q0}, e);
     ffc h1 = cmul_ff(ffc{p1, q1}, e);  // times -i below
