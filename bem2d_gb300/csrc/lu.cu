@@ -934,7 +934,25 @@ panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, i
         // 2. every CTA's candidate visible
         cl.sync();
         // 3. pull all keys and staged rows: loads first, then stores, so
-        //    that a thread's DSMEM loads (up to four ranks) are in flight at once
+        //    that a thread's DSMEM loads (up to four ranks) are in flight at
+        //    once; with no more ranks than warps, warp q pulls rank q
+        if (C <= nw) {
+          if (lw < C) {
+            const int j = ln;
+            float4 t4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            unsigned tv = 0u, tl = 0u;
+            if (j >= (c >> 1)) t4 = cl.map_shared_rank(cand4, lw)[par * (kNB / 2) + j];
+            if (j == 0) {
+              tv = *cl.map_shared_rank(&ckv[par], lw);
+              tl = *cl.map_shared_rank(&ckl[par], lw);
+            }
+            if (j >= (c >> 1)) stage4[lw * (kNB / 2) + j] = t4;
+            if (j == 0) {
+              skv[lw] = tv;
+              skl[lw] = tl;
+            }
+          }
+        } else {
         for (int q0 = 0; q0 < C; q0 += 4 * nw) {
           constexpr int kPer = 4;
           const int j = ln;  // absolute pair index
@@ -963,6 +981,7 @@ panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, i
             }
           }
         }
+        }
         __syncthreads();
         // 4. the pivot, from the local keys (every warp)
         const unsigned kv = ln < C ? skv[ln] : 0u;
@@ -988,17 +1007,18 @@ panel_win_kernel(float2* __restrict__ A, long long lda, int n, int k0, int nb, i
             const float4 pc = stage4[q * (kNB / 2) + (c >> 1)];
             const float2 piv = hi ? make_float2(pc.z, pc.w) : make_float2(pc.x, pc.y);
             const float2 l = cmul(v, crcp_fast(piv));
-            if (h == hc) {  // the pair holding column c
-              if (hi) {
-                r[0].z = l.x;
-                r[0].w = l.y;
-              } else {
-                const float2 u = cfms(make_float2(r[0].z, r[0].w), l, make_float2(pc.z, pc.w));
-                r[0] = make_float4(l.x, l.y, u.x, u.y);
-              }
-            } else if (h > hc) {  // pair 2b + 1, right of column c
-              r[0] = cfms2(r[0], l, pr[0]);
-            }
+            // window position 0 without divergence between the two threads
+            // of a row: the update of the whole pair (pr[0] is the pivot
+            // row's pair of this thread; for h == hc it is pc, for h < hc a
+            // stale slot whose result is discarded), then a select: the
+            // pair holding column c keeps its finished column c - 1 (hi) and
+            // takes the multiplier l at column c; pair 2b + 1 right of column
+            // c takes the update; a finished pair left of c stays
+            const float4 x = cfms2(r[0], l, pr[0]);
+            if (h == hc)
+              r[0] = hi ? make_float4(r[0].x, r[0].y, l.x, l.y) : make_float4(l.x, l.y, x.z, x.w);
+            else if (h > hc)
+              r[0] = x;
 #pragma unroll
             for (int i = 1; i < kW; ++i)
               if (i < kW - b) r[i] = cfms2(r[i], l, pr[2 * i]);
