@@ -22,10 +22,11 @@
 namespace bem2d_gpu {
 
 // The distance-dependent part of the kernel at one node pair: 1/d, the
-// asymptotic P/Q factors of H0 and H1, the amplitude sqrt(2/(pi x)) and
-// e^{i(x - pi/4)}.  Shared by entry (i, j) and entry (j, i).
+// asymptotic P/Q factors of H0 and H1, 1/sqrt(x) (the amplitude
+// sqrt(2/(pi x)) without its constant) and e^{i(x - pi/4)}.  Shared by entry
+// (i, j) and entry (j, i).
 struct HankelTermsFF {
-  ff y, p0, q0, p1, q1, amp;
+  ff y, p0, q0, p1, q1, rx;
   ffc e;
 };
 
@@ -38,7 +39,7 @@ __device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KCo
   const ff x = ff_mul(d, kc.k);
   const ff ix = ff_mul(h.y, kc.invk);
   pq_ff(x.hi, ix, &h.p0, &h.q0, &h.p1, &h.q1);
-  h.amp = ff_mul(kc.amp0, ff_rsqrt(x));  // amp0 / sqrt(x)
+  h.rx = ff_rsqrt(x);
   h.e = expi_ff(x, tab);
   return h;
 }
@@ -46,8 +47,8 @@ __device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KCo
 // E (P + i Q) and a complex value times a real one (ff).
 __device__ __forceinline__ ffc ffc_mul_pq(const ffc& e, ff p, ff q) {
   ffc r;
-  r.re = ff_add_fast(ff_mul(e.re, p), ff_neg(ff_mul(e.im, q)));
-  r.im = ff_add_fast(ff_mul(e.re, q), ff_mul(e.im, p));
+  r.re = ff_dot2(e.re, p, ff_neg(e.im), q);
+  r.im = ff_dot2(e.re, q, e.im, p);
   return r;
 }
 
@@ -224,7 +225,12 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
       // once per row node: (c_row - c_col) + o_row
       const ff Px = ff_add_fast(Dx, ff_make(a0.x, a0.y));
       const ff Py = ff_add_fast(Dy, ff_make(a1.x, a1.y));
-      const ff n1x = ff_make(a2.x, a2.y), n1y = ff_make(a3.x, a3.y), w1 = ff_make(a4.x, a4.y);
+      const ff n1x = ff_make(a2.x, a2.y), n1y = ff_make(a3.x, a3.y);
+      // the row node's constant factors: amp0 w_x with k/4 (double-layer
+      // part) and eta/4 or 1/4 (single-layer part)
+      const ff aw1 = ff_mul(kc.amp0, ff_make(a4.x, a4.y));
+      const ff c1 = ff_mul(aw1, kc.kq);
+      const ff c0 = KERNEL == BEM2D_KERNEL_SINGLE ? ff_scale2(aw1, 0.25f) : ff_mul(aw1, kc.eq);
 #pragma unroll 1
       for (int q2 = 0; q2 < ng; ++q2) {
         const int o2 = q2 * kTileF + cc;
@@ -234,26 +240,26 @@ far_ff_kernel(DevGeom g, NodeTable t, NodeTableFF tf, int ng_rt, KConstFF kc, do
         const ff dx = ff_add_fast(Px, ff_make(-b0.x, -b0.y));
         const ff dy = ff_add_fast(Py, ff_make(-b1.x, -b1.y));
         const HankelTermsFF h = hankel_terms_ff(dx, dy, kc, tab);
-        const ff aw = ff_mul(h.amp, ff_mul(w1, ff_make(b4.x, b4.y)));  // amp w_x w_y
+        const ff g = ff_mul(h.rx, ff_make(b4.x, b4.y));  // w_y / sqrt(x)
         if (KERNEL == BEM2D_KERNEL_SINGLE) {
-          // K w_x w_y = (i/4) aw E (P0 + i Q0), the same in both orientations
-          const ffc Z = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_scale2(aw, 0.25f));
+          // K w_x w_y = (i/4) amp w_x w_y E (P0 + i Q0), the same in both
+          // orientations
+          const ffc Z = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(g, c0));
           ff_acc(s0.re, ff_neg(Z.im));
           ff_acc(s0.im, Z.re);
         } else {
-          // K w_x w_y = Z0 - dot Z1 with Z1 = aw (k/4)/d E (P1 + i Q1) and, for
-          // the combined operator, Z0 = aw (eta/4) E (P0 + i Q0); dot is the
-          // orientation's normal factor (n_y . (y - x) for the double layer
-          // at (x, y), n_x . (x - y) otherwise)
-          const ffc Z1 = ffc_scale(ffc_mul_pq(h.e, h.p1, h.q1), ff_mul(aw, ff_mul(kc.kq, h.y)));
+          // K w_x w_y = Z0 - dot Z1 with Z1 = amp w_x w_y (k/4)/d E (P1 + i Q1)
+          // and, for the combined operator, Z0 = amp w_x w_y (eta/4) E (P0 +
+          // i Q0); dot is the orientation's normal factor (n_y . (y - x) for
+          // the double layer at (x, y), n_x . (x - y) otherwise)
+          const ffc Z1 = ffc_scale(ffc_mul_pq(h.e, h.p1, h.q1), ff_mul(ff_mul(g, h.y), c1));
           if (KERNEL == BEM2D_KERNEL_COMBINED) {
-            const ffc Z0 = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(aw, kc.eq));
+            const ffc Z0 = ffc_scale(ffc_mul_pq(h.e, h.p0, h.q0), ff_mul(g, c0));
             ff_acc(s0.re, Z0.re);
             ff_acc(s0.im, Z0.im);
           }
-          const ff n1w = ff_add_fast(ff_mul(n1x, dx), ff_mul(n1y, dy));  // n_x . (x - y)
-          const ff n2w = ff_add_fast(ff_mul(ff_make(b2.x, b2.y), dx),
-                                     ff_mul(ff_make(b3.x, b3.y), dy));  // n_y . (x - y)
+          const ff n1w = ff_dot2(n1x, dx, n1y, dy);                                // n_x . (x - y)
+          const ff n2w = ff_dot2(ff_make(b2.x, b2.y), dx, ff_make(b3.x, b3.y), dy);  // n_y . (x - y)
           // (row, col): -dot = n2w (double layer) or -n1w; (col, row): the reverse
           const ff m_rc = KERNEL == BEM2D_KERNEL_DOUBLE ? n2w : ff_neg(n1w);
           const ff m_cr = KERNEL == BEM2D_KERNEL_DOUBLE ? ff_neg(n1w) : n2w;

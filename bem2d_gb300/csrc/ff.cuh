@@ -107,6 +107,23 @@ __host__ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   return fast_two_sum(p, e);
 }
 
+// a b + c d: both hi products exact (FMA residuals), their sum by a two-sum,
+// the residuals and cross terms into the low part, one normalisation.  The
+// error is ~2^-47 max(|a b|, |c d|), as ff_add_fast(ff_mul(a, b), ff_mul(c,
+// d)), in fewer operations.
+__host__ __device__ __forceinline__ ff ff_dot2(ff a, ff b, ff c, ff d) {
+  const float p = f_mul_rn(a.hi, b.hi);
+  const float q = f_mul_rn(c.hi, d.hi);
+  float e1 = fmaf(a.hi, b.hi, -p);
+  e1 = fmaf(a.hi, b.lo, e1);
+  e1 = fmaf(a.lo, b.hi, e1);
+  float e2 = fmaf(c.hi, d.hi, -q);
+  e2 = fmaf(c.hi, d.lo, e2);
+  e2 = fmaf(c.lo, d.hi, e2);
+  const ff s = two_sum(p, q);
+  return fast_two_sum(s.hi, s.lo + (e1 + e2));
+}
+
 __host__ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
   const float p = f_mul_rn(a.hi, b);
   float e = fmaf(a.hi, b, -p);

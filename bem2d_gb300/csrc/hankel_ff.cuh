@@ -23,34 +23,46 @@ constexpr float kRedC2 = -2.7319617679211206e-09f;
 constexpr float kRedC3 = -1.0719528187536762e-16f;
 constexpr float kRedInv = 10.18591594696045f;  // 64 / (2 pi)
 
+// 1 - a and 1/2 - a for |a| <= 1/4: the head by a fast two-sum (exact), the
+// low part left unnormalised (|lo| stays a few ulps of hi, which the ff
+// products that consume these values accept)
+__host__ __device__ __forceinline__ ff ff_one_minus(ff a) {
+  const ff s = fast_two_sum(1.0f, -a.hi);
+  return ff_make(s.hi, s.lo - a.lo);
+}
+__host__ __device__ __forceinline__ ff ff_half_minus(ff a) {
+  const ff s = fast_two_sum(0.5f, -a.hi);
+  return ff_make(s.hi, s.lo - a.lo);
+}
+
 // e^{i(x - pi/4)} for x > 0 (ff), table tab[j] = (cos, sin)(2 pi j/64 - pi/4)
 // as ff pairs: tab[4 j] = cos.hi, tab[4 j + 1] = cos.lo, [+2], [+3] = sin.
+// Only the absolute error matters (|E| = 1): ~1e-16 plus x 2^-48 from x
+// itself.
 __host__ __device__ __forceinline__ ffc expi_ff(ff x, const float* tab) {
   const float j = rintf(x.hi * kRedInv);
   const float r1 = fmaf(-j, kRedC1, x.hi);  // exact
-  ff r = two_sum(r1, x.lo);
-  // r - j C2: only the absolute error matters here (|E| = 1), and the fast
-  // addition's is ~2^-48 |r| even where the two nearly cancel
-  r = ff_add_fast(r, ff_neg(two_prod(j, kRedC2)));
-  r = ff_add_f(r, -j * kRedC3);
+  // r = r1 + x.lo - j C2 - j C3: the two larger small terms by two-sums,
+  // the rounding errors, j C2's low part and j C3 into the low part
+  const ff p = two_prod(j, kRedC2);
+  const ff s1 = two_sum(r1, x.lo);
+  const ff s2 = two_sum(s1.hi, -p.hi);
+  const ff r = fast_two_sum(s2.hi, fmaf(-j, kRedC3, (s1.lo + s2.lo) - p.lo));
   const int idx = ((int)j) & 63;
-  const ff r2 = ff_sqr(r);
-  // sin r = r - r^3 (1/6 - r^2/120 + r^4/5040)
+  const ff r2 = ff_sqr(r);  // |r| <= pi/64, r^2 <= 2.5e-3
+  // sin r = r (1 - r^2 S), S = 1/6 - r^2/120 + r^4/5040
   const float st = r2.hi * fmaf(r2.hi, 1.0f / 5040.0f, -1.0f / 120.0f);
   const ff S = ff_add_f(ff_make(0.1666666716337204f, -4.967053879312289e-09f), st);
-  const ff sinr = ff_add_fast(r, ff_neg(ff_mul(ff_mul(r, r2), S)));
-  // cos r = 1 - r^2 (1/2 - r^2/24 + r^4/720 - r^6/40320)
-  const float ct = r2.hi * r2.hi * fmaf(r2.hi, -1.0f / 40320.0f, 1.0f / 720.0f);
-  const ff C = ff_add_f(ff_add_fast(ff_make(0.5f, 0.0f),
-                                    ff_neg(ff_mul(r2, ff_make(0.0416666679084301f,
-                                                              -1.2417634698280722e-09f)))),
-                        ct);
-  const ff cosr = ff_add_fast(ff_make(1.0f, 0.0f), ff_neg(ff_mul(r2, C)));
+  const ff sinr = ff_mul(r, ff_one_minus(ff_mul(r2, S)));
+  // cos r = 1 - r^2 C, C = 1/2 - r^2 D, D = 1/24 - r^2/720 + r^4/40320
+  const float dt = r2.hi * fmaf(r2.hi, 1.0f / 40320.0f, -1.0f / 720.0f);
+  const ff D = ff_add_f(ff_make(0.0416666679084301f, -1.2417634698280722e-09f), dt);
+  const ff cosr = ff_one_minus(ff_mul(r2, ff_half_minus(ff_mul(r2, D))));
   const ff ca = ff_make(tab[4 * idx], tab[4 * idx + 1]);
   const ff sa = ff_make(tab[4 * idx + 2], tab[4 * idx + 3]);
   ffc e;
-  e.re = ff_add_fast(ff_mul(ca, cosr), ff_neg(ff_mul(sa, sinr)));
-  e.im = ff_add_fast(ff_mul(sa, cosr), ff_mul(ca, sinr));
+  e.re = ff_dot2(ca, cosr, ff_neg(sa), sinr);
+  e.im = ff_dot2(sa, cosr, ca, sinr);
   return e;
 }
 
