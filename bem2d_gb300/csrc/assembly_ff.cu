@@ -33,7 +33,7 @@ struct HankelTermsFF {
 __device__ __forceinline__ HankelTermsFF hankel_terms_ff(ff dx, ff dy, const KConstFF& kc,
                                                         const float* tab) {
   HankelTermsFF h;
-  const ff d2 = ff_add_fast(ff_sqr(dx), ff_sqr(dy));
+  const ff d2 = ff_dot2(dx, dx, dy, dy);
   h.y = ff_rsqrt(d2);  // 1/d
   const ff d = ff_mul(d2, h.y);
   const ff x = ff_mul(d, kc.k);
