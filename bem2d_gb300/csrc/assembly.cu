@@ -247,10 +247,9 @@ struct GeoTab {
 __device__ __forceinline__ void geo_fill(const DevGeom& g, int e, int u, const double* vals, int n,
                                          bool mirror, const GeoTab& tb, int off, int lane) {
   const double* prm = g.param + 8 * (size_t)e;
-  const ArcBase arc = arc_base(g.kind[e], prm);
   for (int v = lane; v < n; v += 32) {
     const double s = mirror ? 1 - vals[v] : vals[v];
-    const ElemPt p = arc.ok ? arc_eval(arc, s) : elem_eval(g.kind[e], prm, s);
+    const ElemPt p = elem_eval(g.kind[e], prm, s);
     double nx, ny;
     elem_normal(p, &nx, &ny);
     tb.x[off + v] = p.mx;
@@ -345,7 +344,6 @@ near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npair
     geo_fill(g, e1, pr.i, r.u1, r.nu1, true, S, r.nu1, lane);
     __syncwarp();
     const double* p2 = g.param + 8 * (size_t)e2;
-    const ArcBase arc = arc_base(g.kind[e2], p2);  // elliptic arcs: no sincos per point
     for (int p = lane; p < r.n1; p += 32) {
       const double x = r.r1[3 * p], y = r.r1[3 * p + 1], w = r.r1[3 * p + 2];
       const int si = r.k1[p] & 0xffff;
@@ -353,7 +351,7 @@ near_kernel(DevGeom g, DevRules r, const NearPair* __restrict__ pairs, int npair
       for (int h = 0; h < 2; ++h) {
         const int a = si + h * r.nu1;
         const double t = h == 0 ? (1 - y) * x : 1 - x + y * x;
-        const ElemPt b = arc.ok ? arc_eval(arc, t) : elem_eval(g.kind[e2], p2, t);
+        const ElemPt b = elem_eval(g.kind[e2], p2, t);
         double n2x, n2y, re, im;
         elem_normal(b, &n2x, &n2y);
         near_point<KERNEL, MIXED, false, CK>(k, ki, kq, eq, kc, tab, S.x[a], S.y[a], S.nx[a],

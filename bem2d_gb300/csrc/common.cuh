@@ -143,43 +143,6 @@ __device__ __forceinline__ double elem_jac(const ElemPt& p) {
   return sqrt(p.dx * p.dx + p.dy * p.dy);
 }
 
-// Elliptic-arc element points at many local coordinates s of one element
-// (the self pair's trial side): angle(s) = A0 + s D, so cos / sin follow by
-// the addition theorem from cos / sin A0 (once per element) and the Taylor
-// series of cos / sin (s D) (|s D| <= |D| <= kArcFastMaxD: the terms kept
-// leave < 1e-17).  ok = false: the element is not an elliptic arc or its
-// angle range is too wide; use elem_eval.
-constexpr double kArcFastMaxD = 0.05;
-struct ArcBase {
-  double a, b, D, c0, s0;
-  bool ok;
-};
-__device__ __forceinline__ ArcBase arc_base(int kind, const double* p) {
-  ArcBase r{};
-  r.ok = false;
-  if (kind != BEM2D_ELEM_ELLIPSEARC) return r;
-  const double t1 = p[0], t2 = p[1], a = p[2], b = p[3], ta = p[4], tb = p[5];
-  r.a = a;
-  r.b = b;
-  r.D = (t2 - t1) * (tb - ta);
-  if (!(fabs(r.D) <= kArcFastMaxD)) return r;
-  sincos(ta + t1 * (tb - ta), &r.s0, &r.c0);
-  r.ok = true;
-  return r;
-}
-__device__ __forceinline__ ElemPt arc_eval(const ArcBase& B, double s) {
-  const double x = s * B.D, x2 = x * x;
-  const double sx = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040))));
-  const double cx = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320))));
-  const double co = B.c0 * cx - B.s0 * sx, si = B.s0 * cx + B.c0 * sx;
-  ElemPt r;
-  r.mx = B.a * co;
-  r.my = B.b * si;
-  r.dx = -B.a * B.D * si;
-  r.dy = B.b * B.D * co;
-  return r;
-}
-
 // PolBasis t^d / LinBasis (lib/bem2d_basistypes.h:28-62); all library bases
 // used here are real, so conj(phi) = phi.
 __device__ __forceinline__ double basis_eval(int kind, double param, double t) {
