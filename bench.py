@@ -232,15 +232,16 @@ def far_roofline(n, far_ms, fp32_peak, key=None):
     (16 N^2) plus their complex64 copy (8 N^2)."""
     flops = 100.0 * 25 * (n * n - 3 * n)
     ach = flops / (far_ms * 1e-3) / 1e12
+    traffic = TRAFFIC.get(key) if key else None
     return {"bound": "fp32", "kernel": "far_ff_kernel + deferred_ff_kernel",
             "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
             "peak_source": "bem2d_fma_peak: FP32 FMA throughput measured in this run "
                            "(MEASURED_PEAKS.json has no FP32 figure)",
-            "traffic": TRAFFIC.get(key) if key else None,
+            "traffic": traffic,
             "algorithmic_bytes": 24.0 * n * n,
-            "note": "N=%d; 25 (N^2-3N) evaluations x 100 flops per launch; traffic = ncu "
-                    "dram bytes read+write per far-field launch at this N (null: not captured)"
-                    % n}
+            "note": "N=%d; 25 (N^2-3N) evaluations x 100 flops per launch; %s"
+                    % (n, "traffic = ncu dram bytes read+write per far-field launch at this N"
+                       if traffic is not None else "traffic not captured at this N")}
 
 
 def lu_roofline(n, lu_ms, peaks):
