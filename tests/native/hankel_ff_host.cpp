@@ -53,3 +53,15 @@ extern "C" void bessel01_ff_host(int n, const double* x, double* out) {
 extern "C" void log_ff_host(int n, const double* x, double* out) {
   for (int i = 0; i < n; ++i) out[i] = ff_to_double(ff_log(ff_from_double(x[i])));
 }
+
+// out[2i], out[2i+1] = ff_dot2(a, b, c, d) for in[8i..8i+7] = a.hi, a.lo,
+// b.hi, b.lo, c.hi, c.lo, d.hi, d.lo
+extern "C" void dot2_ff_host(int n, const float* in, float* out) {
+  for (int i = 0; i < n; ++i) {
+    const float* v = in + 8 * i;
+    const ff r = ff_dot2(ff_make(v[0], v[1]), ff_make(v[2], v[3]), ff_make(v[4], v[5]),
+                         ff_make(v[6], v[7]));
+    out[2 * i] = r.hi;
+    out[2 * i + 1] = r.lo;
+  }
+}

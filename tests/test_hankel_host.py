@@ -94,6 +94,7 @@ def hkff(tmp_path_factory):
         return o
     f.bessel = b
     f.log = lg
+    f.path = out
     return f
 
 
@@ -143,3 +144,42 @@ def test_float_float_against_mpmath(hkff):
     e0 = np.abs(h0 - r0) / np.abs(r0) / bound
     e1 = np.abs(h1 - r1) / np.abs(r1) / bound
     assert e0.max() < 1 and e1.max() < 1, (e0.max(), e1.max())
+
+
+def test_float_float_dot2_against_exact(hkff):
+    """ff_dot2(a, b, c, d) = a b + c d in float-float (the far field's complex
+    products, normal factors and squared distance): within 2^-46 (|a b| +
+    |c d|) of the exact value of the float-float inputs (rational
+    arithmetic), including near-total cancellation, and the result
+    normalised (|lo| <= ulp(hi))."""
+    from fractions import Fraction
+    lib = ctypes.CDLL(hkff.path)
+    rng = np.random.default_rng(11)
+    n = 4000
+
+    def ffs(m):
+        hi = (rng.standard_normal(m) * 10.0 ** rng.uniform(-3, 3, m)).astype(np.float32)
+        lo = (hi.astype(np.float64) * rng.uniform(-2 ** -25, 2 ** -25, m)).astype(np.float32)
+        return hi, lo
+    a, b, c, d = ffs(n), ffs(n), ffs(n), ffs(n)
+    # a quarter of the cases: c d = -a b up to the low parts (cancellation)
+    k = n // 4
+    c[0][:k], c[1][:k] = -a[0][:k], np.zeros(k, dtype=np.float32)
+    d[0][:k], d[1][:k] = b[0][:k], (b[0][:k].astype(np.float64) * 2 ** -30).astype(np.float32)
+    v = np.stack([a[0], a[1], b[0], b[1], c[0], c[1], d[0], d[1]], axis=1).astype(np.float32)
+    v = np.ascontiguousarray(v)
+    out = np.zeros((n, 2), dtype=np.float32)
+    lib.dot2_ff_host(ctypes.c_int(n), v.ctypes.data_as(ctypes.c_void_p),
+                     out.ctypes.data_as(ctypes.c_void_p))
+    worst = 0.0
+    for i in range(n):
+        F = [Fraction(float(x)) for x in v[i]]
+        ab = (F[0] + F[1]) * (F[2] + F[3])
+        cd = (F[4] + F[5]) * (F[6] + F[7])
+        exact = ab + cd
+        got = Fraction(float(out[i, 0])) + Fraction(float(out[i, 1]))
+        scale = abs(ab) + abs(cd)
+        if scale:
+            worst = max(worst, float(abs(got - exact) / scale))
+        assert abs(float(out[i, 1])) <= np.spacing(np.float32(abs(out[i, 0]))) or out[i, 0] == 0
+    assert worst <= 2.0 ** -46, worst
