@@ -33,6 +33,21 @@ def test_exports_every_declared_symbol(lib):
     assert sorted(capi.EXPORTS) == names
 
 
+def test_binding_constants_match_header():
+    """The ctypes binding's kernel, functional and precision codes are the
+    header's #defines (no library load needed)."""
+    from bem2d_gb300 import capi
+    src = open(HEADER).read()
+    defs = {m.group(1): int(m.group(2))
+            for m in re.finditer(r"#define\s+(BEM2D_\w+)\s+(-?\d+)", src)}
+    for table, prefix in ((capi.KERNEL, "BEM2D_KERNEL_"), (capi.FUN, "BEM2D_FUN_"),
+                          (capi.PREC, "BEM2D_PREC_")):
+        names = {k: v for k, v in defs.items() if k.startswith(prefix)}
+        assert sorted(table.values()) == sorted(names.values()), (prefix, table, names)
+        for key, code in table.items():
+            assert defs[prefix + key.upper()] == code, (prefix, key)
+
+
 def test_noalloc_layout_fits_at_the_limit(lib):
     """The allocation-free solve's work buffers for n = BEM2D_NOALLOC_MAX_N
     fit its static device array (host-side arithmetic only)."""
