@@ -87,3 +87,19 @@ def test_sm103a_code_in_library(lib):
         pytest.skip("cuobjdump not available")
     out = subprocess.run([tool, "--list-elf", capi.LIB_PATH], capture_output=True, text=True).stdout
     assert "sm_103a" in out
+
+
+def test_leading_dimension_of_torch_views():
+    """The binding's leading dimension for column-major torch views (the
+    solve and assembly entry points take it from the tensor): a transposed
+    contiguous tensor, a padded buffer's transposed view, and row-major
+    storage read as the transpose; numpy arrays are taken as n."""
+    torch = pytest.importorskip("torch")
+    from bem2d_gb300 import capi
+    n = 5
+    a = torch.zeros((n, n), dtype=torch.complex128)
+    assert capi._ld(a.T.contiguous().T, n) == n
+    buf = torch.zeros((n, n + 7), dtype=torch.complex128)
+    assert capi._ld(buf.t(), n) == n + 7
+    assert capi._ld(a, n) == n
+    assert capi._ld(np.zeros((n, n), order="F"), n) == n
