@@ -84,8 +84,6 @@ __host__ __device__ __forceinline__ ff ff_add(ff a, ff b) {
   return fast_two_sum(s.hi, s.lo);
 }
 
-__host__ __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
-
 // addition without the low-part two-sum: accurate unless a and b nearly cancel
 __host__ __device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
   ff s = two_sum(a.hi, b.hi);
@@ -173,14 +171,6 @@ __host__ __device__ __forceinline__ ff ff_rsqrt(ff a) {
   const ff ay2 = ff_mul(a, y2);
   const float e = (1.0f - ay2.hi) - ay2.lo;  // 1 - a y^2, small
   return fast_two_sum(y, 0.5f * y * e);
-}
-
-// sqrt(a) = a * rsqrt(a)
-__host__ __device__ __forceinline__ ff ff_sqrt(ff a) {
-  const float y = sqrtf(a.hi);
-  const ff y2 = two_prod(y, y);
-  const ff d = ff_sub(a, y2);  // a - y^2, small
-  return fast_two_sum(y, d.hi / (2.0f * y));
 }
 
 // 1/a: single-precision seed, one Newton step in ff
